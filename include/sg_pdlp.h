@@ -1,0 +1,157 @@
+/* C ABI of the GB300 PDLP engine (samaya_gb300).
+ *
+ * Drop-in boundary for samaya's PDLP path. Every function is extern "C", takes plain pointers
+ * and sizes, never throws and returns an int status: SG_OK (0) or a negative SG_ERR_* code.
+ * Host buffers belong to the caller; device memory belongs to the engine handle. One handle is
+ * used by one host thread at a time; distinct handles are independent.
+ *
+ * The problem is samaya's LpProblem (reference src/lp/simplex.hpp:18-26): the computational form
+ *     min cost'v  s.t.  [A -I] v = 0,  lower <= v <= upper,  v = (x, r),
+ * with A (m x n) in CSC form (int64 column starts, int32 row indices, float64 values) and
+ * cost/lower/upper of n + m entries (infinite bounds as +-INFINITY). Solutions are returned in
+ * the LpProblem's space, exactly as samaya::solve_pdlp returns them.
+ */
+#ifndef SG_PDLP_H
+#define SG_PDLP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes of a solve: the values of samaya::SimplexStatus (reference
+ * src/lp/simplex.hpp:28-35). */
+enum {
+  SG_STATUS_OPTIMAL = 0,
+  SG_STATUS_INFEASIBLE = 1,
+  SG_STATUS_UNBOUNDED = 2,
+  SG_STATUS_ITERATION_LIMIT = 3,
+  SG_STATUS_TIME_LIMIT = 4,
+  SG_STATUS_NUMERICAL_ERROR = 5
+};
+
+/* Error codes returned by the functions. */
+enum {
+  SG_OK = 0,
+  SG_ERR_INVALID_ARGUMENT = -1,
+  SG_ERR_NO_DEVICE = -2,
+  SG_ERR_CUDA = -3,
+  SG_ERR_OUT_OF_MEMORY = -4,
+  SG_ERR_TOO_LARGE = -5,
+  SG_ERR_INTERNAL = -6,
+  SG_ERR_NOT_READY = -7
+};
+
+/* Precision of the iterations. */
+enum {
+  SG_PRECISION_FP64 = 0,         /* FP64 storage and arithmetic (the reference's precision) */
+  SG_PRECISION_FP32_REFINED = 1  /* FP32 A and iterates, FP64 residuals + outer refinement */
+};
+
+typedef struct sg_pdlp sg_pdlp;
+
+/* Options: the fields of samaya::PdlpOptions (reference src/lp/pdlp.hpp:11-16) plus the
+ * engine's own. */
+typedef struct sg_pdlp_opts {
+  double tol;                /* relative primal, dual and gap tolerance (default 1e-8) */
+  long long max_iterations;  /* -1: automatic, max(1e4, 1e3 (m + n)), as the reference */
+  double time_limit;         /* seconds; <= 0: none */
+  int precision;             /* SG_PRECISION_* */
+  int refine_max_rounds;     /* outer refinement rounds of the FP32 path (default 6) */
+  double inner_tol;          /* tolerance of each FP32 inner solve (default 1e-4) */
+  int verbose;               /* 0 silent */
+} sg_pdlp_opts;
+
+/* Result: the scalars of samaya::PdlpResult (reference src/lp/pdlp.hpp:19-30) plus counters. */
+typedef struct sg_pdlp_result {
+  int status;               /* SG_STATUS_* */
+  long long iterations;     /* PDHG iterations (all refinement rounds for the FP32 path) */
+  double primal_residual;   /* relative, as the reference defines them (pdlp.cpp:493-519) */
+  double dual_residual;
+  double gap;
+  double primal_objective;  /* of the LpProblem (cost'v) at the answer */
+  double dual_objective;
+  long long restarts;
+  long long evaluations;
+  int refinement_rounds;
+  int has_dual_ray;         /* a Farkas certificate was written (status infeasible) */
+  int has_primal_ray;       /* an improving ray was written (status unbounded) */
+  double setup_seconds;
+  double solve_seconds;
+  double step_size;         /* 0.99 / ||[A -I]|| estimate */
+  double primal_weight;     /* final omega */
+  long long kernel_launches;
+} sg_pdlp_result;
+
+/* Fills the defaults (tol 1e-8, automatic iteration limit, no time limit, FP64). */
+void sg_pdlp_default_opts(sg_pdlp_opts* opts);
+
+/* Whether a usable GB300 (sm_103) is present; writes its compute capability and name.
+ * Replaces gpu::gpu_available / gpu::device_name (reference src/gpu/device.hpp:34-63) behind
+ * samaya::gpu_info (src/gpu/info.cpp:12-19). Returns SG_OK or SG_ERR_NO_DEVICE. */
+int sg_pdlp_available(int* cc_major, int* cc_minor, char* name, size_t name_len);
+
+/* Uploads an LpProblem and prepares the engine. Replaces gpu::PdhgDevice::create (reference
+ * src/gpu/pdhg_core.cu:242-273) for the solve_pdlp path: the matrix given here is the
+ * LpProblem's A before PDLP's own equilibration, which the engine performs on the device.
+ * Matrices with 2^31 - 1 or more nonzeros are refused (SG_ERR_TOO_LARGE), as the reference
+ * refuses them (pdhg_core.cu:176-178). */
+int sg_pdlp_create(sg_pdlp** handle, int m, int n, const int64_t* a_colptr,
+                   const int32_t* a_rowidx, const double* a_val, const double* cost,
+                   const double* lower, const double* upper, const sg_pdlp_opts* opts);
+
+/* Runs PDLP: samaya::solve_pdlp (reference src/lp/pdlp.cpp:228-1193) with use_gpu. Writes x
+ * (n + m), y (m), and when the status carries one the Farkas ray (m) or the improving ray (n);
+ * any output pointer may be NULL. Deterministic: a re-run gives the same bits. */
+int sg_pdlp_solve(sg_pdlp* handle, sg_pdlp_result* result, double* x, double* y,
+                  double* dual_ray, double* primal_ray);
+
+void sg_pdlp_destroy(sg_pdlp* handle);
+
+/* Message of an error code, and the last error message of this thread. */
+const char* sg_pdlp_error_string(int code);
+const char* sg_pdlp_last_error(void);
+
+/* One-call solve of an LpProblem (create + solve + destroy). */
+int sg_pdlp_solve_problem(int m, int n, const int64_t* a_colptr, const int32_t* a_rowidx,
+                          const double* a_val, const double* cost, const double* lower,
+                          const double* upper, const sg_pdlp_opts* opts, sg_pdlp_result* result,
+                          double* x, double* y, double* dual_ray, double* primal_ray);
+
+/* ---- Inner seam: the counterpart of the reference's gpu::PdhgDevice
+ * (src/gpu/pdhg_core.hpp:24-79), for kernel-level parity. The handle must come from
+ * sg_pdhg_create, whose problem is used as already equilibrated. which: 0 current (v_new,
+ * y_new), 1 average. Only theta = 1 (the reference's value) is supported. */
+int sg_pdhg_create(sg_pdlp** handle, int m, int n, const int64_t* a_colptr,
+                   const int32_t* a_rowidx, const double* a_val, const double* cost,
+                   const double* lower, const double* upper);
+/* PdhgDevice::set_original (pdhg_core.cu:307-318). */
+int sg_pdhg_set_original(sg_pdlp* handle, const double* col_scale, const double* row_scale,
+                         const double* cost, const double* lower, const double* upper);
+/* PdhgDevice::step (pdhg_core.cu:275-292). */
+int sg_pdhg_step(sg_pdlp* handle, double tau, double sigma, double theta, long long iter);
+/* PdhgDevice::advance (pdhg_core.cu:294-299). */
+int sg_pdhg_advance(sg_pdlp* handle);
+/* PdhgDevice::evaluate (pdhg_core.cu:320-346): sums[7] = primal_sq, dual_sq, primal_obj,
+ * dual_obj, x_sq, r_sq, y_sq. */
+int sg_pdhg_evaluate(sg_pdlp* handle, int which, double* sums);
+/* PdhgDevice::restart_distance (pdhg_core.cu:348-360). */
+int sg_pdhg_restart_distance(sg_pdlp* handle, int which, double* dv_sq, double* dy_sq);
+/* PdhgDevice::restart_to (pdhg_core.cu:362-380). */
+int sg_pdhg_restart_to(sg_pdlp* handle, int which);
+/* PdhgDevice::download (pdhg_core.cu:382-402); any pointer may be NULL. */
+int sg_pdhg_download(sg_pdlp* handle, double* v, double* v_new, double* y, double* y_new,
+                     double* v_erg, double* y_erg);
+
+/* y = A x (transpose = 0, x: n, y: m) or y = A'x (transpose = 1) with the engine's
+ * load-balanced tile kernel on the uploaded values; replaces gpu::csr_spmv (reference
+ * src/gpu/spmv.cu:91-120) for the parity tests. */
+int sg_spmv(sg_pdlp* handle, int transpose, const double* x, double* y);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SG_PDLP_H */

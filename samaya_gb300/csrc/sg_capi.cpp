@@ -1,0 +1,224 @@
+// extern "C" entry points of the GB300 PDLP engine (include/sg_pdlp.h). No exception crosses
+// this layer: every error becomes a negative code plus a thread-local message.
+#include <math.h>
+#include <string.h>
+
+#include <exception>
+#include <new>
+#include <string>
+
+#include "../../include/sg_pdlp.h"
+#include "sg_engine.cuh"
+
+struct sg_pdlp {
+  sg::Engine* engine = nullptr;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& message) {
+  g_last_error = message;
+  return code;
+}
+
+sg::Options to_options(const sg_pdlp_opts* o) {
+  sg::Options opt;
+  sg_pdlp_opts d;
+  sg_pdlp_default_opts(&d);
+  if (o == nullptr) o = &d;
+  opt.tol = o->tol > 0 ? o->tol : 1e-8;
+  opt.max_iterations = o->max_iterations;
+  opt.time_limit = o->time_limit;
+  opt.precision = o->precision;
+  opt.refine_max_rounds = o->refine_max_rounds > 0 ? o->refine_max_rounds : 6;
+  opt.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
+  opt.verbose = o->verbose;
+  return opt;
+}
+
+}  // namespace
+
+extern "C" {
+
+void sg_pdlp_default_opts(sg_pdlp_opts* opts) {
+  if (opts == nullptr) return;
+  memset(opts, 0, sizeof(*opts));
+  opts->tol = 1e-8;
+  opts->max_iterations = -1;
+  opts->time_limit = 0.0;
+  opts->precision = SG_PRECISION_FP64;
+  opts->refine_max_rounds = 6;
+  opts->inner_tol = 1e-4;
+  opts->verbose = 0;
+}
+
+int sg_pdlp_available(int* cc_major, int* cc_minor, char* name, size_t name_len) {
+  try {
+    const int rc = sg::device_info(cc_major, cc_minor, name, name_len);
+    if (rc != sg::kOk) return fail(SG_ERR_NO_DEVICE, "no usable sm_103 GPU");
+    return SG_OK;
+  } catch (...) {
+    return fail(SG_ERR_INTERNAL, "unexpected exception");
+  }
+}
+
+int sg_pdlp_create(sg_pdlp** handle, int m, int n, const int64_t* a_colptr,
+                   const int32_t* a_rowidx, const double* a_val, const double* cost,
+                   const double* lower, const double* upper, const sg_pdlp_opts* opts) {
+  if (handle == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "handle is NULL");
+  *handle = nullptr;
+  try {
+    std::string why;
+    sg::Engine* e = nullptr;
+    const int rc = sg::Engine::create(&e, m, n, a_colptr, a_rowidx, a_val, cost, lower, upper,
+                                      to_options(opts), &why);
+    if (rc != sg::kOk) return fail(rc, why);
+    *handle = new sg_pdlp{e};
+    return SG_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(SG_ERR_OUT_OF_MEMORY, "host allocation failed");
+  } catch (const std::exception& ex) {
+    return fail(SG_ERR_INTERNAL, ex.what());
+  } catch (...) {
+    return fail(SG_ERR_INTERNAL, "unexpected exception");
+  }
+}
+
+int sg_pdlp_solve(sg_pdlp* handle, sg_pdlp_result* result, double* x, double* y,
+                  double* dual_ray, double* primal_ray) {
+  if (handle == nullptr || handle->engine == nullptr || result == nullptr) {
+    return fail(SG_ERR_INVALID_ARGUMENT, "NULL handle or result");
+  }
+  try {
+    memset(result, 0, sizeof(*result));
+    sg::SolveInfo info;
+    std::string why;
+    const int rc = handle->engine->solve(&info, x, y, dual_ray, primal_ray, &why);
+    if (rc != sg::kOk) {
+      result->status = SG_STATUS_NUMERICAL_ERROR;
+      return fail(rc, why);
+    }
+    result->status = info.status;
+    result->iterations = info.iterations;
+    result->primal_residual = info.rel_primal;
+    result->dual_residual = info.rel_dual;
+    result->gap = info.rel_gap;
+    result->primal_objective = info.primal_obj;
+    result->dual_objective = info.dual_obj;
+    result->restarts = info.restarts;
+    result->evaluations = info.evaluations;
+    result->refinement_rounds = info.refinement_rounds;
+    result->has_dual_ray = info.has_dual_ray;
+    result->has_primal_ray = info.has_primal_ray;
+    result->setup_seconds = info.setup_seconds;
+    result->solve_seconds = info.solve_seconds;
+    result->step_size = info.step_size;
+    result->primal_weight = info.omega;
+    result->kernel_launches = info.kernel_launches;
+    return SG_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(SG_ERR_OUT_OF_MEMORY, "host allocation failed");
+  } catch (const std::exception& ex) {
+    return fail(SG_ERR_INTERNAL, ex.what());
+  } catch (...) {
+    return fail(SG_ERR_INTERNAL, "unexpected exception");
+  }
+}
+
+void sg_pdlp_destroy(sg_pdlp* handle) {
+  if (handle == nullptr) return;
+  try {
+    delete handle->engine;
+  } catch (...) {
+  }
+  delete handle;
+}
+
+const char* sg_pdlp_error_string(int code) {
+  switch (code) {
+    case SG_OK: return "ok";
+    case SG_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case SG_ERR_NO_DEVICE: return "no usable GPU";
+    case SG_ERR_CUDA: return "CUDA error";
+    case SG_ERR_OUT_OF_MEMORY: return "out of memory";
+    case SG_ERR_TOO_LARGE: return "problem too large for 32-bit offsets";
+    case SG_ERR_INTERNAL: return "internal error";
+    case SG_ERR_NOT_READY: return "handle not ready for this call";
+    default: return "unknown error";
+  }
+}
+
+const char* sg_pdlp_last_error(void) { return g_last_error.c_str(); }
+
+int sg_pdlp_solve_problem(int m, int n, const int64_t* a_colptr, const int32_t* a_rowidx,
+                          const double* a_val, const double* cost, const double* lower,
+                          const double* upper, const sg_pdlp_opts* opts, sg_pdlp_result* result,
+                          double* x, double* y, double* dual_ray, double* primal_ray) {
+  sg_pdlp* h = nullptr;
+  int rc = sg_pdlp_create(&h, m, n, a_colptr, a_rowidx, a_val, cost, lower, upper, opts);
+  if (rc != SG_OK) return rc;
+  rc = sg_pdlp_solve(h, result, x, y, dual_ray, primal_ray);
+  sg_pdlp_destroy(h);
+  return rc;
+}
+
+int sg_pdhg_create(sg_pdlp** handle, int m, int n, const int64_t* a_colptr,
+                   const int32_t* a_rowidx, const double* a_val, const double* cost,
+                   const double* lower, const double* upper) {
+  sg_pdlp_opts o;
+  sg_pdlp_default_opts(&o);
+  return sg_pdlp_create(handle, m, n, a_colptr, a_rowidx, a_val, cost, lower, upper, &o);
+}
+
+#define SG_SEAM(call)                                                        \
+  do {                                                                       \
+    if (handle == nullptr || handle->engine == nullptr)                      \
+      return fail(SG_ERR_INVALID_ARGUMENT, "NULL handle");                   \
+    try {                                                                    \
+      const int rc_ = (call);                                                \
+      if (rc_ != sg::kOk) return fail(rc_, sg_pdlp_error_string(rc_));       \
+      return SG_OK;                                                          \
+    } catch (...) {                                                          \
+      return fail(SG_ERR_INTERNAL, "unexpected exception");                  \
+    }                                                                        \
+  } while (0)
+
+int sg_pdhg_set_original(sg_pdlp* handle, const double* col_scale, const double* row_scale,
+                         const double* cost, const double* lower, const double* upper) {
+  SG_SEAM(handle->engine->seam_set_original(col_scale, row_scale, cost, lower, upper));
+}
+
+int sg_pdhg_step(sg_pdlp* handle, double tau, double sigma, double theta, long long iter) {
+  if (theta != 1.0) return fail(SG_ERR_INVALID_ARGUMENT, "only theta = 1 is supported");
+  SG_SEAM(handle->engine->seam_step(tau, sigma, iter));
+}
+
+int sg_pdhg_advance(sg_pdlp* handle) { SG_SEAM(handle->engine->seam_advance()); }
+
+int sg_pdhg_evaluate(sg_pdlp* handle, int which, double* sums) {
+  if (sums == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "sums is NULL");
+  SG_SEAM(handle->engine->seam_evaluate(which, sums));
+}
+
+int sg_pdhg_restart_distance(sg_pdlp* handle, int which, double* dv_sq, double* dy_sq) {
+  if (dv_sq == nullptr || dy_sq == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "NULL output");
+  SG_SEAM(handle->engine->seam_restart_distance(which, dv_sq, dy_sq));
+}
+
+int sg_pdhg_restart_to(sg_pdlp* handle, int which) {
+  SG_SEAM(handle->engine->seam_restart_to(which));
+}
+
+int sg_pdhg_download(sg_pdlp* handle, double* v, double* v_new, double* y, double* y_new,
+                     double* v_erg, double* y_erg) {
+  SG_SEAM(handle->engine->seam_download(v, v_new, y, y_new, v_erg, y_erg));
+}
+
+int sg_spmv(sg_pdlp* handle, int transpose, const double* x, double* y) {
+  if (x == nullptr || y == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "NULL vector");
+  SG_SEAM(handle->engine->spmv(transpose, x, y));
+}
+
+}  // extern "C"

@@ -1,0 +1,826 @@
+// Host engine of the GB300 PDLP path (see sg_engine.cuh).
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <limits>
+#include <random>
+#include <type_traits>
+
+#include "sg_engine.cuh"
+
+namespace sg {
+
+namespace {
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+  *p = nullptr;
+  return cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(count, 1) * sizeof(T));
+}
+
+template <typename T>
+void dfree(T*& p) {
+  if (p != nullptr) cudaFree(p);
+  p = nullptr;
+}
+
+// The power iteration's start vector, as the reference draws it (pdlp.cpp:47-51):
+// std::mt19937_64(12345) through std::uniform_real_distribution<double>(-1, 1).
+std::vector<double> power_start(int m) {
+  std::vector<double> u(static_cast<size_t>(m));
+  std::mt19937_64 rng(12345);
+  std::uniform_real_distribution<double> dist(-1.0, 1.0);
+  for (int i = 0; i < m; ++i) u[i] = dist(rng);
+  return u;
+}
+
+}  // namespace
+
+// Tiles: consecutive rows while the tile holds at most tile_nnz nonzeros and tile_rows rows; a
+// row longer than tile_nnz becomes ceil(len / tile_nnz) segment tiles of its own.
+void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, std::vector<Tile>* out,
+                 int* nlong) {
+  out->clear();
+  *nlong = 0;
+  const int rows = static_cast<int>(ptr.size()) - 1;
+  int r = 0;
+  while (r < rows) {
+    const int len = ptr[r + 1] - ptr[r];
+    if (len > tile_nnz) {
+      const int nseg = (len + tile_nnz - 1) / tile_nnz;
+      for (int s = 0; s < nseg; ++s) {
+        Tile t{};
+        t.r0 = r;
+        t.r1 = r + 1;
+        t.k0 = ptr[r] + s * tile_nnz;
+        t.k1 = std::min(ptr[r + 1], t.k0 + tile_nnz);
+        t.kind = 1;
+        t.team = 32;
+        t.seg = s;
+        t.nseg = nseg;
+        t.lrow = *nlong;
+        out->push_back(t);
+      }
+      ++*nlong;
+      ++r;
+      continue;
+    }
+    const int r0 = r;
+    while (r < rows && r - r0 < tile_rows) {
+      const int l = ptr[r + 1] - ptr[r];
+      if (l > tile_nnz) break;
+      if (ptr[r + 1] - ptr[r0] > tile_nnz) break;
+      ++r;
+    }
+    Tile t{};
+    t.r0 = r0;
+    t.r1 = r;
+    t.k0 = ptr[r0];
+    t.k1 = ptr[r];
+    t.kind = 0;
+    const double mean = static_cast<double>(t.k1 - t.k0) / std::max(1, r - r0);
+    int team = 1;
+    while (team < 32 && team < mean) team *= 2;
+    t.team = team;
+    t.seg = 0;
+    t.nseg = 1;
+    t.lrow = -1;
+    out->push_back(t);
+  }
+}
+
+int device_info(int* major, int* minor, char* name, size_t len) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+    cudaGetLastError();
+    return kErrNoDevice;
+  }
+  int dev = 0;
+  cudaDeviceProp prop;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return kErrNoDevice;
+  }
+  if (major) *major = prop.major;
+  if (minor) *minor = prop.minor;
+  if (name && len > 0) {
+    strncpy(name, prop.name, len - 1);
+    name[len - 1] = '\0';
+  }
+  // The kernels are built for sm_103a only.
+  if (prop.major * 10 + prop.minor != 103) return kErrNoDevice;
+  return kOk;
+}
+
+Engine::~Engine() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  if (chunk_exec_) cudaGraphExecDestroy(chunk_exec_);
+  if (chunk_graph_) cudaGraphDestroy(chunk_graph_);
+  for (DevOp* op : {&K_, &Kt_}) {
+    dfree(op->ptr);
+    dfree(op->idx);
+    dfree(op->val);
+    dfree(op->val_orig);
+    dfree(op->val32);
+    dfree(op->tiles);
+    dfree(op->seg_part);
+    dfree(op->lcount);
+  }
+  for (double** p : {&it64_.V[0], &it64_.V[1], &it64_.Vbar, &it64_.Y[0], &it64_.Y[1],
+                     &it64_.Verg, &it64_.Yerg, &it64_.Vrst, &it64_.Yrst, &it64_.cost,
+                     &it64_.lower, &it64_.upper, &it64_.rhs}) {
+    dfree(*p);
+  }
+  for (float** p : {&it32_.V[0], &it32_.V[1], &it32_.Vbar, &it32_.Y[0], &it32_.Y[1],
+                    &it32_.Verg, &it32_.Yerg, &it32_.Vrst, &it32_.Yrst, &it32_.cost,
+                    &it32_.lower, &it32_.upper, &it32_.rhs}) {
+    dfree(*p);
+  }
+  for (double** p : {&cost_orig_, &lower_orig_, &upper_orig_, &cost_ev_, &lower_ev_, &upper_ev_,
+                     &rhs_ev_, &cs_, &rs_, &cn_, &rn_, &pu_, &pv_, &u0_, &scratch_n_, &x_out_,
+                     &y_out_, &ray_out_, &partial_, &long_terms_}) {
+    dfree(*p);
+  }
+  dfree(counter_);
+  dfree(ctl_);
+  if (ctl_host_) cudaFreeHost(ctl_host_);
+  for (auto& e : ev_) {
+    if (e) cudaEventDestroy(e);
+  }
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+int Engine::check(cudaError_t e, const char* what) {
+  (void)what;
+  if (e == cudaSuccess) return kOk;
+  return e == cudaErrorMemoryAllocation ? kErrOutOfMemory : kErrCuda;
+}
+
+#define SG_TRY(call)                        \
+  do {                                      \
+    const cudaError_t e_ = (call);          \
+    if (e_ != cudaSuccess) {                \
+      if (err) *err = std::string(#call) + ": " + cudaGetErrorString(e_); \
+      return e_ == cudaErrorMemoryAllocation ? kErrOutOfMemory : kErrCuda; \
+    }                                       \
+  } while (0)
+
+int Engine::create(Engine** out, int m, int n, const int64_t* colptr, const int32_t* rowidx,
+                   const double* val, const double* cost, const double* lower,
+                   const double* upper, const Options& opt, std::string* err) {
+  *out = nullptr;
+  if (m < 0 || n < 0 || colptr == nullptr || cost == nullptr || lower == nullptr ||
+      upper == nullptr) {
+    if (err) *err = "invalid argument";
+    return kErrInvalidArgument;
+  }
+  const long long nnz = colptr[n];
+  if (nnz < 0 || colptr[0] != 0) {
+    if (err) *err = "column starts must begin at 0";
+    return kErrInvalidArgument;
+  }
+  if (nnz >= static_cast<long long>(std::numeric_limits<int>::max()) ||
+      static_cast<long long>(n) + m >= std::numeric_limits<int>::max()) {
+    if (err) *err = "matrix too large for 32-bit offsets";
+    return kErrTooLarge;
+  }
+  if (nnz > 0 && (rowidx == nullptr || val == nullptr)) {
+    if (err) *err = "null matrix arrays";
+    return kErrInvalidArgument;
+  }
+  for (int j = 0; j < n; ++j) {
+    if (colptr[j + 1] < colptr[j]) {
+      if (err) *err = "column starts must not decrease";
+      return kErrInvalidArgument;
+    }
+  }
+  for (long long p = 0; p < nnz; ++p) {
+    if (rowidx[p] < 0 || rowidx[p] >= m) {
+      if (err) *err = "row index out of range";
+      return kErrInvalidArgument;
+    }
+    if (!std::isfinite(val[p])) {
+      if (err) *err = "matrix value not finite";
+      return kErrInvalidArgument;
+    }
+  }
+  for (long long k = 0; k < static_cast<long long>(n) + m; ++k) {
+    if (!std::isfinite(cost[k]) || std::isnan(lower[k]) || std::isnan(upper[k])) {
+      if (err) *err = "cost or bound not valid";
+      return kErrInvalidArgument;
+    }
+  }
+  int dev_major = 0, dev_minor = 0;
+  if (device_info(&dev_major, &dev_minor, nullptr, 0) != kOk) {
+    if (err) *err = "no sm_103 GPU";
+    return kErrNoDevice;
+  }
+  Engine* e = new Engine();
+  e->m_ = m;
+  e->n_ = n;
+  e->nnz_ = nnz;
+  e->opt_ = opt;
+  e->fp32_ = opt.precision == 1;
+  // K' = A^T by rows is the CSC of A; K = A by rows, by a stable counting sort.
+  std::vector<int> tptr(static_cast<size_t>(n) + 1);
+  for (int j = 0; j <= n; ++j) tptr[j] = static_cast<int>(colptr[j]);
+  std::vector<int> kptr(static_cast<size_t>(m) + 1, 0);
+  for (long long p = 0; p < nnz; ++p) ++kptr[rowidx[p] + 1];
+  for (int i = 0; i < m; ++i) kptr[i + 1] += kptr[i];
+  std::vector<int> kidx(static_cast<size_t>(std::max<long long>(nnz, 1)));
+  std::vector<double> kval(static_cast<size_t>(std::max<long long>(nnz, 1)));
+  {
+    std::vector<int> next(kptr.begin(), kptr.end() - 1);
+    for (int j = 0; j < n; ++j) {
+      for (long long p = colptr[j]; p < colptr[j + 1]; ++p) {
+        const int q = next[rowidx[p]]++;
+        kidx[q] = j;
+        kval[q] = val[p];
+      }
+    }
+  }
+  e->K_.rows = m;
+  e->K_.cols = n;
+  e->K_.nnz = nnz;
+  e->K_.host_ptr = kptr;
+  e->Kt_.rows = n;
+  e->Kt_.cols = m;
+  e->Kt_.nnz = nnz;
+  e->Kt_.host_ptr = tptr;
+  std::string why;
+  int rc = e->alloc_all(&why);
+  if (rc != kOk) {
+    if (err) *err = why;
+    delete e;
+    return rc;
+  }
+  cudaStream_t s = e->stream_;
+  const size_t nb = static_cast<size_t>(nnz);
+  const size_t nt = static_cast<size_t>(n) + m;
+  auto up = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    if (bytes == 0) return cudaSuccess;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+  };
+  cudaError_t ce = cudaSuccess;
+  ce = up(e->K_.ptr, kptr.data(), kptr.size() * sizeof(int));
+  if (ce == cudaSuccess) ce = up(e->K_.idx, kidx.data(), nb * sizeof(int));
+  if (ce == cudaSuccess) ce = up(e->K_.val_orig, kval.data(), nb * sizeof(double));
+  if (ce == cudaSuccess) ce = up(e->Kt_.ptr, tptr.data(), tptr.size() * sizeof(int));
+  if (ce == cudaSuccess) ce = up(e->Kt_.idx, rowidx, nb * sizeof(int));
+  if (ce == cudaSuccess) ce = up(e->Kt_.val_orig, val, nb * sizeof(double));
+  if (ce == cudaSuccess) ce = up(e->cost_orig_, cost, nt * sizeof(double));
+  if (ce == cudaSuccess) ce = up(e->lower_orig_, lower, nt * sizeof(double));
+  if (ce == cudaSuccess) ce = up(e->upper_orig_, upper, nt * sizeof(double));
+  std::vector<double> u0 = power_start(m);
+  if (ce == cudaSuccess) ce = up(e->u0_, u0.data(), u0.size() * sizeof(double));
+  // Tiles.
+  for (DevOp* op : {&e->K_, &e->Kt_}) {
+    std::vector<Tile> tiles;
+    int nlong = 0;
+    build_tiles(op->host_ptr, kTileNnz, kTileRows, &tiles, &nlong);
+    op->ntiles = static_cast<int>(tiles.size());
+    op->nlong = nlong;
+    if (ce == cudaSuccess) ce = dalloc(&op->tiles, tiles.size());
+    if (ce == cudaSuccess) ce = up(op->tiles, tiles.data(), tiles.size() * sizeof(Tile));
+    if (ce == cudaSuccess) ce = dalloc(&op->seg_part, tiles.size() * kMaxVec);
+    if (ce == cudaSuccess) ce = dalloc(&op->lcount, std::max(nlong, 1));
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(op->lcount, 0, std::max(nlong, 1) * sizeof(unsigned), s);
+  }
+  if (ce == cudaSuccess) {
+    const int maxlong = std::max(std::max(e->K_.nlong, e->Kt_.nlong), 1);
+    ce = dalloc(&e->long_terms_, static_cast<size_t>(maxlong) * kMaxSums);
+  }
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) {
+    if (err) *err = std::string("upload: ") + cudaGetErrorString(ce);
+    const int code = ce == cudaErrorMemoryAllocation ? kErrOutOfMemory : kErrCuda;
+    delete e;
+    return code;
+  }
+  // Grids: persistent CTAs for the evaluation kernels (2 per SM with 82 KB of shared memory);
+  // one CTA per tile for the step kernels.
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&e->sm_count_, cudaDevAttrMultiProcessorCount, dev);
+  const int eval_cap = e->sm_count_ * 2;
+  e->grid_k_ = std::max(1, std::min(e->K_.ntiles, eval_cap));
+  e->grid_t_ = std::max(1, std::min(e->Kt_.ntiles, eval_cap));
+  e->grid_step_k_ = std::max(1, std::min(e->K_.ntiles, 65535));
+  e->grid_step_t_ = std::max(1, std::min(e->Kt_.ntiles, 65535));
+  *out = e;
+  return kOk;
+}
+
+int Engine::alloc_all(std::string* err) {
+  const size_t nt = static_cast<size_t>(n_) + m_;
+  const size_t m = static_cast<size_t>(m_);
+  const size_t nb = static_cast<size_t>(nnz_);
+  SG_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  for (auto& ev : ev_) SG_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  for (DevOp* op : {&K_, &Kt_}) {
+    SG_TRY(dalloc(&op->ptr, static_cast<size_t>(op->rows) + 1));
+    SG_TRY(dalloc(&op->idx, nb));
+    SG_TRY(dalloc(&op->val, nb));
+    SG_TRY(dalloc(&op->val_orig, nb));
+    if (fp32_) SG_TRY(dalloc(&op->val32, nb));
+  }
+  for (double** p : {&it64_.V[0], &it64_.V[1], &it64_.Vbar, &it64_.Verg, &it64_.Vrst,
+                     &it64_.cost, &it64_.lower, &it64_.upper}) {
+    SG_TRY(dalloc(p, nt));
+  }
+  for (double** p : {&it64_.Y[0], &it64_.Y[1], &it64_.Yerg, &it64_.Yrst, &it64_.rhs}) {
+    SG_TRY(dalloc(p, m));
+  }
+  if (fp32_) {
+    for (float** p : {&it32_.V[0], &it32_.V[1], &it32_.Vbar, &it32_.Verg, &it32_.Vrst,
+                      &it32_.cost, &it32_.lower, &it32_.upper}) {
+      SG_TRY(dalloc(p, nt));
+    }
+    for (float** p : {&it32_.Y[0], &it32_.Y[1], &it32_.Yerg, &it32_.Yrst, &it32_.rhs}) {
+      SG_TRY(dalloc(p, m));
+    }
+  }
+  for (double** p : {&cost_orig_, &lower_orig_, &upper_orig_, &cost_ev_, &lower_ev_, &upper_ev_,
+                     &x_out_, &scratch_n_}) {
+    SG_TRY(dalloc(p, nt));
+  }
+  for (double** p : {&rhs_ev_, &rs_, &rn_, &pu_, &u0_, &y_out_, &ray_out_}) SG_TRY(dalloc(p, m));
+  for (double** p : {&cs_, &cn_, &pv_}) SG_TRY(dalloc(p, static_cast<size_t>(n_)));
+  SG_TRY(dalloc(&partial_, static_cast<size_t>(4096) * kMaxSums));
+  SG_TRY(dalloc(&counter_, 8));
+  SG_TRY(cudaMemsetAsync(counter_, 0, 8 * sizeof(unsigned), stream_));
+  SG_TRY(dalloc(&ctl_, 1));
+  SG_TRY(cudaMemsetAsync(ctl_, 0, sizeof(Ctl), stream_));
+  SG_TRY(cudaHostAlloc(reinterpret_cast<void**>(&ctl_host_), sizeof(Ctl), cudaHostAllocDefault));
+  memset(ctl_host_, 0, sizeof(Ctl));
+  configure_kernels();
+  return kOk;
+}
+
+template <typename T>
+IterView<T> Engine::iter_view(DevIter<T>& it) {
+  IterView<T> v;
+  v.V[0] = it.V[0];
+  v.V[1] = it.V[1];
+  v.Vbar = it.Vbar;
+  v.Y[0] = it.Y[0];
+  v.Y[1] = it.Y[1];
+  v.Verg = it.Verg;
+  v.Yerg = it.Yerg;
+  v.Vrst = it.Vrst;
+  v.Yrst = it.Yrst;
+  v.cost = it.cost;
+  v.lower = it.lower;
+  v.upper = it.upper;
+  v.rhs = nullptr;
+  v.n = n_;
+  v.m = m_;
+  return v;
+}
+
+EvalView Engine::eval_view() const {
+  EvalView ev;
+  ev.cs = cs_;
+  ev.rs = rs_;
+  ev.cost = cost_ev_;
+  ev.lower = lower_ev_;
+  ev.upper = upper_ev_;
+  ev.rhs = nullptr;
+  return ev;
+}
+
+RedView Engine::red_view() const {
+  RedView r;
+  r.partial = partial_;
+  r.counter = counter_;
+  r.long_terms = long_terms_;
+  return r;
+}
+
+// Device setup (pdlp.cpp:260-316, 377-394, 490-492): working values from the originals,
+// residual-scale constants, Ruiz, A_eq, scaled vectors, operator norm and step sizes; iterates
+// zeroed. Asynchronous on the engine's stream.
+int Engine::setup_device(const double* rhs_orig) {
+  (void)rhs_orig;
+  cudaStream_t s = stream_;
+  const size_t nt = static_cast<size_t>(n_) + m_;
+  const size_t nb = static_cast<size_t>(nnz_);
+  std::string* err = nullptr;
+  if (nb > 0) {
+    SG_TRY(cudaMemcpyAsync(K_.val, K_.val_orig, nb * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    SG_TRY(cudaMemcpyAsync(Kt_.val, Kt_.val_orig, nb * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
+  SG_TRY(cudaMemcpyAsync(cost_ev_, cost_orig_, nt * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  SG_TRY(cudaMemcpyAsync(lower_ev_, lower_orig_, nt * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  SG_TRY(cudaMemcpyAsync(upper_ev_, upper_orig_, nt * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  SG_TRY(cudaMemsetAsync(ctl_, 0, sizeof(Ctl), s));
+  // Constant fields of the control block.
+  Ctl h;
+  memset(&h, 0, sizeof(h));
+  h.m = m_;
+  h.n = n_;
+  h.tol = opt_.tol;
+  long long max_iter = opt_.max_iterations;
+  if (max_iter <= 0) {
+    // pdlp.cpp:365-373.
+    max_iter = std::max<long long>(10000LL, 10000LL * (static_cast<long long>(m_) + n_) / 10);
+    if (!(opt_.time_limit > 0)) max_iter = std::min<long long>(max_iter, 1000000LL);
+  }
+  h.max_iter = max_iter;
+  h.kkt_at_restart = INFINITY;
+  h.kkt_previous = INFINITY;
+  h.status = kRunning;
+  h.omega = 1.0;
+  SG_TRY(cudaMemcpyAsync(ctl_, &h, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+  SG_TRY(cudaStreamSynchronize(s));  // h lives on this stack frame
+  const OpView<double> K = K_.view64();
+  const OpView<double> Kt = Kt_.view64();
+  const RedView red = red_view();
+  // Scale factors start at 1.
+  {
+    std::vector<double> ones(std::max(nt, static_cast<size_t>(1)), 1.0);
+    SG_TRY(cudaMemcpyAsync(cs_, ones.data(), static_cast<size_t>(n_) * sizeof(double),
+                           cudaMemcpyHostToDevice, s));
+    SG_TRY(cudaMemcpyAsync(rs_, ones.data(), static_cast<size_t>(m_) * sizeof(double),
+                           cudaMemcpyHostToDevice, s));
+    SG_TRY(cudaStreamSynchronize(s));
+  }
+  launch_setup_norms(ctl_, K, Kt, cost_orig_, red, grid_k_, grid_t_, s);
+  if (m_ > 0 && n_ > 0) {
+    for (int pass = 0; pass < 10; ++pass) {
+      launch_ruiz_pass(ctl_, K, Kt, rs_, cs_, rn_, cn_, red, grid_k_, grid_t_, s);
+    }
+  }
+  launch_apply_scaling(K, Kt, rs_, cs_, nnz_, s);
+  launch_scale_vectors(n_, m_, cs_, rs_, cost_orig_, lower_orig_, upper_orig_, nullptr,
+                       it64_.cost, it64_.lower, it64_.upper, nullptr, s);
+  if (m_ > 0) {
+    SG_TRY(cudaMemcpyAsync(pu_, u0_, static_cast<size_t>(m_) * sizeof(double),
+                           cudaMemcpyDeviceToDevice, s));
+  }
+  launch_power_iteration(ctl_, K, Kt, pu_, pv_, red, 20, grid_k_, grid_t_, s);
+  // Iterates start at zero (pdlp.cpp:323-329).
+  for (double* p : {it64_.V[0], it64_.V[1], it64_.Vbar, it64_.Verg, it64_.Vrst}) {
+    SG_TRY(cudaMemsetAsync(p, 0, nt * sizeof(double), s));
+  }
+  for (double* p : {it64_.Y[0], it64_.Y[1], it64_.Yerg, it64_.Yrst}) {
+    SG_TRY(cudaMemsetAsync(p, 0, static_cast<size_t>(m_) * sizeof(double), s));
+  }
+  SG_TRY(cudaGetLastError());
+  return kOk;
+}
+
+// One chunk: kCheckFrequency fused iterations, the evaluation, the decisions, restart and
+// detection. Recorded once as a CUDA graph.
+void Engine::enqueue_chunk_body() {
+  cudaStream_t s = stream_;
+  const RedView red = red_view();
+  const EvalView ev = eval_view();
+  int kernels = 0;
+  if (fp32_) {
+    const OpView<float> K = K_.view32();
+    const OpView<float> Kt = Kt_.view32();
+    IterView<float> it = iter_view(it32_);
+    for (int j = 0; j < kCheckFrequency; ++j) {
+      launch_dual_step(ctl_, K, it, j, grid_step_k_, s);
+      launch_primal_step(ctl_, Kt, it, j, grid_step_t_, s);
+      kernels += 2;
+    }
+    launch_eval(ctl_, K, Kt, it, ev, red, grid_k_, grid_t_, -1, s);
+    launch_decide_a(ctl_, s);
+    launch_detect(ctl_, K, Kt, it, ev, red, scratch_n_, nullptr, grid_k_, grid_t_, s);
+    launch_decide_b(ctl_, s);
+    launch_restart(ctl_, it, s);
+  } else {
+    const OpView<double> K = K_.view64();
+    const OpView<double> Kt = Kt_.view64();
+    IterView<double> it = iter_view(it64_);
+    for (int j = 0; j < kCheckFrequency; ++j) {
+      launch_dual_step(ctl_, K, it, j, grid_step_k_, s);
+      launch_primal_step(ctl_, Kt, it, j, grid_step_t_, s);
+      kernels += 2;
+    }
+    launch_eval(ctl_, K, Kt, it, ev, red, grid_k_, grid_t_, -1, s);
+    launch_decide_a(ctl_, s);
+    launch_detect(ctl_, K, Kt, it, ev, red, scratch_n_, nullptr, grid_k_, grid_t_, s);
+    launch_decide_b(ctl_, s);
+    launch_restart(ctl_, it, s);
+  }
+  kernels += 2 + 1 + 6 + 1 + 1;
+  chunk_kernels_ = kernels;
+}
+
+int Engine::capture_chunk() {
+  if (chunk_exec_ != nullptr) return kOk;
+  std::string* err = nullptr;
+  SG_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+  enqueue_chunk_body();
+  SG_TRY(cudaStreamEndCapture(stream_, &chunk_graph_));
+  SG_TRY(cudaGraphInstantiate(&chunk_exec_, chunk_graph_, 0));
+  return kOk;
+}
+
+// Replays the chunk graph until the device says done, keeping a few chunks in flight; the
+// host only reads the status word back (an event per chunk).
+int Engine::run_loop(double deadline_s, SolveInfo* info) {
+  std::string* err = nullptr;
+  constexpr int kInflight = 3;
+  int head = 0;  // oldest in flight
+  int count = 0;
+  long long launches = 0;
+  // Every chunk advances the device's iteration counter by kCheckFrequency until the limit, so
+  // a correct run needs at most this many launches; the bound keeps the host loop finite even
+  // if the device never reported done.
+  long long max_iter = opt_.max_iterations;
+  if (max_iter <= 0) {
+    max_iter = std::max<long long>(10000LL, 10000LL * (static_cast<long long>(m_) + n_) / 10);
+  }
+  const long long launch_cap = max_iter / kCheckFrequency + 2 * kInflight + 4;
+  for (;;) {
+    if (launches >= launch_cap) break;
+    while (count < kInflight) {
+      const int slot = (head + count) % 4;
+      SG_TRY(cudaGraphLaunch(chunk_exec_, stream_));
+      SG_TRY(cudaMemcpyAsync(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_));
+      SG_TRY(cudaEventRecord(ev_[slot], stream_));
+      ++count;
+      ++launches;
+    }
+    SG_TRY(cudaEventSynchronize(ev_[head]));
+    head = (head + 1) % 4;
+    --count;
+    // ctl_host_ holds the latest completed copy (copies complete in stream order).
+    if (ctl_host_->done) break;
+    if (deadline_s > 0 && now_s() > deadline_s) {
+      // Host-side limit: let the device finish its in-flight chunks, then stop.
+      break;
+    }
+  }
+  SG_TRY(cudaStreamSynchronize(stream_));
+  SG_TRY(cudaStreamSynchronize(stream_));
+  SG_TRY(cudaMemcpy(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  info->graph_launches += launches;
+  info->kernel_launches += launches * chunk_kernels_;
+  return kOk;
+}
+
+int Engine::solve(SolveInfo* info, double* x, double* y, double* dual_ray, double* primal_ray,
+                  std::string* err) {
+  *info = SolveInfo();
+  seam_mode_ = false;
+  int rc = fp32_ ? solve_refined(info, x, y, dual_ray, primal_ray)
+                 : solve_fp64(info, x, y, dual_ray, primal_ray);
+  if (rc != kOk && err) *err = std::string("solve failed: ") + cudaGetErrorString(cudaGetLastError());
+  return rc;
+}
+
+int Engine::solve_fp64(SolveInfo* info, double* x, double* y, double* dual_ray,
+                       double* primal_ray) {
+  std::string* err = nullptr;
+  const double t0 = now_s();
+  int rc = setup_device(nullptr);
+  if (rc != kOk) return rc;
+  rc = capture_chunk();
+  if (rc != kOk) return rc;
+  // Deadline on the device clock (%globaltimer), checked by the decision kernel.
+  if (opt_.time_limit > 0) launch_set_deadline(ctl_, opt_.time_limit - (now_s() - t0), stream_);
+  const double deadline = opt_.time_limit > 0 ? t0 + opt_.time_limit : 0.0;
+  const double t_setup = now_s();
+  info->setup_seconds = t_setup - t0;
+  rc = run_loop(deadline, info);
+  if (rc != kOk) return rc;
+  const Ctl& c = *ctl_host_;
+  if (c.done == 0) {
+    // The host's own time limit ended the loop.
+    info->status = kTimeLimit;
+    info->iterations = c.t;
+  } else {
+    info->status = c.status;
+    info->iterations = c.iterations;
+  }
+  info->rel_primal = c.res[0];
+  info->rel_dual = c.res[1];
+  info->rel_gap = c.res[2];
+  info->primal_obj = c.pobj;
+  info->dual_obj = c.dobj;
+  info->restarts = c.restarts;
+  info->evaluations = c.evaluations;
+  info->omega = c.omega;
+  info->step_size = c.eta;
+  info->operator_norm = c.op_norm;
+  if (c.done == 0 || c.status == kTimeLimit || c.status == kIterationLimit) {
+    // The relative residuals of the last evaluation's current iterate.
+    info->rel_primal = c.meas[0][0];
+    info->rel_dual = c.meas[0][1];
+    info->rel_gap = c.meas[0][2];
+  }
+  // Answer.
+  IterView<double> it = iter_view(it64_);
+  const EvalView ev = eval_view();
+  if (c.done == 0) {
+    // Make the extract kernel read the current iterate.
+    Ctl h = c;
+    h.result_average = 0;
+    SG_TRY(cudaMemcpy(ctl_, &h, sizeof(Ctl), cudaMemcpyHostToDevice));
+  }
+  launch_extract(ctl_, it, ev, x_out_, y_out_, c.status == kInfeasible ? ray_out_ : nullptr,
+                 nullptr, stream_);
+  SG_TRY(cudaGetLastError());
+  const size_t nt = static_cast<size_t>(n_) + m_;
+  if (x) SG_TRY(cudaMemcpyAsync(x, x_out_, nt * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  if (y && m_ > 0) {
+    SG_TRY(cudaMemcpyAsync(y, y_out_, static_cast<size_t>(m_) * sizeof(double),
+                           cudaMemcpyDeviceToHost, stream_));
+  }
+  if (c.status == kInfeasible && dual_ray && m_ > 0) {
+    SG_TRY(cudaMemcpyAsync(dual_ray, ray_out_, static_cast<size_t>(m_) * sizeof(double),
+                           cudaMemcpyDeviceToHost, stream_));
+    info->has_dual_ray = 1;
+  }
+  if (c.status == kUnbounded && primal_ray && n_ > 0) {
+    SG_TRY(cudaMemcpyAsync(primal_ray, scratch_n_, static_cast<size_t>(n_) * sizeof(double),
+                           cudaMemcpyDeviceToHost, stream_));
+    info->has_primal_ray = 1;
+  }
+  SG_TRY(cudaStreamSynchronize(stream_));
+  info->solve_seconds = now_s() - t0;
+  return kOk;
+}
+
+int Engine::solve_refined(SolveInfo* info, double* x, double* y, double* dual_ray,
+                          double* primal_ray) {
+  (void)info;
+  (void)x;
+  (void)y;
+  (void)dual_ray;
+  (void)primal_ray;
+  return kErrInternal;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Inner seam (the reference's gpu::PdhgDevice): here the uploaded problem is used as already
+// equilibrated, and the host supplies the step sizes.
+
+int Engine::seam_set_original(const double* cs, const double* rs, const double* cost,
+                              const double* lower, const double* upper) {
+  std::string* err = nullptr;
+  cudaStream_t s = stream_;
+  const size_t nt = static_cast<size_t>(n_) + m_;
+  const size_t nb = static_cast<size_t>(nnz_);
+  if (!seam_mode_) {
+    // Working values = the given (equilibrated) values; vectors as given; iterates zero.
+    if (nb > 0) {
+      SG_TRY(cudaMemcpyAsync(K_.val, K_.val_orig, nb * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      SG_TRY(cudaMemcpyAsync(Kt_.val, Kt_.val_orig, nb * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+    SG_TRY(cudaMemcpyAsync(it64_.cost, cost_orig_, nt * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    SG_TRY(cudaMemcpyAsync(it64_.lower, lower_orig_, nt * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    SG_TRY(cudaMemcpyAsync(it64_.upper, upper_orig_, nt * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    for (double* p : {it64_.V[0], it64_.V[1], it64_.Vbar, it64_.Verg, it64_.Vrst}) {
+      SG_TRY(cudaMemsetAsync(p, 0, nt * sizeof(double), s));
+    }
+    for (double* p : {it64_.Y[0], it64_.Y[1], it64_.Yerg, it64_.Yrst}) {
+      SG_TRY(cudaMemsetAsync(p, 0, static_cast<size_t>(m_) * sizeof(double), s));
+    }
+    Ctl h;
+    memset(&h, 0, sizeof(h));
+    h.m = m_;
+    h.n = n_;
+    h.max_iter = std::numeric_limits<long long>::max();
+    h.status = kRunning;
+    SG_TRY(cudaMemcpyAsync(ctl_, &h, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+    SG_TRY(cudaStreamSynchronize(s));
+    seam_mode_ = true;
+    seam_steps_ = 0;
+  }
+  SG_TRY(cudaMemcpyAsync(cs_, cs, static_cast<size_t>(n_) * sizeof(double), cudaMemcpyHostToDevice, s));
+  SG_TRY(cudaMemcpyAsync(rs_, rs, static_cast<size_t>(m_) * sizeof(double), cudaMemcpyHostToDevice, s));
+  SG_TRY(cudaMemcpyAsync(cost_ev_, cost, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+  SG_TRY(cudaMemcpyAsync(lower_ev_, lower, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+  SG_TRY(cudaMemcpyAsync(upper_ev_, upper, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+  SG_TRY(cudaStreamSynchronize(s));
+  return kOk;
+}
+
+int Engine::seam_step(double tau, double sigma, long long iter) {
+  std::string* err = nullptr;
+  if (!seam_mode_) return kErrNotReady;
+  // Step sizes and counters through the control block: t = steps taken (buffer parity),
+  // k = `iter` (the averaging weight 1 / (iter + 1)).
+  SG_TRY(cudaStreamSynchronize(stream_));
+  SG_TRY(cudaMemcpy(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  ctl_host_->tau = tau;
+  ctl_host_->sigma = sigma;
+  ctl_host_->t = seam_steps_;
+  ctl_host_->k = iter;
+  ctl_host_->done = 0;
+  ctl_host_->max_iter = std::numeric_limits<long long>::max();
+  SG_TRY(cudaMemcpy(ctl_, ctl_host_, sizeof(Ctl), cudaMemcpyHostToDevice));
+  IterView<double> it = iter_view(it64_);
+  launch_dual_step(ctl_, K_.view64(), it, 0, grid_step_k_, stream_);
+  launch_primal_step(ctl_, Kt_.view64(), it, 0, grid_step_t_, stream_);
+  SG_TRY(cudaGetLastError());
+  SG_TRY(cudaStreamSynchronize(stream_));
+  return kOk;
+}
+
+int Engine::seam_advance() {
+  if (!seam_mode_) return kErrNotReady;
+  ++seam_steps_;
+  return kOk;
+}
+
+int Engine::seam_evaluate(int which, double* sums7) {
+  std::string* err = nullptr;
+  if (!seam_mode_) return kErrNotReady;
+  IterView<double> it = iter_view(it64_);
+  const int parity = static_cast<int>((seam_steps_ + 1) & 1);  // v_new after step()
+  launch_eval(ctl_, K_.view64(), Kt_.view64(), it, eval_view(), red_view(), grid_k_, grid_t_,
+              parity, stream_);
+  SG_TRY(cudaGetLastError());
+  SG_TRY(cudaStreamSynchronize(stream_));
+  SG_TRY(cudaMemcpy(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  const int w = which == 0 ? 0 : 1;
+  for (int q = 0; q < 7; ++q) sums7[q] = ctl_host_->eval_c[w * 7 + q] + ctl_host_->eval_r[w * 7 + q];
+  return kOk;
+}
+
+int Engine::seam_restart_distance(int which, double* dv, double* dy) {
+  std::string* err = nullptr;
+  if (!seam_mode_) return kErrNotReady;
+  IterView<double> it = iter_view(it64_);
+  const int parity = static_cast<int>((seam_steps_ + 1) & 1);
+  launch_eval(ctl_, K_.view64(), Kt_.view64(), it, eval_view(), red_view(), grid_k_, grid_t_,
+              parity, stream_);
+  SG_TRY(cudaGetLastError());
+  SG_TRY(cudaStreamSynchronize(stream_));
+  SG_TRY(cudaMemcpy(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  const int a = which == 0 ? 14 : 16;
+  *dv = ctl_host_->eval_c[a] + ctl_host_->eval_r[a];
+  *dy = ctl_host_->eval_r[a + 1];
+  return kOk;
+}
+
+int Engine::seam_restart_to(int which) {
+  std::string* err = nullptr;
+  if (!seam_mode_) return kErrNotReady;
+  // The restart kernel restarts at the iterate in buffer (t & 1) or the average.
+  SG_TRY(cudaStreamSynchronize(stream_));
+  SG_TRY(cudaMemcpy(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  ctl_host_->t = seam_steps_ + 1;
+  ctl_host_->restart_pending = 1;
+  ctl_host_->restart_to_avg = which == 0 ? 0 : 1;
+  SG_TRY(cudaMemcpy(ctl_, ctl_host_, sizeof(Ctl), cudaMemcpyHostToDevice));
+  launch_restart(ctl_, iter_view(it64_), stream_);
+  SG_TRY(cudaGetLastError());
+  SG_TRY(cudaStreamSynchronize(stream_));
+  ctl_host_->restart_pending = 0;
+  ctl_host_->t = seam_steps_;
+  SG_TRY(cudaMemcpy(ctl_, ctl_host_, sizeof(Ctl), cudaMemcpyHostToDevice));
+  return kOk;
+}
+
+int Engine::seam_download(double* v, double* v_new, double* y, double* y_new, double* v_erg,
+                          double* y_erg) {
+  std::string* err = nullptr;
+  if (!seam_mode_) return kErrNotReady;
+  const size_t nt = static_cast<size_t>(n_) + m_;
+  const size_t m = static_cast<size_t>(m_);
+  const int p = static_cast<int>(seam_steps_ & 1);
+  SG_TRY(cudaStreamSynchronize(stream_));
+  if (v) SG_TRY(cudaMemcpy(v, it64_.V[p], nt * sizeof(double), cudaMemcpyDeviceToHost));
+  if (v_new) SG_TRY(cudaMemcpy(v_new, it64_.V[p ^ 1], nt * sizeof(double), cudaMemcpyDeviceToHost));
+  if (y && m) SG_TRY(cudaMemcpy(y, it64_.Y[p], m * sizeof(double), cudaMemcpyDeviceToHost));
+  if (y_new && m) SG_TRY(cudaMemcpy(y_new, it64_.Y[p ^ 1], m * sizeof(double), cudaMemcpyDeviceToHost));
+  if (v_erg) SG_TRY(cudaMemcpy(v_erg, it64_.Verg, nt * sizeof(double), cudaMemcpyDeviceToHost));
+  if (y_erg && m) SG_TRY(cudaMemcpy(y_erg, it64_.Yerg, m * sizeof(double), cudaMemcpyDeviceToHost));
+  return kOk;
+}
+
+int Engine::spmv(int transpose, const double* x, double* y) {
+  std::string* err = nullptr;
+  const DevOp& op = transpose ? Kt_ : K_;
+  double* dx = nullptr;
+  double* dy = nullptr;
+  SG_TRY(dalloc(&dx, static_cast<size_t>(op.cols)));
+  SG_TRY(dalloc(&dy, static_cast<size_t>(op.rows)));
+  SG_TRY(cudaMemcpy(dx, x, static_cast<size_t>(op.cols) * sizeof(double), cudaMemcpyHostToDevice));
+  OpView<double> v = op.view64();
+  v.val = op.val_orig;
+  launch_spmv(v, dx, dy, std::max(1, std::min(op.ntiles, 65535)), stream_);
+  SG_TRY(cudaGetLastError());
+  SG_TRY(cudaStreamSynchronize(stream_));
+  SG_TRY(cudaMemcpy(y, dy, static_cast<size_t>(op.rows) * sizeof(double), cudaMemcpyDeviceToHost));
+  cudaFree(dx);
+  cudaFree(dy);
+  return kOk;
+}
+
+}  // namespace sg

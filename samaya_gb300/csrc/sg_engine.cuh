@@ -1,0 +1,194 @@
+// Host side of the GB300 PDLP engine: owns the device memory of one LP, runs the device setup,
+// captures one chunk of the iteration loop (kCheckFrequency fused PDHG iterations + evaluation +
+// decisions + restart + detection) as a CUDA graph and replays it until the device-side status
+// word says done. No exception crosses this interface; errors are negative codes.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "sg_kernels.cuh"
+
+namespace sg {
+
+enum Error : int {
+  kOk = 0,
+  kErrInvalidArgument = -1,
+  kErrNoDevice = -2,
+  kErrCuda = -3,
+  kErrOutOfMemory = -4,
+  kErrTooLarge = -5,
+  kErrInternal = -6,
+  kErrNotReady = -7,
+};
+
+struct Options {
+  double tol = 1e-8;
+  long long max_iterations = -1;
+  double time_limit = 0.0;  // seconds; <= 0: none
+  int precision = 0;        // 0 FP64, 1 FP32 storage + FP64 refinement
+  int refine_max_rounds = 6;
+  double inner_tol = 1e-4;
+  int verbose = 0;
+};
+
+struct SolveInfo {
+  int status = kNumericalError;
+  long long iterations = 0;
+  double rel_primal = 0, rel_dual = 0, rel_gap = 0;
+  double primal_obj = 0, dual_obj = 0;
+  long long restarts = 0, evaluations = 0;
+  int refinement_rounds = 0;
+  double setup_seconds = 0, solve_seconds = 0;
+  double omega = 1, step_size = 0, operator_norm = 0;
+  int has_dual_ray = 0, has_primal_ray = 0;
+  long long graph_launches = 0;
+  long long kernel_launches = 0;
+};
+
+// A device operator by rows with its tiles.
+struct DevOp {
+  int rows = 0;
+  int cols = 0;
+  long long nnz = 0;
+  int* ptr = nullptr;
+  int* idx = nullptr;
+  double* val = nullptr;       // working FP64 values (equilibrated after setup)
+  double* val_orig = nullptr;  // values as given
+  float* val32 = nullptr;      // FP32 copy for the mixed-precision path
+  Tile* tiles = nullptr;
+  int ntiles = 0;
+  int nlong = 0;
+  double* seg_part = nullptr;
+  unsigned* lcount = nullptr;
+  std::vector<int> host_ptr;
+
+  TileSet tileset() const {
+    TileSet t;
+    t.tiles = tiles;
+    t.ntiles = ntiles;
+    t.nlong = nlong;
+    t.seg_part = seg_part;
+    t.lcount = lcount;
+    return t;
+  }
+  OpView<double> view64() const { return OpView<double>{ptr, idx, val, rows, tileset()}; }
+  OpView<float> view32() const { return OpView<float>{ptr, idx, val32, rows, tileset()}; }
+};
+
+// Iterate storage of one precision.
+template <typename T>
+struct DevIter {
+  T* V[2] = {nullptr, nullptr};
+  T* Vbar = nullptr;
+  T* Y[2] = {nullptr, nullptr};
+  T* Verg = nullptr;
+  T* Yerg = nullptr;
+  T* Vrst = nullptr;
+  T* Yrst = nullptr;
+  T* cost = nullptr;
+  T* lower = nullptr;
+  T* upper = nullptr;
+  T* rhs = nullptr;
+};
+
+class Engine {
+ public:
+  ~Engine();
+
+  // Uploads the LpProblem (A as CSC m x n, cost/lower/upper n + m) and builds both operators.
+  static int create(Engine** out, int m, int n, const int64_t* colptr, const int32_t* rowidx,
+                    const double* val, const double* cost, const double* lower,
+                    const double* upper, const Options& opt, std::string* err);
+
+  // Full PDLP solve (setup on the device, graph-replayed iterations). Outputs in the
+  // LpProblem's space: x (n + m), y (m), dual_ray (m), primal_ray (n); any may be null.
+  int solve(SolveInfo* info, double* x, double* y, double* dual_ray, double* primal_ray,
+            std::string* err);
+
+  // Inner GPU seam, the counterpart of the reference's gpu::PdhgDevice (pdhg_core.hpp:24-79):
+  // the problem given is already equilibrated; the host drives single steps.
+  int seam_set_original(const double* cs, const double* rs, const double* cost,
+                        const double* lower, const double* upper);
+  int seam_step(double tau, double sigma, long long iter);
+  int seam_advance();
+  int seam_evaluate(int which, double* sums7);
+  int seam_restart_distance(int which, double* dv, double* dy);
+  int seam_restart_to(int which);
+  int seam_download(double* v, double* v_new, double* y, double* y_new, double* v_erg,
+                    double* y_erg);
+  // y = K x (rows of A) or y = K' x through the tile kernel (FP64).
+  int spmv(int transpose, const double* x, double* y);
+
+  int m() const { return m_; }
+  int n() const { return n_; }
+  long long nnz() const { return nnz_; }
+
+ private:
+  Engine() = default;
+  int alloc_all(std::string* err);
+  int setup_device(const double* rhs_orig);
+  int capture_chunk();
+  template <typename T>
+  IterView<T> iter_view(DevIter<T>& it);
+  EvalView eval_view() const;
+  RedView red_view() const;
+  int run_loop(double deadline_s, SolveInfo* info);
+  int solve_fp64(SolveInfo* info, double* x, double* y, double* dual_ray, double* primal_ray);
+  int solve_refined(SolveInfo* info, double* x, double* y, double* dual_ray, double* primal_ray);
+  void enqueue_chunk_body();
+  int check(cudaError_t e, const char* what);
+
+  int m_ = 0, n_ = 0;
+  long long nnz_ = 0;
+  Options opt_;
+  int grid_k_ = 1, grid_t_ = 1, grid_step_k_ = 1, grid_step_t_ = 1;
+  int sm_count_ = 148;
+  bool fp32_ = false;
+  DevOp K_, Kt_;
+  DevIter<double> it64_;
+  DevIter<float> it32_;
+  // FP64 problem data.
+  double* cost_orig_ = nullptr;   // n + m, as given (LpProblem space)
+  double* lower_orig_ = nullptr;
+  double* upper_orig_ = nullptr;
+  double* cost_ev_ = nullptr;     // evaluation copies (the problem the iterations solve)
+  double* lower_ev_ = nullptr;
+  double* upper_ev_ = nullptr;
+  double* rhs_ev_ = nullptr;      // m, null when zero
+  double* cs_ = nullptr;
+  double* rs_ = nullptr;
+  double* cn_ = nullptr;
+  double* rn_ = nullptr;
+  double* pu_ = nullptr;          // power iteration vectors
+  double* pv_ = nullptr;
+  double* u0_ = nullptr;          // power iteration start (mt19937_64(12345) uniform(-1, 1))
+  double* scratch_n_ = nullptr;
+  double* x_out_ = nullptr;
+  double* y_out_ = nullptr;
+  double* ray_out_ = nullptr;
+  double* partial_ = nullptr;
+  unsigned* counter_ = nullptr;
+  double* long_terms_ = nullptr;
+  Ctl* ctl_ = nullptr;
+  Ctl* ctl_host_ = nullptr;       // pinned
+  cudaStream_t stream_ = nullptr;
+  cudaGraphExec_t chunk_exec_ = nullptr;
+  cudaGraph_t chunk_graph_ = nullptr;
+  int chunk_kernels_ = 0;
+  long long seam_steps_ = 0;
+  bool seam_mode_ = false;
+  cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+// Builds the tile partition of a CSR operator (host). Exposed for the CPU tests.
+void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, std::vector<Tile>* out,
+                 int* nlong);
+
+// Device facts for sg_pdlp_available.
+int device_info(int* major, int* minor, char* name, size_t len);
+
+}  // namespace sg

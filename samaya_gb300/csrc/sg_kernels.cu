@@ -1,0 +1,1238 @@
+// Kernels of the GB300 PDLP engine: the two fused PDHG step kernels, the evaluation kernels, the
+// single-CTA decision kernels, restarts, infeasibility/unboundedness detection and the
+// device-side setup (Ruiz, power iteration, norms).
+//
+// Reference algorithm: src/lp/pdlp.cpp (CPU loop and decisions) and src/gpu/pdhg_core.cu (its
+// GPU arithmetic). Here every decision of the loop runs on the device, so a chunk of
+// kCheckFrequency iterations plus its evaluation replays from one CUDA graph.
+#include <math.h>
+
+#include <type_traits>
+
+#include "sg_kernels.cuh"
+#include "sg_tile.cuh"
+
+namespace sg {
+
+namespace {
+
+template <typename ACC, int NV>
+__device__ __forceinline__ TileSmem<ACC, NV>& tile_smem() {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  return *reinterpret_cast<TileSmem<ACC, NV>*>(smem_raw);
+}
+
+template <typename T>
+__device__ __forceinline__ T clampv(T v, T lo, T hi) {
+  return fmin(fmax(v, lo), hi);
+}
+
+// lambda of the reduced cost g for a variable with bounds [lo, up] (pdlp.cpp:455-465).
+__device__ __forceinline__ double bound_part(double g, double lo, double up) {
+  const bool hl = lo > -INFINITY;
+  const bool hu = up < INFINITY;
+  return hl && hu ? g : hl ? fmax(g, 0.0) : hu ? fmin(g, 0.0) : 0.0;
+}
+
+template <typename T, typename ACC>
+struct Gather1 {
+  const T* x;
+  __device__ __forceinline__ ACC operator()(int, T a, int j) const {
+    return static_cast<ACC>(a) * static_cast<ACC>(ldg(x + j));
+  }
+};
+
+template <typename T>
+struct Gather2 {
+  const T* x0;
+  const T* x1;
+  __device__ __forceinline__ double operator()(int v, T a, int j) const {
+    return static_cast<double>(a) * static_cast<double>(ldg((v == 0 ? x0 : x1) + j));
+  }
+};
+
+// ------------------------------------------------------------------------------------------
+// Step kernels. One PDHG iteration (pdlp.cpp:574-641; pdhg_core.cu:23-50) is two launches:
+//   dual   (rows of K):  y+ = y + sigma (K xbar - rbar - q); r+ = proj(r - tau (c_r - y+));
+//                        rbar' = r+ + (r+ - r); averages of y and r
+//   primal (rows of K'): x+ = proj(x - tau (c_x + K' y+)); xbar' = x+ + (x+ - x); average of x
+// The extrapolation of the reference's first kernel is produced by the previous step's
+// epilogue (xbar'), so the SpMV gathers one vector.
+
+template <typename T, typename ACC>
+struct DualEpi {
+  const T* y;
+  T* y_new;
+  const T* vr;   // r (n offset applied)
+  T* vr_new;
+  T* vbar_r;
+  const T* c;
+  const T* l;
+  const T* u;
+  const T* q;
+  T* yerg;
+  T* verg_r;
+  ACC sigma, tau, alpha, beta;
+  __device__ __forceinline__ void row(int i, const ACC (&s)[1]) {
+    ACC res = s[0] - static_cast<ACC>(vbar_r[i]);
+    if (q != nullptr) res -= static_cast<ACC>(q[i]);
+    const ACC yn = static_cast<ACC>(y[i]) + sigma * res;
+    y_new[i] = static_cast<T>(yn);
+    const ACC r = static_cast<ACC>(vr[i]);
+    ACC rn = r - tau * (static_cast<ACC>(c[i]) - yn);
+    rn = clampv<ACC>(rn, static_cast<ACC>(l[i]), static_cast<ACC>(u[i]));
+    vr_new[i] = static_cast<T>(rn);
+    vbar_r[i] = static_cast<T>(rn + (rn - r));
+    yerg[i] = static_cast<T>(beta * static_cast<ACC>(yerg[i]) + alpha * yn);
+    verg_r[i] = static_cast<T>(beta * static_cast<ACC>(verg_r[i]) + alpha * rn);
+  }
+  __device__ __forceinline__ void long_row(int, int i, const ACC (&s)[1]) { row(i, s); }
+};
+
+template <typename T, typename ACC>
+struct PrimalEpi {
+  const T* x;
+  T* x_new;
+  T* xbar;
+  const T* c;
+  const T* l;
+  const T* u;
+  T* xerg;
+  ACC tau, alpha, beta;
+  __device__ __forceinline__ void row(int j, const ACC (&s)[1]) {
+    const ACC xo = static_cast<ACC>(x[j]);
+    ACC xn = xo - tau * (static_cast<ACC>(c[j]) + s[0]);
+    xn = clampv<ACC>(xn, static_cast<ACC>(l[j]), static_cast<ACC>(u[j]));
+    x_new[j] = static_cast<T>(xn);
+    xbar[j] = static_cast<T>(xn + (xn - xo));
+    xerg[j] = static_cast<T>(beta * static_cast<ACC>(xerg[j]) + alpha * xn);
+  }
+  __device__ __forceinline__ void long_row(int, int j, const ACC (&s)[1]) { row(j, s); }
+};
+
+template <typename T>
+using Acc = T;  // FP64 storage accumulates in FP64, FP32 storage in FP32.
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) dual_step_kernel(const Ctl* __restrict__ ctl,
+                                                           OpView<T> K, IterView<T> it, int j) {
+  if (ctl->done) return;
+  const long long t = ctl->t + j;
+  if (t >= ctl->max_iter) return;
+  using ACC = Acc<T>;
+  const int p = static_cast<int>(t & 1);
+  const long long k = ctl->k + j;
+  const double alpha = 1.0 / static_cast<double>(k + 1);
+  DualEpi<T, ACC> epi;
+  const int n = it.n;
+  epi.y = it.Y[p];
+  epi.y_new = it.Y[p ^ 1];
+  epi.vr = it.V[p] + n;
+  epi.vr_new = it.V[p ^ 1] + n;
+  epi.vbar_r = it.Vbar + n;
+  epi.c = it.cost + n;
+  epi.l = it.lower + n;
+  epi.u = it.upper + n;
+  epi.q = it.rhs;
+  epi.yerg = it.Yerg;
+  epi.verg_r = it.Verg + n;
+  epi.sigma = static_cast<ACC>(ctl->sigma);
+  epi.tau = static_cast<ACC>(ctl->tau);
+  epi.alpha = static_cast<ACC>(alpha);
+  epi.beta = static_cast<ACC>(1.0 - alpha);
+  Gather1<T, ACC> g{it.Vbar};
+  run_tiles<T, ACC, 1>(K.ts, K.ptr, K.idx, K.val, g, epi, tile_smem<ACC, 1>());
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) primal_step_kernel(const Ctl* __restrict__ ctl,
+                                                             OpView<T> Kt, IterView<T> it, int j) {
+  if (ctl->done) return;
+  const long long t = ctl->t + j;
+  if (t >= ctl->max_iter) return;
+  using ACC = Acc<T>;
+  const int p = static_cast<int>(t & 1);
+  const long long k = ctl->k + j;
+  const double alpha = 1.0 / static_cast<double>(k + 1);
+  PrimalEpi<T, ACC> epi;
+  epi.x = it.V[p];
+  epi.x_new = it.V[p ^ 1];
+  epi.xbar = it.Vbar;
+  epi.c = it.cost;
+  epi.l = it.lower;
+  epi.u = it.upper;
+  epi.xerg = it.Verg;
+  epi.tau = static_cast<ACC>(ctl->tau);
+  epi.alpha = static_cast<ACC>(alpha);
+  epi.beta = static_cast<ACC>(1.0 - alpha);
+  Gather1<T, ACC> g{it.Y[p ^ 1]};
+  run_tiles<T, ACC, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi, tile_smem<ACC, 1>());
+}
+
+// ------------------------------------------------------------------------------------------
+// Evaluation (pdhg_core.cu:102-144 / pdlp.cpp:411-488): the seven sums of the current and the
+// average iterate in the space before equilibration, plus the restart distances, from one
+// pass over each operator (both iterates share the matrix read).
+
+template <typename T>
+struct EvalRowEpi {
+  // rows of K: logicals r and duals y
+  const T* vr[2];
+  const T* y[2];
+  const T* vr_rst;
+  const T* y_rst;
+  EvalView ev;
+  int n;
+  double acc[kEvalSums];
+  double* long_terms;
+  __device__ __forceinline__ void terms(int i, const double (&s)[2], double (&a)[kEvalSums]) {
+    const double rs = ev.rs[i];
+    const double c = ev.cost[n + i];
+    const double lo = ev.lower[n + i];
+    const double up = ev.upper[n + i];
+    const double q = ev.rhs != nullptr ? ev.rhs[i] : 0.0;
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+      const double vrv = static_cast<double>(vr[w][i]);
+      const double yv = static_cast<double>(y[w][i]);
+      const double value = vrv / rs;
+      const double yo = yv * rs;
+      const double g = c - yo;
+      const double e = s[w] / rs - value - q;
+      a[w * 7 + 0] += e * e;
+      a[w * 7 + 5] += value * value;
+      a[w * 7 + 6] += yo * yo;
+      a[w * 7 + 2] += c * value;
+      const double lam = bound_part(g, lo, up);
+      a[w * 7 + 1] += (g - lam) * (g - lam);
+      if (lam > 0.0) a[w * 7 + 3] += lam * lo;
+      if (lam < 0.0) a[w * 7 + 3] += lam * up;
+      // With a right-hand side ([A -I] v = q) the dual objective carries -y'q.
+      if (q != 0.0) a[w * 7 + 3] -= yo * q;
+      const double dv = vrv - static_cast<double>(vr_rst[i]);
+      const double dy = yv - static_cast<double>(y_rst[i]);
+      a[14 + 2 * w] += dv * dv;
+      a[15 + 2 * w] += dy * dy;
+    }
+  }
+  __device__ __forceinline__ void row(int i, const double (&s)[2]) { terms(i, s, acc); }
+  __device__ __forceinline__ void long_row(int lrow, int i, const double (&s)[2]) {
+    double a[kEvalSums];
+#pragma unroll
+    for (int q = 0; q < kEvalSums; ++q) a[q] = 0.0;
+    terms(i, s, a);
+#pragma unroll
+    for (int q = 0; q < kEvalSums; ++q) long_terms[lrow * kMaxSums + q] = a[q];
+  }
+};
+
+template <typename T>
+struct EvalColEpi {
+  // rows of K': structurals x
+  const T* x[2];
+  const T* x_rst;
+  EvalView ev;
+  int m;
+  double acc[kEvalSums];
+  double* long_terms;
+  __device__ __forceinline__ void terms(int j, const double (&s)[2], double (&a)[kEvalSums]) {
+    const double cs = ev.cs[j];
+    const double c = ev.cost[j];
+    const double lo = ev.lower[j];
+    const double up = ev.upper[j];
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+      const double xv = static_cast<double>(x[w][j]);
+      const double value = xv * cs;
+      const double g = c + (m > 0 ? s[w] / cs : 0.0);
+      a[w * 7 + 4] += value * value;
+      a[w * 7 + 2] += c * value;
+      const double lam = bound_part(g, lo, up);
+      a[w * 7 + 1] += (g - lam) * (g - lam);
+      if (lam > 0.0) a[w * 7 + 3] += lam * lo;
+      if (lam < 0.0) a[w * 7 + 3] += lam * up;
+      const double dv = xv - static_cast<double>(x_rst[j]);
+      a[14 + 2 * w] += dv * dv;
+    }
+  }
+  __device__ __forceinline__ void row(int j, const double (&s)[2]) { terms(j, s, acc); }
+  __device__ __forceinline__ void long_row(int lrow, int j, const double (&s)[2]) {
+    double a[kEvalSums];
+#pragma unroll
+    for (int q = 0; q < kEvalSums; ++q) a[q] = 0.0;
+    terms(j, s, a);
+#pragma unroll
+    for (int q = 0; q < kEvalSums; ++q) long_terms[lrow * kMaxSums + q] = a[q];
+  }
+};
+
+// Adds the split rows' terms (in split-row order) to the grid totals and stores them.
+struct EvalFin {
+  double* out;
+  const double* long_terms;
+  int nlong;
+  __device__ __forceinline__ void operator()(const double (&tot)[kEvalSums]) const {
+    for (int q = 0; q < kEvalSums; ++q) {
+      double s = tot[q];
+      for (int l = 0; l < nlong; ++l) s += __ldcg(long_terms + l * kMaxSums + q);
+      out[q] = s;
+    }
+  }
+};
+
+__device__ __forceinline__ int eval_parity(const Ctl* ctl, int fixed_parity) {
+  if (fixed_parity >= 0) return fixed_parity;
+  long long steps = ctl->max_iter - ctl->t;
+  if (steps > kCheckFrequency) steps = kCheckFrequency;
+  return static_cast<int>((ctl->t + steps) & 1);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) eval_rows_kernel(Ctl* ctl, OpView<T> K, IterView<T> it,
+                                                           EvalView ev, RedView red,
+                                                           int fixed_parity) {
+  if (fixed_parity < 0 && ctl->done) return;
+  const int cur = eval_parity(ctl, fixed_parity);
+  EvalRowEpi<T> epi;
+  const int n = it.n;
+  epi.vr[0] = it.V[cur] + n;
+  epi.vr[1] = it.Verg + n;
+  epi.y[0] = it.Y[cur];
+  epi.y[1] = it.Yerg;
+  epi.vr_rst = it.Vrst + n;
+  epi.y_rst = it.Yrst;
+  epi.ev = ev;
+  epi.n = n;
+  epi.long_terms = red.long_terms;
+#pragma unroll
+  for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0;
+  Gather2<T> g{it.V[cur], it.Verg};
+  TileSmem<double, 2>& sm = tile_smem<double, 2>();
+  run_tiles<T, double, 2>(K.ts, K.ptr, K.idx, K.val, g, epi, sm);
+  EvalFin fin{ctl->eval_r, red.long_terms, K.ts.nlong};
+  grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, sm.red, fin);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) eval_cols_kernel(Ctl* ctl, OpView<T> Kt, IterView<T> it,
+                                                           EvalView ev, RedView red,
+                                                           int fixed_parity) {
+  if (fixed_parity < 0 && ctl->done) return;
+  const int cur = eval_parity(ctl, fixed_parity);
+  EvalColEpi<T> epi;
+  epi.x[0] = it.V[cur];
+  epi.x[1] = it.Verg;
+  epi.x_rst = it.Vrst;
+  epi.ev = ev;
+  epi.m = it.m;
+  epi.long_terms = red.long_terms;
+#pragma unroll
+  for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0;
+  Gather2<T> g{it.Y[cur], it.Yerg};
+  TileSmem<double, 2>& sm = tile_smem<double, 2>();
+  run_tiles<T, double, 2>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi, sm);
+  EvalFin fin{ctl->eval_c, red.long_terms, Kt.ts.nlong};
+  grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, sm.red, fin);
+}
+
+// ------------------------------------------------------------------------------------------
+// Decisions (pdlp.cpp:493-541, 674-713, 1069-1131), one thread.
+
+struct Meas {
+  double rp, rd, rg, pobj, dobj;
+};
+
+__device__ Meas finish_sums(const Ctl* c, const double* s) {
+  // s = (primal_sq, dual_sq, primal_obj, dual_obj, x_sq, r_sq, y_sq)
+  Meas r;
+  const double primal_res = sqrt(s[0]);
+  const double dual_res = sqrt(s[1]);
+  const double gap = s[2] - s[3];
+  const double primal_scale = 1.0 + c->a_norm_max_col * sqrt(s[4]) + sqrt(s[5]);
+  const double dual_scale = 1.0 + c->at_norm_max_row * sqrt(s[6]) + c->c_norm;
+  const double gap_scale = 1.0 + fabs(s[2]) + fabs(s[3]);
+  r.rp = c->m > 0 ? primal_res / primal_scale : 0.0;
+  r.rd = c->m > 0 ? dual_res / dual_scale : 0.0;
+  r.rg = gap / gap_scale;
+  r.pobj = s[2];
+  r.dobj = s[3];
+  return r;
+}
+
+__device__ __forceinline__ double kkt_weighted(double omega, const Meas& e) {
+  return sqrt(omega * omega * e.rp * e.rp + e.rd * e.rd / (omega * omega) + e.rg * e.rg);
+}
+
+__device__ __forceinline__ bool converged(const Meas& e, double tol) {
+  return e.rp < tol && e.rd < tol && fabs(e.rg) < tol;
+}
+
+__device__ void set_answer(Ctl* c, int status, const Meas& e, long long iterations, int avg) {
+  c->status = status;
+  c->res[0] = e.rp;
+  c->res[1] = e.rd;
+  c->res[2] = e.rg;
+  c->pobj = e.pobj;
+  c->dobj = e.dobj;
+  c->iterations = iterations;
+  c->result_average = avg;
+  c->done = 1;
+}
+
+// Termination test after the evaluation; schedules the detection checks.
+__global__ void decide_a_kernel(Ctl* c) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  c->restart_pending = 0;
+  c->detect_pending = 0;
+  if (c->done) return;
+  long long steps = c->max_iter - c->t;
+  if (steps > kCheckFrequency) steps = kCheckFrequency;
+  const long long t_new = c->t + steps;
+  const long long iter = t_new - 1;
+  double s_cur[7], s_avg[7];
+  for (int q = 0; q < 7; ++q) {
+    s_cur[q] = c->eval_c[q] + c->eval_r[q];
+    s_avg[q] = c->eval_c[7 + q] + c->eval_r[7 + q];
+  }
+  const Meas cur = finish_sums(c, s_cur);
+  const Meas avg = finish_sums(c, s_avg);
+  c->evaluations += 1;
+  const double wc[5] = {cur.rp, cur.rd, cur.rg, cur.pobj, cur.dobj};
+  const double wa[5] = {avg.rp, avg.rd, avg.rg, avg.pobj, avg.dobj};
+  for (int q = 0; q < 5; ++q) {
+    c->meas[0][q] = wc[q];
+    c->meas[1][q] = wa[q];
+  }
+  if (converged(cur, c->tol)) {
+    set_answer(c, kOptimal, cur, t_new, 0);
+    c->t = t_new;
+    return;
+  }
+  if (converged(avg, c->tol)) {
+    set_answer(c, kOptimal, avg, t_new, 1);
+    c->t = t_new;
+    return;
+  }
+  c->detect_pending = (iter > 1000 && c->m > 0 && ((iter + 1) / kCheckFrequency) % 8 == 0) ? 1 : 0;
+  for (int q = 0; q < 8; ++q) c->det_flags[q] = 0;
+}
+
+// Detection verdict, then PDLP's adaptive restart and primal-weight update; advances the
+// iteration counters and applies the iteration and time limits.
+__global__ void decide_b_kernel(Ctl* c) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (c->done) return;
+  long long steps = c->max_iter - c->t;
+  if (steps > kCheckFrequency) steps = kCheckFrequency;
+  const long long t_new = c->t + steps;
+  const long long iter = t_new - 1;
+  Meas cur{c->meas[0][0], c->meas[0][1], c->meas[0][2], c->meas[0][3], c->meas[0][4]};
+  Meas avg{c->meas[1][0], c->meas[1][1], c->meas[1][2], c->meas[1][3], c->meas[1][4]};
+  if (c->detect_pending) {
+    if (c->det_flags[0]) {
+      set_answer(c, kInfeasible, cur, t_new, 0);
+      c->t = t_new;
+      return;
+    }
+    if (c->det_flags[1]) {
+      set_answer(c, kUnbounded, cur, t_new, 0);
+      c->t = t_new;
+      return;
+    }
+  }
+  const long long k_new = c->k + steps;
+  const double omega = c->omega;
+  const double kkt_cur = kkt_weighted(omega, cur);
+  const double kkt_avg = kkt_weighted(omega, avg);
+  const bool to_average = kkt_avg < kkt_cur;
+  const double cand = fmin(kkt_cur, kkt_avg);
+  if (!(c->kkt_at_restart < INFINITY)) c->kkt_at_restart = cand;
+  const bool restart = cand <= 0.2 * c->kkt_at_restart ||
+                       (cand <= 0.8 * c->kkt_at_restart && cand > c->kkt_previous) ||
+                       static_cast<double>(k_new) >= 0.36 * static_cast<double>(iter + 1);
+  c->kkt_previous = cand;
+  c->last_kkt = cand;
+  if (restart) {
+    const double dx = sqrt(c->eval_c[to_average ? 16 : 14] + c->eval_r[to_average ? 16 : 14]);
+    const double dy = sqrt(c->eval_r[to_average ? 17 : 15]);
+    if (dx > 1e-10 && dy > 1e-10) {
+      const double w = exp(0.5 * log(dy / dx) + 0.5 * log(omega));
+      c->omega = w;
+      c->tau = c->eta / w;
+      c->sigma = c->eta * w;
+    }
+    c->restart_pending = 1;
+    c->restart_to_avg = to_average ? 1 : 0;
+    c->k = 0;
+    c->kkt_at_restart = cand;
+    c->kkt_previous = INFINITY;
+    c->restarts += 1;
+  } else {
+    c->k = k_new;
+  }
+  c->t = t_new;
+  if (c->t >= c->max_iter) {
+    set_answer(c, kIterationLimit, cur, c->max_iter, 0);
+    return;
+  }
+  if (c->deadline_ns != 0ull && globaltimer_ns() > c->deadline_ns) {
+    set_answer(c, kTimeLimit, cur, c->t, 0);
+  }
+}
+
+// Restart at the candidate (pdhg_core.cu:362-380 + advance()): it becomes the current point
+// (both ping-pong buffers), the extrapolated point (no momentum) and the restart point.
+template <typename T>
+__global__ void restart_kernel(const Ctl* __restrict__ ctl, IterView<T> it) {
+  if (!ctl->restart_pending) return;
+  const int cur = static_cast<int>(ctl->t & 1);
+  const bool avg = ctl->restart_to_avg != 0;
+  const int nt = it.n + it.m;
+  const T* vc = avg ? it.Verg : it.V[cur];
+  const T* yc = avg ? it.Yerg : it.Y[cur];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
+    const T val = vc[k];
+    it.Vrst[k] = val;
+    it.V[0][k] = val;
+    it.V[1][k] = val;
+    it.Vbar[k] = val;
+    if (k < it.m) {
+      const T yv = yc[k];
+      it.Yrst[k] = yv;
+      it.Y[0][k] = yv;
+      it.Y[1][k] = yv;
+    }
+  }
+}
+
+__global__ void set_deadline_kernel(Ctl* c, unsigned long long budget_ns) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) c->deadline_ns = globaltimer_ns() + budget_ns;
+}
+
+// The answer in the LpProblem's space (pdlp.cpp:1167-1189): x = v cs, r = v / rs, y = y rs.
+template <typename T>
+__global__ void extract_kernel(const Ctl* __restrict__ ctl, IterView<T> it, EvalView ev,
+                               double* x_out, double* y_out, double* dual_ray) {
+  const int cur = static_cast<int>(ctl->t & 1);
+  const bool avg = ctl->result_average != 0;
+  const T* v = avg ? it.Verg : it.V[cur];
+  const T* y = avg ? it.Yerg : it.Y[cur];
+  const int n = it.n;
+  const int nt = n + it.m;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
+    if (k < n) {
+      x_out[k] = static_cast<double>(v[k]) * ev.cs[k];
+    } else {
+      x_out[k] = static_cast<double>(v[k]) / ev.rs[k - n];
+    }
+    if (k < it.m) {
+      y_out[k] = static_cast<double>(y[k]) * ev.rs[k];
+      if (dual_ray != nullptr) dual_ray[k] = static_cast<double>(it.Yerg[k]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Infeasibility and unboundedness detection (pdlp.cpp:715-1043), on the device: Farkas
+// certificate from the average dual, improving ray from the difference of consecutive
+// iterates. Gated by Ctl::detect_pending; scalars land in Ctl::det / det_flags.
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) det_farkas_rows_kernel(Ctl* c, IterView<T> it,
+                                                                 EvalView ev, RedView red) {
+  if (c->done || !c->detect_pending) return;
+  __shared__ double scratch[kMaxSums * (kBlock / 32)];
+  double a[2] = {0.0, 0.0};  // max |yf|, sum |yf|
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < it.m; i += gridDim.x * blockDim.x) {
+    const double yf = fabs(static_cast<double>(it.Yerg[i]) * ev.rs[i]);
+    a[0] = fmax(a[0], yf);
+    a[1] += yf;
+  }
+  grid_reduce<2, 1u>(a, red.partial, red.counter, scratch, [c](const double (&t)[2]) {
+    c->det[0] = t[0];
+    c->det[1] = t[1];
+  });
+}
+
+// A'yf by columns: aty_j = (K' yerg)_j / cs_j, stored, and sum |aty_j|.
+template <typename T>
+struct FarkasColEpi {
+  double* aty;
+  const double* cs;
+  double acc[1];
+  __device__ __forceinline__ void row(int j, const double (&s)[1]) {
+    const double a = s[0] / cs[j];
+    aty[j] = a;
+    acc[0] += fabs(a);
+  }
+  __device__ __forceinline__ void long_row(int lrow, int j, const double (&s)[1]) {
+    const double a = s[0] / cs[j];
+    aty[j] = a;
+    long_abs[lrow] = fabs(a);
+  }
+  double* long_abs;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) det_farkas_cols_kernel(Ctl* c, OpView<T> Kt,
+                                                                 IterView<T> it, EvalView ev,
+                                                                 RedView red, double* aty) {
+  if (c->done || !c->detect_pending) return;
+  FarkasColEpi<T> epi;
+  epi.aty = aty;
+  epi.cs = ev.cs;
+  epi.acc[0] = 0.0;
+  epi.long_abs = red.long_terms;
+  struct G {
+    const T* y;
+    __device__ __forceinline__ double operator()(int, T a, int i) const {
+      return static_cast<double>(a) * static_cast<double>(ldg(y + i));
+    }
+  } g{it.Yerg};
+  TileSmem<double, 1>& sm = tile_smem<double, 1>();
+  run_tiles<T, double, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi, sm);
+  const int nlong = Kt.ts.nlong;
+  const double* la = red.long_terms;
+  grid_reduce<1>(epi.acc, red.partial, red.counter, sm.red, [c, nlong, la](const double (&t)[1]) {
+    double s = t[0];
+    for (int l = 0; l < nlong; ++l) s += __ldcg(la + l);
+    // w_scale: columns first, then the logicals' |yf| (pdlp.cpp:761-767).
+    c->det[1] = s + c->det[1];
+  });
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) det_farkas_bounds_kernel(Ctl* c, IterView<T> it,
+                                                                   EvalView ev, RedView red,
+                                                                   const double* aty) {
+  if (c->done || !c->detect_pending) return;
+  __shared__ double scratch[kMaxSums * (kBlock / 32)];
+  const double y_max = c->det[0];
+  const double tol = 1e-9 * c->det[1];
+  const int n = it.n;
+  const int nt = n + it.m;
+  // min_f finite part, max_f finite part, min_f has -inf, max_f has +inf, scale
+  double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
+    const double raw = k < n ? aty[k] : -(static_cast<double>(it.Yerg[k - n]) * ev.rs[k - n]);
+    const double lo = ev.lower[k];
+    const double up = ev.upper[k];
+    const double coef = fabs(raw) <= tol ? 0.0 : raw;
+    if (coef > 0) {
+      if (lo > -INFINITY) a[0] += coef * lo; else a[2] = 1.0;
+      if (up < INFINITY) a[1] += coef * up; else a[3] = 1.0;
+    } else if (coef < 0) {
+      if (up < INFINITY) a[0] += coef * up; else a[2] = 1.0;
+      if (lo > -INFINITY) a[1] += coef * lo; else a[3] = 1.0;
+    }
+    const double w = k < n ? raw / y_max : -raw / y_max;
+    if (fabs(w) > 1e-9) {
+      if (lo > -INFINITY) a[4] = fmax(a[4], fabs(w * lo));
+      if (up < INFINITY) a[4] = fmax(a[4], fabs(w * up));
+    }
+  }
+  grid_reduce<5, 0x1Cu>(a, red.partial, red.counter, scratch, [c](const double (&t)[5]) {
+    const double min_f = t[2] > 0.0 ? -INFINITY : t[0];
+    const double max_f = t[3] > 0.0 ? INFINITY : t[1];
+    double scale = t[4];
+    if (!isfinite(scale)) scale = 0.0;
+    const double margin = 1e-8 * (1.0 + scale);
+    c->det[2] = min_f;
+    c->det[3] = max_f;
+    c->det[4] = scale;
+    const bool found = c->det[0] > 1e-6 && ((isfinite(min_f) && min_f > margin) ||
+                                            (isfinite(max_f) && max_f < -margin));
+    c->det_flags[0] = found ? 1 : 0;
+  });
+}
+
+// Ray candidate d = v_new - v: v_max = max |d|.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) det_ray_max_kernel(Ctl* c, IterView<T> it, RedView red) {
+  if (c->done || !c->detect_pending || c->det_flags[0]) return;
+  __shared__ double scratch[kMaxSums * (kBlock / 32)];
+  const int cur = static_cast<int>(((c->t + (c->max_iter - c->t < kCheckFrequency
+                                                  ? c->max_iter - c->t
+                                                  : kCheckFrequency))) & 1);
+  const T* vn = it.V[cur];
+  const T* vo = it.V[cur ^ 1];
+  const int nt = it.n + it.m;
+  double a[1] = {0.0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
+    a[0] = fmax(a[0], fabs(static_cast<double>(vn[k]) - static_cast<double>(vo[k])));
+  }
+  grid_reduce<1, 1u>(a, red.partial, red.counter, scratch,
+                     [c](const double (&t)[1]) { c->det[5] = t[0]; });
+}
+
+// Columns of the ray: cost_dir (structural part), bound checks and the polished ray x
+// (pdlp.cpp:887-964). ray_x (n) in the LpProblem's space.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) det_ray_cols_kernel(Ctl* c, IterView<T> it, EvalView ev,
+                                                              RedView red, double* ray_x) {
+  if (c->done || !c->detect_pending || c->det_flags[0]) return;
+  __shared__ double scratch[kMaxSums * (kBlock / 32)];
+  const int cur = static_cast<int>(((c->t + (c->max_iter - c->t < kCheckFrequency
+                                                  ? c->max_iter - c->t
+                                                  : kCheckFrequency))) & 1);
+  const T* vn = it.V[cur];
+  const T* vo = it.V[cur ^ 1];
+  const double v_max = c->det[5];
+  double a[2] = {0.0, 0.0};  // cost_dir (cols), bound failure
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < it.n; j += gridDim.x * blockDim.x) {
+    const double d = (static_cast<double>(vn[j]) - static_cast<double>(vo[j])) / v_max;
+    double xj = d * ev.cs[j];
+    a[0] += ev.cost[j] * xj;
+    const double lo = ev.lower[j];
+    const double up = ev.upper[j];
+    const bool lb = lo > -INFINITY / 2;
+    const bool ub = up < INFINITY / 2;
+    const bool fixed = lb && ub && (up - lo <= 1e-10 * (1.0 + fabs(lo)));
+    if (lb && ub) {
+      if (fabs(xj) > (fixed ? 1e-3 : 1e-4)) a[1] = 1.0;
+      xj = 0.0;
+    } else if (lb) {
+      if (xj < -1e-4) a[1] = 1.0;
+      xj = fmax(xj, 0.0);
+    } else if (ub) {
+      if (xj > 1e-4) a[1] = 1.0;
+      xj = fmin(xj, 0.0);
+    }
+    ray_x[j] = xj;
+  }
+  grid_reduce<2, 2u>(a, red.partial, red.counter, scratch, [c](const double (&t)[2]) {
+    c->det[7] = t[0];
+    c->det_flags[4] = t[1] > 0.0 ? 0 : 1;
+  });
+}
+
+// Rows of the ray: primal feasibility of the raw direction and cost_dir of the logicals
+// (NV 0: K d_x), and the row bounds of the polished ray (NV 1: K (ray_x / cs)).
+template <typename T>
+struct RayRowEpi {
+  const T* vn;
+  const T* vo;
+  double inv_vmax;
+  EvalView ev;
+  int n;
+  double acc[3];  // primal_feas^2, cost_dir (rows), row failure
+  double* long_terms;
+  __device__ __forceinline__ void terms(int i, const double (&s)[2], double (&a)[3]) {
+    const double rs = ev.rs[i];
+    const double dr = (static_cast<double>(vn[n + i]) - static_cast<double>(vo[n + i])) * inv_vmax;
+    const double res = s[0] / rs - dr / rs;
+    a[0] += res * res;
+    a[1] += ev.cost[n + i] * (dr / rs);
+    const double av = s[1] / rs;
+    const double lo = ev.lower[n + i];
+    const double up = ev.upper[n + i];
+    const bool lb = lo > -INFINITY / 2;
+    const bool ub = up < INFINITY / 2;
+    const bool fixed = lb && ub && (up - lo <= 1e-10 * (1.0 + fabs(lo)));
+    if (lb && ub) {
+      if (fabs(av) > (fixed ? 1e-3 : 1e-4)) a[2] = 1.0;
+    } else if (lb) {
+      if (av < -1e-4) a[2] = 1.0;
+    } else if (ub) {
+      if (av > 1e-4) a[2] = 1.0;
+    }
+  }
+  __device__ __forceinline__ void row(int i, const double (&s)[2]) { terms(i, s, acc); }
+  __device__ __forceinline__ void long_row(int lrow, int i, const double (&s)[2]) {
+    double a[3] = {0.0, 0.0, 0.0};
+    terms(i, s, a);
+    for (int q = 0; q < 3; ++q) long_terms[lrow * kMaxSums + q] = a[q];
+  }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) det_ray_rows_kernel(Ctl* c, OpView<T> K, IterView<T> it,
+                                                              EvalView ev, RedView red,
+                                                              const double* ray_x) {
+  if (c->done || !c->detect_pending || c->det_flags[0]) return;
+  const int cur = static_cast<int>(((c->t + (c->max_iter - c->t < kCheckFrequency
+                                                  ? c->max_iter - c->t
+                                                  : kCheckFrequency))) & 1);
+  RayRowEpi<T> epi;
+  epi.vn = it.V[cur];
+  epi.vo = it.V[cur ^ 1];
+  epi.inv_vmax = 1.0;
+  const double v_max = c->det[5];
+  epi.ev = ev;
+  epi.n = it.n;
+  epi.acc[0] = epi.acc[1] = epi.acc[2] = 0.0;
+  epi.long_terms = red.long_terms;
+  struct G {
+    const T* vn;
+    const T* vo;
+    const double* ray_x;
+    const double* cs;
+    double v_max;
+    __device__ __forceinline__ double operator()(int v, T a, int j) const {
+      if (v == 0) {
+        const double d = (static_cast<double>(vn[j]) - static_cast<double>(vo[j])) / v_max;
+        return static_cast<double>(a) * d;
+      }
+      return static_cast<double>(a) * (ray_x[j] / cs[j]);
+    }
+  } g{epi.vn, epi.vo, ray_x, ev.cs, v_max};
+  epi.inv_vmax = 1.0 / v_max;
+  TileSmem<double, 2>& sm = tile_smem<double, 2>();
+  run_tiles<T, double, 2>(K.ts, K.ptr, K.idx, K.val, g, epi, sm);
+  const int nlong = K.ts.nlong;
+  const double* lt = red.long_terms;
+  grid_reduce<3, 4u>(epi.acc, red.partial, red.counter, sm.red,
+                     [c, nlong, lt](const double (&t)[3]) {
+    double pf = t[0], cd = t[1], fail = t[2];
+    for (int l = 0; l < nlong; ++l) {
+      pf += __ldcg(lt + l * kMaxSums + 0);
+      cd += __ldcg(lt + l * kMaxSums + 1);
+      fail = fmax(fail, __ldcg(lt + l * kMaxSums + 2));
+    }
+    const double primal_feas = sqrt(pf);
+    const double cost_dir = c->det[7] + cd;
+    c->det[6] = primal_feas;
+    c->det[7] = cost_dir;
+    const bool ok = c->det_flags[4] != 0 && !(fail > 0.0);
+    c->det_flags[1] = (c->det[5] > 1e-6 && primal_feas < 1e-6 && cost_dir < -1e-8 && ok) ? 1 : 0;
+  });
+}
+
+// ------------------------------------------------------------------------------------------
+// Setup on the device (pdlp.cpp:36-187, 289-299, 377-394, 490-492), FP64.
+
+struct MaxNormEpi {
+  double acc[1];
+  __device__ __forceinline__ void row(int, const double (&s)[1]) { acc[0] = fmax(acc[0], sqrt(s[0])); }
+  __device__ __forceinline__ void long_row(int, int, const double (&s)[1]) {
+    acc[0] = fmax(acc[0], sqrt(s[0]));
+  }
+};
+
+struct SqProd {
+  __device__ __forceinline__ double operator()(int, double a, int) const { return a * a; }
+};
+
+__global__ void __launch_bounds__(kBlock) max_norm_kernel(OpView<double> A, RedView red,
+                                                          double* out) {
+  MaxNormEpi epi;
+  epi.acc[0] = 0.0;
+  TileSmem<double, 1>& sm = tile_smem<double, 1>();
+  run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, SqProd{}, epi, sm);
+  grid_reduce<1, 1u>(epi.acc, red.partial, red.counter, sm.red,
+                     [out](const double (&t)[1]) { *out = t[0]; });
+}
+
+__global__ void __launch_bounds__(kBlock) sum_sq_kernel(const double* x, int len, RedView red,
+                                                        double* out_sqrt) {
+  __shared__ double scratch[kMaxSums * (kBlock / 32)];
+  double a[1] = {0.0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < len; k += gridDim.x * blockDim.x) {
+    a[0] += x[k] * x[k];
+  }
+  grid_reduce<1>(a, red.partial, red.counter, scratch,
+                 [out_sqrt](const double (&t)[1]) { *out_sqrt = sqrt(t[0]); });
+}
+
+// Ruiz norms of D_r A D_c: product (a * scale[col])^2, row norm = rowscale * sqrt(sum).
+struct RuizProd {
+  const double* other;
+  __device__ __forceinline__ double operator()(int, double a, int j) const {
+    const double v = a * other[j];
+    return v * v;
+  }
+};
+
+struct RuizEpi {
+  const double* own;
+  double* norm;
+  __device__ __forceinline__ void row(int r, const double (&s)[1]) { norm[r] = sqrt(s[0]) * own[r]; }
+  __device__ __forceinline__ void long_row(int, int r, const double (&s)[1]) { row(r, s); }
+};
+
+__global__ void __launch_bounds__(kBlock) ruiz_norm_kernel(const Ctl* c, OpView<double> A,
+                                                           const double* own, const double* other,
+                                                           double* norm) {
+  if (c->ruiz_done) return;
+  RuizEpi epi{own, norm};
+  run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, RuizProd{other}, epi,
+                               tile_smem<double, 1>());
+}
+
+// Scale update of one Ruiz pass (pdlp.cpp:154-178) over columns then rows.
+__global__ void __launch_bounds__(kBlock) ruiz_update_kernel(Ctl* c, int n, int m, double* cs,
+                                                             const double* cn, double* rs,
+                                                             const double* rn, RedView red) {
+  if (c->ruiz_done) return;
+  __shared__ double scratch[kMaxSums * (kBlock / 32)];
+  double a[1] = {0.0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n + m; k += gridDim.x * blockDim.x) {
+    double* sc = k < n ? cs + k : rs + (k - n);
+    const double nv = k < n ? cn[k] : rn[k - n];
+    if (nv > 0) {
+      const double old = *sc;
+      double s = old / nv;
+      s = fmax(1e-8, fmin(1e8, s));
+      if (fabs(s - old) / fmax(fabs(old), 1.0) > 0.1) a[0] = 1.0;
+      *sc = s;
+    }
+  }
+  grid_reduce<1, 1u>(a, red.partial, red.counter, scratch,
+                     [c](const double (&t)[1]) { c->ruiz_done = t[0] > 0.0 ? 0 : 1; });
+}
+
+// A_eq = D_r A D_c on both operators: K entries (a rs_i) cs_j, K' entries (a cs_j) rs_i, the
+// association of apply_equilibration for A and A' (pdlp.cpp:204, 265-266). Rows by binary
+// search in the row starts.
+__device__ __forceinline__ int row_of(const int* ptr, int rows, int k) {
+  int lo = 0, hi = rows;  // ptr[lo] <= k < ptr[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (ptr[mid] <= k) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void apply_scaling_kernel(OpView<double> K, OpView<double> Kt, const double* rs,
+                                     const double* cs, long long nnz) {
+  for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nnz;
+       k += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int kk = static_cast<int>(k);
+    const int i = row_of(K.ptr, K.rows, kk);
+    const int j = K.idx[kk];
+    K.val[kk] = K.val[kk] * rs[i] * cs[j];
+    const int jj = row_of(Kt.ptr, Kt.rows, kk);
+    const int ii = Kt.idx[kk];
+    Kt.val[kk] = Kt.val[kk] * cs[jj] * rs[ii];
+  }
+}
+
+__global__ void scale_vectors_kernel(int n, int m, const double* cs, const double* rs,
+                                     const double* cost, const double* lower, const double* upper,
+                                     const double* rhs, double* cost_eq, double* lower_eq,
+                                     double* upper_eq, double* rhs_eq) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n + m; k += gridDim.x * blockDim.x) {
+    if (k < n) {
+      cost_eq[k] = cost[k] * cs[k];
+      lower_eq[k] = lower[k] / cs[k];
+      upper_eq[k] = upper[k] / cs[k];
+    } else {
+      const double r = rs[k - n];
+      cost_eq[k] = cost[k] * r;
+      lower_eq[k] = lower[k] * r;
+      upper_eq[k] = upper[k] * r;
+      if (rhs != nullptr) rhs_eq[k - n] = rhs[k - n] * r;
+    }
+  }
+}
+
+// Power iteration (pdlp.cpp:36-103) on A_eq: v = A' u, u = A v, sigma = |u| / |v|.
+struct StoreSqEpi {
+  double* out;
+  double acc[1];
+  double* long_terms;
+  __device__ __forceinline__ void row(int r, const double (&s)[1]) {
+    out[r] = s[0];
+    acc[0] += s[0] * s[0];
+  }
+  __device__ __forceinline__ void long_row(int lrow, int r, const double (&s)[1]) {
+    out[r] = s[0];
+    long_terms[lrow * kMaxSums] = s[0] * s[0];
+  }
+};
+
+__global__ void __launch_bounds__(kBlock) power_spmv_kernel(Ctl* c, OpView<double> A,
+                                                            const double* x, double* y,
+                                                            RedView red, int which) {
+  if (c->power_done) return;
+  StoreSqEpi epi;
+  epi.out = y;
+  epi.acc[0] = 0.0;
+  epi.long_terms = red.long_terms;
+  TileSmem<double, 1>& sm = tile_smem<double, 1>();
+  run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, Gather1<double, double>{x}, epi, sm);
+  const int nlong = A.ts.nlong;
+  const double* lt = red.long_terms;
+  grid_reduce<1>(epi.acc, red.partial, red.counter, sm.red,
+                 [c, nlong, lt, which](const double (&t)[1]) {
+    double s = t[0];
+    for (int l = 0; l < nlong; ++l) s += __ldcg(lt + l * kMaxSums);
+    const double nrm = sqrt(s);
+    if (which == 0) {
+      c->power_vnorm = nrm;
+      if (nrm == 0.0) c->power_done = 1;
+    } else {
+      c->power_unorm = nrm;
+      if (nrm == 0.0) {
+        c->power_done = 1;
+      } else {
+        c->power_sigma = nrm / c->power_vnorm;
+      }
+    }
+  });
+}
+
+__global__ void scale_by_norm_kernel(const Ctl* c, double* u, int m, int first) {
+  if (!first && c->power_done) return;
+  const double nrm = c->power_unorm;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    u[i] = u[i] / nrm;
+  }
+}
+
+__global__ void power_finish_kernel(Ctl* c) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double L = 1.0;
+  if (c->m > 0 && !c->power_done) {
+    const double la = c->power_sigma * 1.01;
+    L = sqrt(la * la + 1.0);
+  } else if (c->m > 0 && c->power_done && c->power_sigma > 0.0) {
+    // A zero vector after some iterations: the reference returns 1 (pdlp.cpp:74, 92).
+    L = 1.0;
+  }
+  c->op_norm = L;
+  c->eta = 0.99 / L;
+  c->omega = 1.0;
+  c->tau = c->eta;
+  c->sigma = c->eta;
+}
+
+__global__ void init_state_kernel(Ctl* c) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  c->t = 0;
+  c->k = 0;
+  c->kkt_at_restart = INFINITY;
+  c->kkt_previous = INFINITY;
+  c->status = kRunning;
+  c->done = 0;
+  c->result_average = 0;
+  c->restart_pending = 0;
+  c->detect_pending = 0;
+  c->iterations = 0;
+  c->restarts = 0;
+  c->evaluations = 0;
+  c->res[0] = c->res[1] = c->res[2] = 0.0;
+}
+
+template <typename Src, typename Dst>
+__global__ void convert_kernel(const Src* src, Dst* dst, long long count) {
+  for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < count;
+       k += static_cast<long long>(gridDim.x) * blockDim.x) {
+    dst[k] = static_cast<Dst>(src[k]);
+  }
+}
+
+struct StoreEpi {
+  double* out;
+  __device__ __forceinline__ void row(int r, const double (&s)[1]) { out[r] = s[0]; }
+  __device__ __forceinline__ void long_row(int, int r, const double (&s)[1]) { out[r] = s[0]; }
+};
+
+__global__ void __launch_bounds__(kBlock) spmv_kernel(OpView<double> A, const double* x,
+                                                      double* y) {
+  StoreEpi epi{y};
+  run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, Gather1<double, double>{x}, epi,
+                               tile_smem<double, 1>());
+}
+
+int vec_grid(long long len) {
+  long long g = (len + kBlock - 1) / kBlock;
+  if (g < 1) g = 1;
+  if (g > 4096) g = 4096;
+  return static_cast<int>(g);
+}
+
+}  // namespace
+
+size_t tile_smem_bytes(int nv, bool fp64) {
+  if (fp64) return nv == 1 ? sizeof(TileSmem<double, 1>) : sizeof(TileSmem<double, 2>);
+  return nv == 1 ? sizeof(TileSmem<float, 1>) : sizeof(TileSmem<double, 2>);
+}
+
+void configure_kernels() {
+  const int big = static_cast<int>(sizeof(TileSmem<double, 2>));
+  const int one = static_cast<int>(sizeof(TileSmem<double, 1>));
+  cudaFuncSetAttribute(eval_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(eval_cols_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(eval_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(eval_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(det_ray_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(det_ray_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(dual_step_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
+  cudaFuncSetAttribute(primal_step_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
+  cudaFuncSetAttribute(det_farkas_cols_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
+  cudaFuncSetAttribute(det_farkas_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
+  cudaFuncSetAttribute(max_norm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
+  cudaFuncSetAttribute(ruiz_norm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
+  cudaFuncSetAttribute(power_spmv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
+  cudaFuncSetAttribute(spmv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
+}
+
+template <typename T>
+void launch_dual_step(const Ctl* ctl, const OpView<T>& K, const IterView<T>& it, int j, int grid,
+                      cudaStream_t s) {
+  if (K.ts.ntiles == 0) return;
+  const size_t sm = std::is_same<T, double>::value ? sizeof(TileSmem<double, 1>)
+                                                   : sizeof(TileSmem<float, 1>);
+  dual_step_kernel<T><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
+}
+
+template <typename T>
+void launch_primal_step(const Ctl* ctl, const OpView<T>& Kt, const IterView<T>& it, int j,
+                        int grid, cudaStream_t s) {
+  if (Kt.ts.ntiles == 0) return;
+  const size_t sm = std::is_same<T, double>::value ? sizeof(TileSmem<double, 1>)
+                                                   : sizeof(TileSmem<float, 1>);
+  primal_step_kernel<T><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
+}
+
+template <typename T>
+void launch_eval(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
+                 const EvalView& ev, const RedView& red, int grid_k, int grid_t,
+                 int fixed_parity, cudaStream_t s) {
+  const size_t sm = sizeof(TileSmem<double, 2>);
+  eval_rows_kernel<T><<<grid_k, kBlock, sm, s>>>(ctl, K, it, ev, red, fixed_parity);
+  eval_cols_kernel<T><<<grid_t, kBlock, sm, s>>>(ctl, Kt, it, ev, red, fixed_parity);
+}
+
+void launch_decide_a(Ctl* ctl, cudaStream_t s) { decide_a_kernel<<<1, 32, 0, s>>>(ctl); }
+void launch_decide_b(Ctl* ctl, cudaStream_t s) { decide_b_kernel<<<1, 32, 0, s>>>(ctl); }
+
+template <typename T>
+void launch_restart(const Ctl* ctl, const IterView<T>& it, cudaStream_t s) {
+  restart_kernel<T><<<vec_grid(it.n + it.m), kBlock, 0, s>>>(ctl, it);
+}
+
+template <typename T>
+void launch_detect(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
+                   const EvalView& ev, const RedView& red, double* scratch_n, double* scratch_nt,
+                   int grid_k, int grid_t, cudaStream_t s) {
+  (void)scratch_nt;
+  const int gm = vec_grid(it.m) < 1024 ? vec_grid(it.m) : 1024;
+  const int gn = vec_grid(it.n) < 1024 ? vec_grid(it.n) : 1024;
+  const int gnt = vec_grid(it.n + it.m) < 1024 ? vec_grid(it.n + it.m) : 1024;
+  det_farkas_rows_kernel<T><<<gm, kBlock, 0, s>>>(ctl, it, ev, red);
+  det_farkas_cols_kernel<T><<<grid_t, kBlock, sizeof(TileSmem<double, 1>), s>>>(ctl, Kt, it, ev,
+                                                                                red, scratch_n);
+  det_farkas_bounds_kernel<T><<<gnt, kBlock, 0, s>>>(ctl, it, ev, red, scratch_n);
+  det_ray_max_kernel<T><<<gnt, kBlock, 0, s>>>(ctl, it, red);
+  det_ray_cols_kernel<T><<<gn, kBlock, 0, s>>>(ctl, it, ev, red, scratch_n);
+  det_ray_rows_kernel<T><<<grid_k, kBlock, sizeof(TileSmem<double, 2>), s>>>(ctl, K, it, ev, red,
+                                                                             scratch_n);
+}
+
+template <typename T>
+void launch_extract(const Ctl* ctl, const IterView<T>& it, const EvalView& ev, double* x_out,
+                    double* y_out, double* dual_ray, double* primal_ray_src, cudaStream_t s) {
+  (void)primal_ray_src;
+  extract_kernel<T><<<vec_grid(it.n + it.m), kBlock, 0, s>>>(ctl, it, ev, x_out, y_out, dual_ray);
+}
+
+void launch_setup_norms(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt,
+                        const double* cost, const RedView& red, int grid_k, int grid_t,
+                        cudaStream_t s) {
+  const size_t sm = sizeof(TileSmem<double, 1>);
+  if (K.rows > 0) {
+    if (Kt.ts.ntiles > 0) max_norm_kernel<<<grid_t, kBlock, sm, s>>>(Kt, red, &ctl->a_norm_max_col);
+    if (K.ts.ntiles > 0) max_norm_kernel<<<grid_k, kBlock, sm, s>>>(K, red, &ctl->at_norm_max_row);
+  }
+  const int nt = K.rows + Kt.rows;
+  sum_sq_kernel<<<vec_grid(nt) < 1024 ? vec_grid(nt) : 1024, kBlock, 0, s>>>(cost, nt, red,
+                                                                          &ctl->c_norm);
+}
+
+void launch_ruiz_pass(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt, double* rs,
+                      double* cs, double* rn, double* cn, const RedView& red, int grid_k,
+                      int grid_t, cudaStream_t s) {
+  const size_t sm = sizeof(TileSmem<double, 1>);
+  // Column norms (rows of K'), then row norms (rows of K), both with the old scales.
+  ruiz_norm_kernel<<<grid_t, kBlock, sm, s>>>(ctl, Kt, cs, rs, cn);
+  ruiz_norm_kernel<<<grid_k, kBlock, sm, s>>>(ctl, K, rs, cs, rn);
+  const int nt = K.rows + Kt.rows;
+  ruiz_update_kernel<<<vec_grid(nt) < 1024 ? vec_grid(nt) : 1024, kBlock, 0, s>>>(
+      ctl, Kt.rows, K.rows, cs, cn, rs, rn, red);
+}
+
+void launch_apply_scaling(const OpView<double>& K, const OpView<double>& Kt, const double* rs,
+                          const double* cs, long long nnz, cudaStream_t s) {
+  if (nnz == 0) return;
+  apply_scaling_kernel<<<vec_grid(nnz), kBlock, 0, s>>>(K, Kt, rs, cs, nnz);
+}
+
+void launch_scale_vectors(int n, int m, const double* cs, const double* rs, const double* cost,
+                          const double* lower, const double* upper, const double* rhs,
+                          double* cost_eq, double* lower_eq, double* upper_eq, double* rhs_eq,
+                          cudaStream_t s) {
+  scale_vectors_kernel<<<vec_grid(n + m), kBlock, 0, s>>>(n, m, cs, rs, cost, lower, upper, rhs,
+                                                          cost_eq, lower_eq, upper_eq, rhs_eq);
+}
+
+void launch_power_iteration(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt,
+                            double* u, double* v, const RedView& red, int iters, int grid_k,
+                            int grid_t, cudaStream_t s) {
+  const int m = K.rows;
+  if (m > 0) {
+    const size_t sm = sizeof(TileSmem<double, 1>);
+    const int gm = vec_grid(m) < 1024 ? vec_grid(m) : 1024;
+    sum_sq_kernel<<<gm, kBlock, 0, s>>>(u, m, red, &ctl->power_unorm);
+    scale_by_norm_kernel<<<gm, kBlock, 0, s>>>(ctl, u, m, 1);
+    for (int it = 0; it < iters; ++it) {
+      if (Kt.ts.ntiles > 0) power_spmv_kernel<<<grid_t, kBlock, sm, s>>>(ctl, Kt, u, v, red, 0);
+      if (K.ts.ntiles > 0) power_spmv_kernel<<<grid_k, kBlock, sm, s>>>(ctl, K, v, u, red, 1);
+      scale_by_norm_kernel<<<gm, kBlock, 0, s>>>(ctl, u, m, 0);
+    }
+  }
+  power_finish_kernel<<<1, 32, 0, s>>>(ctl);
+}
+
+void launch_init_state(Ctl* ctl, cudaStream_t s) { init_state_kernel<<<1, 32, 0, s>>>(ctl); }
+
+void launch_set_deadline(Ctl* ctl, double seconds, cudaStream_t s) {
+  const double ns = seconds * 1e9;
+  const unsigned long long budget = ns > 1.8e19 ? 18000000000000000000ull
+                                                : static_cast<unsigned long long>(ns);
+  set_deadline_kernel<<<1, 32, 0, s>>>(ctl, budget);
+}
+
+template <typename Src, typename Dst>
+void launch_convert(const Src* src, Dst* dst, long long count, cudaStream_t s) {
+  if (count <= 0) return;
+  convert_kernel<Src, Dst><<<vec_grid(count), kBlock, 0, s>>>(src, dst, count);
+}
+
+void launch_spmv(const OpView<double>& A, const double* x, double* y, int grid, cudaStream_t s) {
+  if (A.ts.ntiles == 0) return;
+  spmv_kernel<<<grid, kBlock, sizeof(TileSmem<double, 1>), s>>>(A, x, y);
+}
+
+// Explicit instantiations.
+template void launch_dual_step<double>(const Ctl*, const OpView<double>&, const IterView<double>&,
+                                       int, int, cudaStream_t);
+template void launch_dual_step<float>(const Ctl*, const OpView<float>&, const IterView<float>&, int,
+                                      int, cudaStream_t);
+template void launch_primal_step<double>(const Ctl*, const OpView<double>&,
+                                         const IterView<double>&, int, int, cudaStream_t);
+template void launch_primal_step<float>(const Ctl*, const OpView<float>&, const IterView<float>&,
+                                        int, int, cudaStream_t);
+template void launch_eval<double>(Ctl*, const OpView<double>&, const OpView<double>&,
+                                  const IterView<double>&, const EvalView&, const RedView&, int,
+                                  int, int, cudaStream_t);
+template void launch_eval<float>(Ctl*, const OpView<float>&, const OpView<float>&,
+                                 const IterView<float>&, const EvalView&, const RedView&, int, int,
+                                 int, cudaStream_t);
+template void launch_restart<double>(const Ctl*, const IterView<double>&, cudaStream_t);
+template void launch_restart<float>(const Ctl*, const IterView<float>&, cudaStream_t);
+template void launch_detect<double>(Ctl*, const OpView<double>&, const OpView<double>&,
+                                    const IterView<double>&, const EvalView&, const RedView&,
+                                    double*, double*, int, int, cudaStream_t);
+template void launch_detect<float>(Ctl*, const OpView<float>&, const OpView<float>&,
+                                   const IterView<float>&, const EvalView&, const RedView&, double*,
+                                   double*, int, int, cudaStream_t);
+template void launch_extract<double>(const Ctl*, const IterView<double>&, const EvalView&, double*,
+                                     double*, double*, double*, cudaStream_t);
+template void launch_extract<float>(const Ctl*, const IterView<float>&, const EvalView&, double*,
+                                    double*, double*, double*, cudaStream_t);
+template void launch_convert<double, float>(const double*, float*, long long, cudaStream_t);
+template void launch_convert<float, double>(const float*, double*, long long, cudaStream_t);
+
+}  // namespace sg

@@ -1,0 +1,106 @@
+// Kernel interfaces of the GB300 PDLP engine (see sg_common.cuh for the HBM layout).
+#pragma once
+
+#include "sg_common.cuh"
+
+namespace sg {
+
+// An operator stored by rows (CSR) with its tile partition.
+template <typename T>
+struct OpView {
+  const int* ptr;
+  const int* idx;
+  T* val;
+  int rows;
+  TileSet ts;
+};
+
+// Iterates and the equilibrated problem vectors, in storage type T.
+template <typename T>
+struct IterView {
+  T* V[2];     // (x, r) ping-pong by step parity, n + m
+  T* Vbar;     // extrapolated point of the next step, n + m
+  T* Y[2];     // duals ping-pong, m
+  T* Verg;     // running average since the last restart, n + m
+  T* Yerg;     // m
+  T* Vrst;     // restart point, n + m
+  T* Yrst;     // m
+  const T* cost;   // n + m
+  const T* lower;  // n + m
+  const T* upper;  // n + m
+  const T* rhs;    // m right-hand side q of [A -I] v = q (null: zero)
+  int n, m;
+};
+
+// The data the evaluation maps iterates back with (FP64): equilibration factors and the
+// problem before equilibration.
+struct EvalView {
+  const double* cs;      // n
+  const double* rs;      // m
+  const double* cost;    // n + m
+  const double* lower;   // n + m
+  const double* upper;   // n + m
+  const double* rhs;     // m (null: zero)
+};
+
+// Scratch of the grid reductions.
+struct RedView {
+  double* partial;       // [max CTAs * kMaxSums]
+  unsigned* counter;     // [8]
+  double* long_terms;    // [nlong * kMaxSums]
+};
+
+constexpr int kEvalSums = 18;
+
+template <typename T>
+void launch_dual_step(const Ctl* ctl, const OpView<T>& K, const IterView<T>& it, int j,
+                      int grid, cudaStream_t s);
+template <typename T>
+void launch_primal_step(const Ctl* ctl, const OpView<T>& Kt, const IterView<T>& it, int j,
+                        int grid, cudaStream_t s);
+template <typename T>
+void launch_eval(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
+                 const EvalView& ev, const RedView& red, int grid_k, int grid_t,
+                 int fixed_parity, cudaStream_t s);
+void launch_decide_a(Ctl* ctl, cudaStream_t s);
+void launch_decide_b(Ctl* ctl, cudaStream_t s);
+template <typename T>
+void launch_restart(const Ctl* ctl, const IterView<T>& it, cudaStream_t s);
+template <typename T>
+void launch_detect(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
+                   const EvalView& ev, const RedView& red, double* scratch_n, double* scratch_nt,
+                   int grid_k, int grid_t, cudaStream_t s);
+template <typename T>
+void launch_extract(const Ctl* ctl, const IterView<T>& it, const EvalView& ev, double* x_out,
+                    double* y_out, double* dual_ray, double* primal_ray_src, cudaStream_t s);
+
+// Setup on the device (FP64 master copy).
+void launch_setup_norms(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt,
+                        const double* cost, const RedView& red, int grid_k, int grid_t,
+                        cudaStream_t s);
+void launch_ruiz_pass(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt, double* rs,
+                      double* cs, double* rn, double* cn, const RedView& red, int grid_k,
+                      int grid_t, cudaStream_t s);
+void launch_apply_scaling(const OpView<double>& K, const OpView<double>& Kt, const double* rs,
+                          const double* cs, long long nnz, cudaStream_t s);
+void launch_scale_vectors(int n, int m, const double* cs, const double* rs, const double* cost,
+                          const double* lower, const double* upper, const double* rhs,
+                          double* cost_eq, double* lower_eq, double* upper_eq, double* rhs_eq,
+                          cudaStream_t s);
+void launch_power_iteration(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt,
+                            double* u, double* v, const RedView& red, int iters, int grid_k,
+                            int grid_t, cudaStream_t s);
+void launch_init_state(Ctl* ctl, cudaStream_t s);
+void launch_set_deadline(Ctl* ctl, double seconds, cudaStream_t s);
+
+template <typename Src, typename Dst>
+void launch_convert(const Src* src, Dst* dst, long long count, cudaStream_t s);
+
+// Plain y = A x by rows through the tile kernel (diagnostics and the SpMV parity test).
+void launch_spmv(const OpView<double>& A, const double* x, double* y, int grid, cudaStream_t s);
+
+// Sizes of dynamic shared memory of the tile kernels.
+size_t tile_smem_bytes(int nv, bool fp64);
+void configure_kernels();
+
+}  // namespace sg

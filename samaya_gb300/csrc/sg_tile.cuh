@@ -1,0 +1,146 @@
+// Load-balanced, deterministic CSR tile kernel core with fused per-row epilogues.
+//
+// A CTA processes one tile at a time (persistent loop over tiles):
+//   phase A  streams the tile's nonzeros [k0, k1) with coalesced loads and stages the NV
+//            products prod(v, val, col) in shared memory;
+//   phase B  reduces each row's products inside the tile: `team` lanes per row (chosen from the
+//            tile's mean row length), lanes step by `team`, then a fixed shuffle tree;
+//   phase C  calls epi(row, sums) with one thread per row, so the epilogue's vector accesses
+//            (iterates, bounds, averages) are coalesced across the CTA.
+// A row longer than kTileNnz is cut into consecutive segment tiles; each segment's block sum
+// goes to TileSet::seg_part and the last segment to arrive (counter) adds the segments in tile
+// order and runs the epilogue (epi.long_row). Every sum is taken in a fixed order, so results do
+// not depend on scheduling and a re-run is bit-identical.
+#pragma once
+
+#include "sg_common.cuh"
+
+namespace sg {
+
+template <typename ACC, int NV>
+struct TileSmem {
+  ACC prod[NV][kTileNnz];
+  ACC rows[NV][kTileRows];
+  double red[kMaxSums * (kBlock / 32)];
+};
+
+// Iterates over tiles. Prod: ACC operator()(int v, T val, int col) const.
+// Epi: void row(int r, const ACC (&s)[NV]) for rows of kind-0 tiles (called by one thread),
+//      void long_row(int lrow, int r, const ACC (&s)[NV]) for a split row (thread 0 of the CTA
+//      that completes it).
+template <typename T, typename ACC, int NV, typename Prod, typename Epi>
+__device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restrict__ ptr,
+                                          const int* __restrict__ idx,
+                                          const T* __restrict__ val, const Prod& prod, Epi& epi,
+                                          TileSmem<ACC, NV>& sm) {
+  const int tid = threadIdx.x;
+  for (int ti = blockIdx.x; ti < ts.ntiles; ti += gridDim.x) {
+    const Tile tile = ts.tiles[ti];
+    const int k0 = tile.k0;
+    const int len = tile.k1 - k0;
+    // Phase A: coalesced stream of the tile's nonzeros (4 independent loads in flight per
+    // thread).
+    {
+      int q = tid;
+      for (; q + 3 * kBlock < len; q += 4 * kBlock) {
+        const T a0 = ldg(val + k0 + q);
+        const T a1 = ldg(val + k0 + q + kBlock);
+        const T a2 = ldg(val + k0 + q + 2 * kBlock);
+        const T a3 = ldg(val + k0 + q + 3 * kBlock);
+        const int j0 = ldg(idx + k0 + q);
+        const int j1 = ldg(idx + k0 + q + kBlock);
+        const int j2 = ldg(idx + k0 + q + 2 * kBlock);
+        const int j3 = ldg(idx + k0 + q + 3 * kBlock);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          sm.prod[v][q] = prod(v, a0, j0);
+          sm.prod[v][q + kBlock] = prod(v, a1, j1);
+          sm.prod[v][q + 2 * kBlock] = prod(v, a2, j2);
+          sm.prod[v][q + 3 * kBlock] = prod(v, a3, j3);
+        }
+      }
+      for (; q < len; q += kBlock) {
+        const T a = ldg(val + k0 + q);
+        const int j = ldg(idx + k0 + q);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) sm.prod[v][q] = prod(v, a, j);
+      }
+    }
+    __syncthreads();
+    if (tile.kind == 0) {
+      // Phase B: team-per-row reduction in shared memory.
+      const int team = tile.team;
+      const int nteams = kBlock / team;
+      const int my_team = tid / team;
+      const int lane = tid % team;
+      const int nrows = tile.r1 - tile.r0;
+      const int rounds = (nrows + nteams - 1) / nteams;
+      for (int rr = 0; rr < rounds; ++rr) {
+        const int lr = rr * nteams + my_team;
+        ACC s[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) s[v] = ACC(0);
+        if (lr < nrows) {
+          const int b = ldg(ptr + tile.r0 + lr) - k0;
+          const int e = ldg(ptr + tile.r0 + lr + 1) - k0;
+          for (int q = b + lane; q < e; q += team) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) s[v] += sm.prod[v][q];
+          }
+        }
+        for (int o = team / 2; o > 0; o >>= 1) {
+#pragma unroll
+          for (int v = 0; v < NV; ++v) s[v] += __shfl_down_sync(0xffffffffu, s[v], o, team);
+        }
+        if (lane == 0 && lr < nrows) {
+#pragma unroll
+          for (int v = 0; v < NV; ++v) sm.rows[v][lr] = s[v];
+        }
+      }
+      __syncthreads();
+      // Phase C: epilogue, one thread per row.
+      for (int lr = tid; lr < nrows; lr += kBlock) {
+        ACC s[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) s[v] = sm.rows[v][lr];
+        epi.row(tile.r0 + lr, s);
+      }
+    } else {
+      // A segment of a long row: block sum in a fixed order.
+      double part[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        ACC s = ACC(0);
+        for (int q = tid; q < len; q += kBlock) s += sm.prod[v][q];
+        part[v] = static_cast<double>(s);
+      }
+      double tot[NV];
+      block_sum<NV>(part, sm.red, tot);
+      __shared__ bool last_seg;
+      if (tid == 0) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) ts.seg_part[ti * kMaxVec + v] = tot[v];
+        __threadfence();
+        const unsigned prev = atomicAdd(ts.lcount + tile.lrow, 1u);
+        last_seg = (prev == static_cast<unsigned>(tile.nseg - 1));
+      }
+      __syncthreads();
+      if (last_seg && tid == 0) {
+        __threadfence();
+        const int first = ti - tile.seg;
+        ACC s[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          double acc = 0.0;
+          for (int g = 0; g < tile.nseg; ++g) acc += __ldcg(ts.seg_part + (first + g) * kMaxVec + v);
+          s[v] = static_cast<ACC>(acc);
+        }
+        ts.lcount[tile.lrow] = 0u;
+        epi.long_row(tile.lrow, tile.r0, s);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace sg

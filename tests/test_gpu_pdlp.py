@@ -1,0 +1,141 @@
+"""End-to-end parity of the GPU PDLP engine with the reference's CPU PDLP (golden fixtures made
+from the reference's own code) and with its simplex oracles — the counterparts of the
+reference's tests/test_pdlp.cpp and tests/test_gpu.cpp solve tests."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import load_group
+
+pytestmark = pytest.mark.gpu
+
+
+def model_objective(case, x):
+    """Objective in the model's space of a PDLP answer x (LpProblem space): x_model = x * col
+    scale, obj = offset + c'x (tests/test_pdlp.cpp:105-127)."""
+    m = case.model
+    xm = x[:m.n] * case.col_scale
+    return m.obj_offset + float(np.dot(m.obj, xm))
+
+
+def solve(engine, case, **kw):
+    opts = engine.PdlpOptions(tol=case.tol, max_iterations=case.max_iter, **kw)
+    return engine.solve_pdlp(case.lp, opts)
+
+
+def test_basic_box_lp(engine):
+    """pdlp_basic (tests/test_pdlp.cpp:54-83): min x, 1 <= x <= 2, no rows."""
+    case = load_group("basic")[0]
+    r = solve(engine, case)
+    assert r.status == engine.OPTIMAL
+    assert r.iterations > 0
+    assert r.primal_residual < case.tol and r.dual_residual < case.tol and r.gap < case.tol
+    assert abs(r.x[0] - 1.0) < 1e-4
+
+
+def test_random_feasible_objectives_and_iterations(engine):
+    """pdlp_random_feasible (tests/test_pdlp.cpp:85-232): 50 LPs at 1e-8; every optimum's
+    objective within 1e-6 (1 + |ref|) of the dense reference simplex, statuses agree with the
+    reference's CPU PDLP, and the mean iteration count stays at most 1500."""
+    optimal, iters, mismatches = 0, 0, []
+    for case in load_group("feasible8"):
+        r = solve(engine, case)
+        if r.status != case.ref_status:
+            mismatches.append((case.k, r.status, case.ref_status))
+            continue
+        if r.status == engine.OPTIMAL:
+            st, ref_obj = case.refnlp
+            assert int(st) == 0
+            obj = model_objective(case, r.x)
+            if abs(obj - ref_obj) > 1e-6 * (1 + abs(ref_obj)):
+                mismatches.append((case.k, obj, ref_obj))
+            optimal += 1
+            iters += r.iterations
+    assert not mismatches, mismatches
+    assert optimal > 10
+    assert iters / optimal <= 1500
+
+
+def test_against_reference_cpu_pdlp_at_1e4(engine):
+    """pdlp_vs_simplex (tests/test_pdlp.cpp:234-400) LPs at 1e-4: same status as the reference's
+    CPU PDLP; optimal objectives within 1e-4 relative of the reference dual simplex."""
+    bad = []
+    for case in load_group("vs_simplex10"):
+        r = solve(engine, case)
+        if r.status != case.ref_status:
+            bad.append(("status", case.k, r.status, case.ref_status))
+            continue
+        if r.status == engine.OPTIMAL and case.simplex is not None and int(case.simplex[0]) == 0:
+            obj = model_objective(case, r.x)
+            ref_obj = float(case.simplex[1])
+            if abs(obj - ref_obj) > 1e-4 * (1 + abs(ref_obj)) * 10:
+                bad.append(("objective", case.k, obj, ref_obj))
+    assert not bad, bad
+
+
+def test_gpu_matches_cpu_solutions(engine):
+    """gpu_pdlp_vs_cpu (tests/test_gpu.cpp:407-477): at 1e-6 the GPU answer's x matches the CPU
+    PDLP's x within 1e-4 relative on every LP both solve."""
+    passed = total = 0
+    for case in load_group("gpu_vs_cpu6"):
+        if case.refnlp is None or int(case.refnlp[0]) != 0:
+            continue
+        total += 1
+        r = solve(engine, case)
+        if r.status == case.ref_status == engine.OPTIMAL:
+            n = case.lp.n
+            rel = np.abs(r.x[:n] - case.ref_x[:n]) / np.maximum(
+                1.0, np.maximum(np.abs(r.x[:n]), np.abs(case.ref_x[:n])))
+            passed += int(rel.max() <= 1e-4)
+        elif r.status == case.ref_status:
+            passed += 1
+    assert total > 0 and passed == total
+
+
+def test_runs_are_bit_repeatable(engine):
+    """gpu_pdlp_runs_are_repeatable (tests/test_gpu.cpp:675-697): two solves give the same
+    iteration count and bit-identical x, y."""
+    for case in load_group("repeatable30"):
+        with engine.PdlpSolver(case.lp, engine.PdlpOptions(tol=case.tol,
+                                                           max_iterations=case.max_iter)) as s:
+            a = s.solve()
+            b = s.solve()
+        c = solve(engine, case)
+        assert a.status == b.status == c.status
+        assert a.iterations == b.iterations == c.iterations
+        assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)
+        assert np.array_equal(a.x, c.x) and np.array_equal(a.y, c.y)
+
+
+def test_infeasible_and_unbounded_detection(engine):
+    """pdlp_infeasible_unbounded (tests/test_pdlp.cpp:402-478): the device-side Farkas and ray
+    checks detect the certificates the reference's CPU PDLP detects."""
+    detected = {1: 0, 2: 0}
+    agree = total = 0
+    for group, status in (("infeasible8", 1), ("loose8", 2)):
+        for case in load_group(group):
+            if case.refnlp is None or int(case.refnlp[0]) != status:
+                continue
+            r = solve(engine, case)
+            total += 1
+            agree += int(r.status == case.ref_status)
+            if r.status == status:
+                detected[status] += 1
+                if status == 1:
+                    assert r.dual_ray.shape == (case.lp.m,)
+                else:
+                    assert r.primal_ray.shape == (case.lp.n,)
+    assert detected[1] > 0 and detected[2] > 0
+    assert agree >= int(0.8 * total)
+
+
+def test_random_sparse_lp_objective_vs_dual_simplex(engine):
+    """The 200 x 500 random sparse LPs at 1e-4: objective within 1e-4 relative of the reference
+    dual simplex (the benchmark spec's bar for the plain path)."""
+    for case in load_group("config0_small"):
+        r = solve(engine, case)
+        assert r.status == engine.OPTIMAL
+        ref_obj = float(case.simplex[1])
+        obj = model_objective(case, r.x)
+        assert abs(obj - ref_obj) <= 1e-4 * (1 + abs(ref_obj)), (obj, ref_obj)
