@@ -62,7 +62,17 @@ typedef struct sg_pdlp_opts {
   int refine_max_rounds;     /* outer refinement rounds of the FP32 path (default 6) */
   double inner_tol;          /* tolerance of each FP32 inner solve (default 1e-4) */
   int verbose;               /* 0 silent */
+  int algorithm;             /* SG_ALGORITHM_* (default SG_ALGORITHM_REFERENCE) */
 } sg_pdlp_opts;
+
+/* Algorithm variants. REFERENCE follows samaya's PDLP step for step (L2 Ruiz, fixed step
+ * 0.99 / ||[A -I]||, primal weight 1 updated at restarts, the 0.2 / 0.8 / 0.36 restarts);
+ * ENHANCED replaces the preconditioning by infinity-norm Ruiz + Pock-Chambolle (alpha = 1)
+ * and starts the primal weight at |c| / |b|; everything else is the same. */
+enum {
+  SG_ALGORITHM_REFERENCE = 0,
+  SG_ALGORITHM_ENHANCED = 1
+};
 
 /* Result: the scalars of samaya::PdlpResult (reference src/lp/pdlp.hpp:19-30) plus counters. */
 typedef struct sg_pdlp_result {

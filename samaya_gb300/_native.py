@@ -22,7 +22,7 @@ class Opts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("max_iterations", ctypes.c_longlong),
                 ("time_limit", ctypes.c_double), ("precision", ctypes.c_int),
                 ("refine_max_rounds", ctypes.c_int), ("inner_tol", ctypes.c_double),
-                ("verbose", ctypes.c_int)]
+                ("verbose", ctypes.c_int), ("algorithm", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):

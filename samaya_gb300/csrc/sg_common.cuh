@@ -43,6 +43,8 @@ struct TileSet {
   int nlong;        // number of split rows
   double* seg_part; // [ntiles * kMaxVec] partial sums of long-row segments
   unsigned* lcount; // [nlong] arrival counters (reset by the last arrival)
+  int cap_nnz;      // nonzeros per tile at most (shared-memory staging capacity)
+  int cap_rows;     // rows per tile at most
 };
 
 constexpr int kMaxVec = 2;
@@ -102,6 +104,15 @@ struct Ctl {
   double det[8];
   int det_flags[8];
   double last_kkt;
+  // Iterative refinement (FP32 path): |q| of the inner problem's right-hand side (added to the
+  // primal scale; 0 for the reference problem), the residual maxima of the FP64 point, and the
+  // primal / dual scale factors of the current and previous correction problems.
+  double q_norm;
+  double ir_pmax, ir_dmax;
+  double ir_dp, ir_dd, ir_dp_prev, ir_dd_prev;
+  double ir_omega0;
+  int no_detect;  // 1: no infeasibility/unboundedness checks (the refinement's inner solves)
+  int pad1;
 };
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {

@@ -9,6 +9,7 @@
 #include <type_traits>
 
 #include "sg_engine.cuh"
+#include "sg_refine.cuh"
 
 namespace sg {
 
@@ -148,6 +149,13 @@ Engine::~Engine() {
                      &y_out_, &ray_out_, &partial_, &long_terms_}) {
     dfree(*p);
   }
+  for (double** p : {&ones_n_, &ones_m_, &cost_in_, &lower_in_, &upper_in_, &rhs_in_, &bh_,
+                     &dvec_}) {
+    dfree(*p);
+  }
+  if (chunk32_exec_) cudaGraphExecDestroy(chunk32_exec_);
+  if (chunk32_graph_) cudaGraphDestroy(chunk32_graph_);
+  dfree(ctl32_);
   dfree(counter_);
   dfree(ctl_);
   if (ctl_host_) cudaFreeHost(ctl_host_);
@@ -280,11 +288,23 @@ int Engine::create(Engine** out, int m, int n, const int64_t* colptr, const int3
   if (ce == cudaSuccess) ce = up(e->upper_orig_, upper, nt * sizeof(double));
   std::vector<double> u0 = power_start(m);
   if (ce == cudaSuccess) ce = up(e->u0_, u0.data(), u0.size() * sizeof(double));
-  // Tiles.
+  // Tiles: the capacity is a power of two between 256 and kTileNnz nonzeros chosen so each
+  // operator has about 8 tiles per SM (small problems spread over every SM; large ones stream
+  // long tiles); rows per tile at most half the nonzero capacity (at least 256).
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&e->sm_count_, cudaDevAttrMultiProcessorCount, dev);
+  }
   for (DevOp* op : {&e->K_, &e->Kt_}) {
+    const long long target = std::max<long long>(1, op->nnz / (8LL * e->sm_count_));
+    int cap = 256;
+    while (cap < kTileNnz && cap < target) cap *= 2;
+    op->cap_nnz = cap;
+    op->cap_rows = std::min(kTileRows, std::max(256, cap / 2));
     std::vector<Tile> tiles;
     int nlong = 0;
-    build_tiles(op->host_ptr, kTileNnz, kTileRows, &tiles, &nlong);
+    build_tiles(op->host_ptr, op->cap_nnz, op->cap_rows, &tiles, &nlong);
     op->ntiles = static_cast<int>(tiles.size());
     op->nlong = nlong;
     if (ce == cudaSuccess) ce = dalloc(&op->tiles, tiles.size());
@@ -346,6 +366,18 @@ int Engine::alloc_all(std::string* err) {
     for (float** p : {&it32_.Y[0], &it32_.Y[1], &it32_.Yerg, &it32_.Yrst, &it32_.rhs}) {
       SG_TRY(dalloc(p, m));
     }
+    for (double** p : {&cost_in_, &lower_in_, &upper_in_, &dvec_}) SG_TRY(dalloc(p, nt));
+    for (double** p : {&rhs_in_, &bh_, &ones_m_}) SG_TRY(dalloc(p, m));
+    SG_TRY(dalloc(&ones_n_, static_cast<size_t>(n_)));
+    {
+      std::vector<double> ones(std::max<size_t>(std::max<size_t>(m, n_), 1), 1.0);
+      SG_TRY(cudaMemcpy(ones_n_, ones.data(), static_cast<size_t>(n_) * sizeof(double),
+                        cudaMemcpyHostToDevice));
+      SG_TRY(cudaMemcpy(ones_m_, ones.data(), m * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    SG_TRY(dalloc(&ctl32_, 1));
+    SG_TRY(cudaMemsetAsync(ctl32_, 0, sizeof(Ctl), stream_));
+    configure_refine_kernels();
   }
   for (double** p : {&cost_orig_, &lower_orig_, &upper_orig_, &cost_ev_, &lower_ev_, &upper_ev_,
                      &x_out_, &scratch_n_}) {
@@ -454,8 +486,12 @@ int Engine::setup_device(const double* rhs_orig) {
   }
   launch_setup_norms(ctl_, K, Kt, cost_orig_, red, grid_k_, grid_t_, s);
   if (m_ > 0 && n_ > 0) {
-    for (int pass = 0; pass < 10; ++pass) {
-      launch_ruiz_pass(ctl_, K, Kt, rs_, cs_, rn_, cn_, red, grid_k_, grid_t_, s);
+    if (opt_.algorithm == 1) {
+      launch_enhanced_scaling(K, Kt, rs_, cs_, rn_, cn_, grid_k_, grid_t_, s);
+    } else {
+      for (int pass = 0; pass < 10; ++pass) {
+        launch_ruiz_pass(ctl_, K, Kt, rs_, cs_, rn_, cn_, red, grid_k_, grid_t_, s);
+      }
     }
   }
   launch_apply_scaling(K, Kt, rs_, cs_, nnz_, s);
@@ -466,6 +502,9 @@ int Engine::setup_device(const double* rhs_orig) {
                            cudaMemcpyDeviceToDevice, s));
   }
   launch_power_iteration(ctl_, K, Kt, pu_, pv_, red, 20, grid_k_, grid_t_, s);
+  if (opt_.algorithm == 1) {
+    launch_primal_weight_init(ctl_, n_, m_, it64_.cost, it64_.lower, it64_.upper, red, s);
+  }
   // Iterates start at zero (pdlp.cpp:323-329).
   for (double* p : {it64_.V[0], it64_.V[1], it64_.Vbar, it64_.Verg, it64_.Vrst}) {
     SG_TRY(cudaMemsetAsync(p, 0, nt * sizeof(double), s));
@@ -479,42 +518,34 @@ int Engine::setup_device(const double* rhs_orig) {
 
 // One chunk: kCheckFrequency fused iterations, the evaluation, the decisions, restart and
 // detection. Recorded once as a CUDA graph.
-void Engine::enqueue_chunk_body() {
-  cudaStream_t s = stream_;
-  const RedView red = red_view();
-  const EvalView ev = eval_view();
+namespace {
+
+// The kernels of one chunk; returns how many launches it records.
+template <typename T>
+int enqueue_chunk(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
+                  const EvalView& ev, const RedView& red, double* scratch_n, int gsk, int gst,
+                  int gk, int gt, cudaStream_t s) {
   int kernels = 0;
-  if (fp32_) {
-    const OpView<float> K = K_.view32();
-    const OpView<float> Kt = Kt_.view32();
-    IterView<float> it = iter_view(it32_);
-    for (int j = 0; j < kCheckFrequency; ++j) {
-      launch_dual_step(ctl_, K, it, j, grid_step_k_, s);
-      launch_primal_step(ctl_, Kt, it, j, grid_step_t_, s);
-      kernels += 2;
-    }
-    launch_eval(ctl_, K, Kt, it, ev, red, grid_k_, grid_t_, -1, s);
-    launch_decide_a(ctl_, s);
-    launch_detect(ctl_, K, Kt, it, ev, red, scratch_n_, nullptr, grid_k_, grid_t_, s);
-    launch_decide_b(ctl_, s);
-    launch_restart(ctl_, it, s);
-  } else {
-    const OpView<double> K = K_.view64();
-    const OpView<double> Kt = Kt_.view64();
-    IterView<double> it = iter_view(it64_);
-    for (int j = 0; j < kCheckFrequency; ++j) {
-      launch_dual_step(ctl_, K, it, j, grid_step_k_, s);
-      launch_primal_step(ctl_, Kt, it, j, grid_step_t_, s);
-      kernels += 2;
-    }
-    launch_eval(ctl_, K, Kt, it, ev, red, grid_k_, grid_t_, -1, s);
-    launch_decide_a(ctl_, s);
-    launch_detect(ctl_, K, Kt, it, ev, red, scratch_n_, nullptr, grid_k_, grid_t_, s);
-    launch_decide_b(ctl_, s);
-    launch_restart(ctl_, it, s);
+  for (int j = 0; j < kCheckFrequency; ++j) {
+    if (K.ts.ntiles > 0) ++kernels;
+    if (Kt.ts.ntiles > 0) ++kernels;
+    launch_dual_step(ctl, K, it, j, gsk, s);
+    launch_primal_step(ctl, Kt, it, j, gst, s);
   }
-  kernels += 2 + 1 + 6 + 1 + 1;
-  chunk_kernels_ = kernels;
+  launch_eval(ctl, K, Kt, it, ev, red, gk, gt, -1, s);
+  launch_decide_a(ctl, s);
+  launch_detect(ctl, K, Kt, it, ev, red, scratch_n, nullptr, gk, gt, s);
+  launch_decide_b(ctl, s);
+  launch_restart(ctl, it, s);
+  return kernels + 2 + 1 + 6 + 1 + 1;
+}
+
+}  // namespace
+
+void Engine::enqueue_chunk_body() {
+  chunk_kernels_ = enqueue_chunk(ctl_, K_.view64(), Kt_.view64(), iter_view(it64_), eval_view(),
+                                 red_view(), scratch_n_, grid_step_k_, grid_step_t_, grid_k_,
+                                 grid_t_, stream_);
 }
 
 int Engine::capture_chunk() {
@@ -527,9 +558,47 @@ int Engine::capture_chunk() {
   return kOk;
 }
 
-// Replays the chunk graph until the device says done, keeping a few chunks in flight; the
-// host only reads the status word back (an event per chunk).
-int Engine::run_loop(double deadline_s, SolveInfo* info) {
+// The FP32 inner solves' chunk: FP32 operators and iterates, the correction problem's
+// right-hand side, evaluation in the equilibrated space (unit scales), its own control block.
+int Engine::capture_chunk32() {
+  if (chunk32_exec_ != nullptr) return kOk;
+  std::string* err = nullptr;
+  IterView<float> it = iter_view(it32_);
+  it.rhs = it32_.rhs;
+  SG_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+  chunk32_kernels_ = enqueue_chunk(ctl32_, K_.view32(), Kt_.view32(), it, inner_eval_view(),
+                                   red_view(), scratch_n_, grid_step_k_, grid_step_t_, grid_k_,
+                                   grid_t_, stream_);
+  SG_TRY(cudaStreamEndCapture(stream_, &chunk32_graph_));
+  SG_TRY(cudaGraphInstantiate(&chunk32_exec_, chunk32_graph_, 0));
+  return kOk;
+}
+
+EvalView Engine::inner_eval_view() const {
+  EvalView ev;
+  ev.cs = ones_n_;
+  ev.rs = ones_m_;
+  ev.cost = cost_in_;
+  ev.lower = lower_in_;
+  ev.upper = upper_in_;
+  ev.rhs = rhs_in_;
+  return ev;
+}
+
+// The FP64 point of the refinement as an iterate (current = average = the point).
+IterView<double> Engine::master_view() {
+  IterView<double> v = iter_view(it64_);
+  v.V[1] = v.V[0];
+  v.Verg = v.V[0];
+  v.Y[1] = v.Y[0];
+  v.Yerg = v.Y[0];
+  return v;
+}
+
+// Replays a chunk graph until the device says done, keeping a few chunks in flight; the host
+// only reads the control block back (an event per chunk).
+int Engine::run_loop(double deadline_s, SolveInfo* info, cudaGraphExec_t exec, Ctl* ctl,
+                     int kernels_per_chunk, long long max_iter) {
   std::string* err = nullptr;
   constexpr int kInflight = 3;
   int head = 0;  // oldest in flight
@@ -538,17 +607,13 @@ int Engine::run_loop(double deadline_s, SolveInfo* info) {
   // Every chunk advances the device's iteration counter by kCheckFrequency until the limit, so
   // a correct run needs at most this many launches; the bound keeps the host loop finite even
   // if the device never reported done.
-  long long max_iter = opt_.max_iterations;
-  if (max_iter <= 0) {
-    max_iter = std::max<long long>(10000LL, 10000LL * (static_cast<long long>(m_) + n_) / 10);
-  }
   const long long launch_cap = max_iter / kCheckFrequency + 2 * kInflight + 4;
   for (;;) {
     if (launches >= launch_cap) break;
     while (count < kInflight) {
       const int slot = (head + count) % 4;
-      SG_TRY(cudaGraphLaunch(chunk_exec_, stream_));
-      SG_TRY(cudaMemcpyAsync(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_));
+      SG_TRY(cudaGraphLaunch(exec, stream_));
+      SG_TRY(cudaMemcpyAsync(ctl_host_, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_));
       SG_TRY(cudaEventRecord(ev_[slot], stream_));
       ++count;
       ++launches;
@@ -556,7 +621,7 @@ int Engine::run_loop(double deadline_s, SolveInfo* info) {
     SG_TRY(cudaEventSynchronize(ev_[head]));
     head = (head + 1) % 4;
     --count;
-    // ctl_host_ holds the latest completed copy (copies complete in stream order).
+    // The done flag of a completed copy (later copies only ever set it too).
     if (ctl_host_->done) break;
     if (deadline_s > 0 && now_s() > deadline_s) {
       // Host-side limit: let the device finish its in-flight chunks, then stop.
@@ -564,10 +629,9 @@ int Engine::run_loop(double deadline_s, SolveInfo* info) {
     }
   }
   SG_TRY(cudaStreamSynchronize(stream_));
-  SG_TRY(cudaStreamSynchronize(stream_));
-  SG_TRY(cudaMemcpy(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  SG_TRY(cudaMemcpy(ctl_host_, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
   info->graph_launches += launches;
-  info->kernel_launches += launches * chunk_kernels_;
+  info->kernel_launches += launches * kernels_per_chunk;
   return kOk;
 }
 
@@ -594,7 +658,7 @@ int Engine::solve_fp64(SolveInfo* info, double* x, double* y, double* dual_ray,
   const double deadline = opt_.time_limit > 0 ? t0 + opt_.time_limit : 0.0;
   const double t_setup = now_s();
   info->setup_seconds = t_setup - t0;
-  rc = run_loop(deadline, info);
+  rc = run_loop(deadline, info, chunk_exec_, ctl_, chunk_kernels_, max_iterations());
   if (rc != kOk) return rc;
   const Ctl& c = *ctl_host_;
   if (c.done == 0) {
@@ -654,14 +718,173 @@ int Engine::solve_fp64(SolveInfo* info, double* x, double* y, double* dual_ray,
   return kOk;
 }
 
+long long Engine::max_iterations() const {
+  long long max_iter = opt_.max_iterations;
+  if (max_iter <= 0) {
+    // pdlp.cpp:365-373.
+    max_iter = std::max<long long>(10000LL, 10000LL * (static_cast<long long>(m_) + n_) / 10);
+    if (!(opt_.time_limit > 0)) max_iter = std::min<long long>(max_iter, 1000000LL);
+  }
+  return max_iter;
+}
+
+namespace {
+
+// The reference's relative residuals and gap (pdlp.cpp:493-519) from the seven sums.
+void finish_host(const Ctl& c, const double* s, double* rp, double* rd, double* rg) {
+  const double primal_scale = 1.0 + c.a_norm_max_col * sqrt(s[4]) + sqrt(s[5]);
+  const double dual_scale = 1.0 + c.at_norm_max_row * sqrt(s[6]) + c.c_norm;
+  const double gap_scale = 1.0 + fabs(s[2]) + fabs(s[3]);
+  *rp = c.m > 0 ? sqrt(s[0]) / primal_scale : 0.0;
+  *rd = c.m > 0 ? sqrt(s[1]) / dual_scale : 0.0;
+  *rg = (s[2] - s[3]) / gap_scale;
+}
+
+}  // namespace
+
+// FP32 storage and arithmetic in the iterations, FP64 for the point, the residuals, the scale
+// factors and every decision: round 0 solves the problem itself in FP32 to the inner
+// tolerance, every later round an FP32 correction problem built from the FP64 residuals; the
+// FP64 point stops when it meets the reference's relative KKT test at the requested tolerance.
 int Engine::solve_refined(SolveInfo* info, double* x, double* y, double* dual_ray,
                           double* primal_ray) {
-  (void)info;
-  (void)x;
-  (void)y;
   (void)dual_ray;
   (void)primal_ray;
-  return kErrInternal;
+  std::string* err = nullptr;
+  const double t0 = now_s();
+  cudaStream_t s = stream_;
+  int rc = setup_device(nullptr);
+  if (rc != kOk) return rc;
+  const size_t nt = static_cast<size_t>(n_) + m_;
+  const size_t nb = static_cast<size_t>(nnz_);
+  // FP32 copies of the equilibrated operators.
+  launch_convert(K_.val, K_.val32, static_cast<long long>(nb), s);
+  launch_convert(Kt_.val, Kt_.val32, static_cast<long long>(nb), s);
+  // The inner solves' control block: the outer one's step size and initial weight, the norms of
+  // the equilibrated matrix for their relative residuals.
+  SG_TRY(cudaMemcpyAsync(ctl32_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToDevice, s));
+  launch_setup_norms(ctl32_, K_.view64(), Kt_.view64(), it64_.cost, red_view(), grid_k_, grid_t_,
+                     s);
+  SG_TRY(cudaStreamSynchronize(s));
+  {
+    Ctl h;
+    SG_TRY(cudaMemcpy(&h, ctl32_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    h.ir_omega0 = h.omega;
+    h.q_norm = 0.0;
+    SG_TRY(cudaMemcpy(ctl32_, &h, sizeof(Ctl), cudaMemcpyHostToDevice));
+  }
+  rc = capture_chunk32();
+  if (rc != kOk) return rc;
+  // The FP64 point starts at zero.
+  SG_TRY(cudaMemsetAsync(it64_.V[0], 0, nt * sizeof(double), s));
+  SG_TRY(cudaMemsetAsync(it64_.Y[0], 0, static_cast<size_t>(m_) * sizeof(double), s));
+  SG_TRY(cudaMemsetAsync(it64_.Vrst, 0, nt * sizeof(double), s));
+  SG_TRY(cudaMemsetAsync(it64_.Yrst, 0, static_cast<size_t>(m_) * sizeof(double), s));
+  IrView irv;
+  irv.v = it64_.V[0];
+  irv.y = it64_.Y[0];
+  irv.cost_eq = it64_.cost;
+  irv.lower_eq = it64_.lower;
+  irv.upper_eq = it64_.upper;
+  irv.bh = bh_;
+  irv.d = dvec_;
+  irv.cost_in = cost_in_;
+  irv.lower_in = lower_in_;
+  irv.upper_in = upper_in_;
+  irv.rhs_in = rhs_in_;
+  irv.cost32 = it32_.cost;
+  irv.lower32 = it32_.lower;
+  irv.upper32 = it32_.upper;
+  irv.rhs32 = it32_.rhs;
+  irv.red = red_view();
+  irv.n = n_;
+  irv.m = m_;
+  IterView<float> it32 = iter_view(it32_);
+  it32.rhs = it32_.rhs;
+  const IterView<double> master = master_view();
+  const long long inner_max = max_iterations();
+  const double deadline = opt_.time_limit > 0 ? t0 + opt_.time_limit : 0.0;
+  info->setup_seconds = now_s() - t0;
+  long long total_iters = 0;
+  double rp = INFINITY, rd = INFINITY, rg = INFINITY, pobj = 0.0, dobj = 0.0;
+  int status = kIterationLimit;
+  int rounds = 0;
+  for (int round = 0; round < opt_.refine_max_rounds; ++round) {
+    if (round > 0) {
+      launch_ir_residual(ctl32_, K_.view64(), Kt_.view64(), irv, grid_k_, grid_t_, s);
+    }
+    launch_ir_scales(ctl32_, round, 1e6, s);
+    launch_ir_build(ctl32_, irv, round, s);
+    for (float* p : {it32_.V[0], it32_.V[1], it32_.Vbar, it32_.Verg, it32_.Vrst}) {
+      SG_TRY(cudaMemsetAsync(p, 0, nt * sizeof(float), s));
+    }
+    for (float* p : {it32_.Y[0], it32_.Y[1], it32_.Yerg, it32_.Yrst}) {
+      SG_TRY(cudaMemsetAsync(p, 0, static_cast<size_t>(m_) * sizeof(float), s));
+    }
+    launch_norm_into(cost_in_, static_cast<long long>(nt), red_view(), &ctl32_->c_norm, s);
+    launch_norm_into(rhs_in_, m_, red_view(), &ctl32_->q_norm, s);
+    launch_ir_reset(ctl32_, opt_.inner_tol, inner_max, s);
+    if (opt_.time_limit > 0) launch_set_deadline(ctl32_, opt_.time_limit - (now_s() - t0), s);
+    rc = run_loop(deadline, info, chunk32_exec_, ctl32_, chunk32_kernels_, inner_max);
+    if (rc != kOk) return rc;
+    total_iters += ctl_host_->t;
+    info->restarts += ctl_host_->restarts;
+    info->evaluations += ctl_host_->evaluations;
+    info->omega = ctl_host_->omega;
+    launch_ir_update(ctl32_, it32, irv, round, s);
+    // FP64 evaluation of the original problem at the refined point.
+    launch_eval(ctl_, K_.view64(), Kt_.view64(), master, eval_view(), red_view(), grid_k_,
+                grid_t_, 0, s);
+    SG_TRY(cudaGetLastError());
+    SG_TRY(cudaStreamSynchronize(s));
+    Ctl h;
+    SG_TRY(cudaMemcpy(&h, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    double sums[7];
+    for (int q = 0; q < 7; ++q) sums[q] = h.eval_c[q] + h.eval_r[q];
+    finish_host(h, sums, &rp, &rd, &rg);
+    pobj = sums[2];
+    dobj = sums[3];
+    rounds = round + 1;
+    if (opt_.verbose) {
+      printf("refine round %d: %lld inner iterations, rel primal %.3e dual %.3e gap %.3e\n",
+             round, ctl_host_->t, rp, rd, rg);
+    }
+    if (rp < opt_.tol && rd < opt_.tol && fabs(rg) < opt_.tol) {
+      status = kOptimal;
+      break;
+    }
+    if (deadline > 0 && now_s() > deadline) {
+      status = kTimeLimit;
+      break;
+    }
+  }
+  info->status = status;
+  info->iterations = total_iters;
+  info->refinement_rounds = rounds;
+  info->rel_primal = rp;
+  info->rel_dual = rd;
+  info->rel_gap = rg;
+  info->primal_obj = pobj;
+  info->dual_obj = dobj;
+  {
+    Ctl h;
+    SG_TRY(cudaMemcpy(&h, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    info->step_size = h.eta;
+    info->operator_norm = h.op_norm;
+    h.t = 0;
+    h.result_average = 0;
+    SG_TRY(cudaMemcpy(ctl_, &h, sizeof(Ctl), cudaMemcpyHostToDevice));
+  }
+  launch_extract(ctl_, master, eval_view(), x_out_, y_out_, nullptr, nullptr, s);
+  SG_TRY(cudaGetLastError());
+  if (x) SG_TRY(cudaMemcpyAsync(x, x_out_, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (y && m_ > 0) {
+    SG_TRY(cudaMemcpyAsync(y, y_out_, static_cast<size_t>(m_) * sizeof(double),
+                           cudaMemcpyDeviceToHost, s));
+  }
+  SG_TRY(cudaStreamSynchronize(s));
+  info->solve_seconds = now_s() - t0;
+  return kOk;
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -33,6 +33,7 @@ struct Options {
   int refine_max_rounds = 6;
   double inner_tol = 1e-4;
   int verbose = 0;
+  int algorithm = 0;        // 0 the reference's PDLP, 1 enhanced preconditioning + weight
 };
 
 struct SolveInfo {
@@ -64,6 +65,8 @@ struct DevOp {
   int nlong = 0;
   double* seg_part = nullptr;
   unsigned* lcount = nullptr;
+  int cap_nnz = kTileNnz;
+  int cap_rows = kTileRows;
   std::vector<int> host_ptr;
 
   TileSet tileset() const {
@@ -73,6 +76,8 @@ struct DevOp {
     t.nlong = nlong;
     t.seg_part = seg_part;
     t.lcount = lcount;
+    t.cap_nnz = cap_nnz;
+    t.cap_rows = cap_rows;
     return t;
   }
   OpView<double> view64() const { return OpView<double>{ptr, idx, val, rows, tileset()}; }
@@ -136,7 +141,12 @@ class Engine {
   IterView<T> iter_view(DevIter<T>& it);
   EvalView eval_view() const;
   RedView red_view() const;
-  int run_loop(double deadline_s, SolveInfo* info);
+  int run_loop(double deadline_s, SolveInfo* info, cudaGraphExec_t exec, Ctl* ctl,
+               int kernels_per_chunk, long long max_iter);
+  int capture_chunk32();
+  long long max_iterations() const;
+  IterView<double> master_view();
+  EvalView inner_eval_view() const;
   int solve_fp64(SolveInfo* info, double* x, double* y, double* dual_ray, double* primal_ray);
   int solve_refined(SolveInfo* info, double* x, double* y, double* dual_ray, double* primal_ray);
   void enqueue_chunk_body();
@@ -182,6 +192,20 @@ class Engine {
   long long seam_steps_ = 0;
   bool seam_mode_ = false;
   cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+  // Mixed-precision path: the inner solves' control block and graph, the correction problem
+  // (FP64 evaluation copy), unit scales for its evaluation, and the residual vectors.
+  Ctl* ctl32_ = nullptr;
+  cudaGraphExec_t chunk32_exec_ = nullptr;
+  cudaGraph_t chunk32_graph_ = nullptr;
+  int chunk32_kernels_ = 0;
+  double* ones_n_ = nullptr;
+  double* ones_m_ = nullptr;
+  double* cost_in_ = nullptr;
+  double* lower_in_ = nullptr;
+  double* upper_in_ = nullptr;
+  double* rhs_in_ = nullptr;
+  double* bh_ = nullptr;
+  double* dvec_ = nullptr;
 };
 
 // Builds the tile partition of a CSR operator (host). Exposed for the CPU tests.

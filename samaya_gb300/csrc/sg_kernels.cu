@@ -16,12 +16,6 @@ namespace sg {
 
 namespace {
 
-template <typename ACC, int NV>
-__device__ __forceinline__ TileSmem<ACC, NV>& tile_smem() {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  return *reinterpret_cast<TileSmem<ACC, NV>*>(smem_raw);
-}
-
 template <typename T>
 __device__ __forceinline__ T clampv(T v, T lo, T hi) {
   return fmin(fmax(v, lo), hi);
@@ -141,7 +135,7 @@ __global__ void __launch_bounds__(kBlock) dual_step_kernel(const Ctl* __restrict
   epi.alpha = static_cast<ACC>(alpha);
   epi.beta = static_cast<ACC>(1.0 - alpha);
   Gather1<T, ACC> g{it.Vbar};
-  run_tiles<T, ACC, 1>(K.ts, K.ptr, K.idx, K.val, g, epi, tile_smem<ACC, 1>());
+  run_tiles<T, ACC, 1>(K.ts, K.ptr, K.idx, K.val, g, epi);
 }
 
 template <typename T>
@@ -166,7 +160,7 @@ __global__ void __launch_bounds__(kBlock) primal_step_kernel(const Ctl* __restri
   epi.alpha = static_cast<ACC>(alpha);
   epi.beta = static_cast<ACC>(1.0 - alpha);
   Gather1<T, ACC> g{it.Y[p ^ 1]};
-  run_tiles<T, ACC, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi, tile_smem<ACC, 1>());
+  run_tiles<T, ACC, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -307,10 +301,9 @@ __global__ void __launch_bounds__(kBlock) eval_rows_kernel(Ctl* ctl, OpView<T> K
 #pragma unroll
   for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0;
   Gather2<T> g{it.V[cur], it.Verg};
-  TileSmem<double, 2>& sm = tile_smem<double, 2>();
-  run_tiles<T, double, 2>(K.ts, K.ptr, K.idx, K.val, g, epi, sm);
+  run_tiles<T, double, 2>(K.ts, K.ptr, K.idx, K.val, g, epi);
   EvalFin fin{ctl->eval_r, red.long_terms, K.ts.nlong};
-  grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, sm.red, fin);
+  grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, smem_red(), fin);
 }
 
 template <typename T>
@@ -329,10 +322,9 @@ __global__ void __launch_bounds__(kBlock) eval_cols_kernel(Ctl* ctl, OpView<T> K
 #pragma unroll
   for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0;
   Gather2<T> g{it.Y[cur], it.Yerg};
-  TileSmem<double, 2>& sm = tile_smem<double, 2>();
-  run_tiles<T, double, 2>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi, sm);
+  run_tiles<T, double, 2>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
   EvalFin fin{ctl->eval_c, red.long_terms, Kt.ts.nlong};
-  grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, sm.red, fin);
+  grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, smem_red(), fin);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -348,7 +340,7 @@ __device__ Meas finish_sums(const Ctl* c, const double* s) {
   const double primal_res = sqrt(s[0]);
   const double dual_res = sqrt(s[1]);
   const double gap = s[2] - s[3];
-  const double primal_scale = 1.0 + c->a_norm_max_col * sqrt(s[4]) + sqrt(s[5]);
+  const double primal_scale = 1.0 + c->a_norm_max_col * sqrt(s[4]) + sqrt(s[5]) + c->q_norm;
   const double dual_scale = 1.0 + c->at_norm_max_row * sqrt(s[6]) + c->c_norm;
   const double gap_scale = 1.0 + fabs(s[2]) + fabs(s[3]);
   r.rp = c->m > 0 ? primal_res / primal_scale : 0.0;
@@ -413,7 +405,9 @@ __global__ void decide_a_kernel(Ctl* c) {
     c->t = t_new;
     return;
   }
-  c->detect_pending = (iter > 1000 && c->m > 0 && ((iter + 1) / kCheckFrequency) % 8 == 0) ? 1 : 0;
+  c->detect_pending =
+      (!c->no_detect && iter > 1000 && c->m > 0 && ((iter + 1) / kCheckFrequency) % 8 == 0) ? 1
+                                                                                              : 0;
   for (int q = 0; q < 8; ++q) c->det_flags[q] = 0;
 }
 
@@ -589,11 +583,10 @@ __global__ void __launch_bounds__(kBlock) det_farkas_cols_kernel(Ctl* c, OpView<
       return static_cast<double>(a) * static_cast<double>(ldg(y + i));
     }
   } g{it.Yerg};
-  TileSmem<double, 1>& sm = tile_smem<double, 1>();
-  run_tiles<T, double, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi, sm);
+  run_tiles<T, double, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
   const int nlong = Kt.ts.nlong;
   const double* la = red.long_terms;
-  grid_reduce<1>(epi.acc, red.partial, red.counter, sm.red, [c, nlong, la](const double (&t)[1]) {
+  grid_reduce<1>(epi.acc, red.partial, red.counter, smem_red(), [c, nlong, la](const double (&t)[1]) {
     double s = t[0];
     for (int l = 0; l < nlong; ++l) s += __ldcg(la + l);
     // w_scale: columns first, then the logicals' |yf| (pdlp.cpp:761-767).
@@ -777,11 +770,10 @@ __global__ void __launch_bounds__(kBlock) det_ray_rows_kernel(Ctl* c, OpView<T> 
     }
   } g{epi.vn, epi.vo, ray_x, ev.cs, v_max};
   epi.inv_vmax = 1.0 / v_max;
-  TileSmem<double, 2>& sm = tile_smem<double, 2>();
-  run_tiles<T, double, 2>(K.ts, K.ptr, K.idx, K.val, g, epi, sm);
+  run_tiles<T, double, 2>(K.ts, K.ptr, K.idx, K.val, g, epi);
   const int nlong = K.ts.nlong;
   const double* lt = red.long_terms;
-  grid_reduce<3, 4u>(epi.acc, red.partial, red.counter, sm.red,
+  grid_reduce<3, 4u>(epi.acc, red.partial, red.counter, smem_red(),
                      [c, nlong, lt](const double (&t)[3]) {
     double pf = t[0], cd = t[1], fail = t[2];
     for (int l = 0; l < nlong; ++l) {
@@ -817,9 +809,8 @@ __global__ void __launch_bounds__(kBlock) max_norm_kernel(OpView<double> A, RedV
                                                           double* out) {
   MaxNormEpi epi;
   epi.acc[0] = 0.0;
-  TileSmem<double, 1>& sm = tile_smem<double, 1>();
-  run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, SqProd{}, epi, sm);
-  grid_reduce<1, 1u>(epi.acc, red.partial, red.counter, sm.red,
+  run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, SqProd{}, epi);
+  grid_reduce<1, 1u>(epi.acc, red.partial, red.counter, smem_red(),
                      [out](const double (&t)[1]) { *out = t[0]; });
 }
 
@@ -855,8 +846,7 @@ __global__ void __launch_bounds__(kBlock) ruiz_norm_kernel(const Ctl* c, OpView<
                                                            double* norm) {
   if (c->ruiz_done) return;
   RuizEpi epi{own, norm};
-  run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, RuizProd{other}, epi,
-                               tile_smem<double, 1>());
+  run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, RuizProd{other}, epi);
 }
 
 // Scale update of one Ruiz pass (pdlp.cpp:154-178) over columns then rows.
@@ -949,11 +939,10 @@ __global__ void __launch_bounds__(kBlock) power_spmv_kernel(Ctl* c, OpView<doubl
   epi.out = y;
   epi.acc[0] = 0.0;
   epi.long_terms = red.long_terms;
-  TileSmem<double, 1>& sm = tile_smem<double, 1>();
-  run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, Gather1<double, double>{x}, epi, sm);
+  run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, Gather1<double, double>{x}, epi);
   const int nlong = A.ts.nlong;
   const double* lt = red.long_terms;
-  grid_reduce<1>(epi.acc, red.partial, red.counter, sm.red,
+  grid_reduce<1>(epi.acc, red.partial, red.counter, smem_red(),
                  [c, nlong, lt, which](const double (&t)[1]) {
     double s = t[0];
     for (int l = 0; l < nlong; ++l) s += __ldcg(lt + l * kMaxSums);
@@ -1031,8 +1020,77 @@ struct StoreEpi {
 __global__ void __launch_bounds__(kBlock) spmv_kernel(OpView<double> A, const double* x,
                                                       double* y) {
   StoreEpi epi{y};
-  run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, Gather1<double, double>{x}, epi,
-                               tile_smem<double, 1>());
+  run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, Gather1<double, double>{x}, epi);
+}
+
+// ------------------------------------------------------------------------------------------
+// Enhanced preconditioning (the engine's own, not the reference's): Ruiz equilibration in the
+// infinity norm (10 passes: every row and column divided by the square root of its largest
+// scaled magnitude) followed by Pock-Chambolle scaling with alpha = 1 (divide by the square
+// root of the scaled absolute row / column sums), both updating rows and columns from the same
+// matrix. Statistics by the tile kernel: products |a| * scale[other], max (Ruiz) or sum (PC).
+
+struct AbsProd {
+  const double* other;
+  __device__ __forceinline__ double operator()(int, double a, int j) const {
+    return fabs(a) * other[j];
+  }
+};
+
+struct StatEpi {
+  const double* own;
+  double* stat;
+  __device__ __forceinline__ void row(int r, const double (&s)[1]) { stat[r] = s[0] * own[r]; }
+  __device__ __forceinline__ void long_row(int, int r, const double (&s)[1]) { row(r, s); }
+};
+
+template <bool MAXRED>
+__global__ void __launch_bounds__(kBlock) abs_stat_kernel(OpView<double> A, const double* own,
+                                                          const double* other, double* stat) {
+  StatEpi epi{own, stat};
+  run_tiles<double, double, 1, AbsProd, StatEpi, MAXRED>(A.ts, A.ptr, A.idx, A.val,
+                                                         AbsProd{other}, epi);
+}
+
+// scale /= sqrt(stat) where stat > 0, columns then rows.
+__global__ void sqrt_rescale_kernel(int n, int m, double* cs, const double* cn, double* rs,
+                                    const double* rn) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n + m; k += gridDim.x * blockDim.x) {
+    if (k < n) {
+      if (cn[k] > 0.0) cs[k] = cs[k] / sqrt(cn[k]);
+    } else {
+      if (rn[k - n] > 0.0) rs[k - n] = rs[k - n] / sqrt(rn[k - n]);
+    }
+  }
+}
+
+// Initial primal weight |c| / |b| of the equilibrated problem (b: each row's largest finite
+// bound magnitude), 1 when either is ~0.
+__global__ void __launch_bounds__(kBlock) primal_weight_init_kernel(Ctl* c, int n, int m,
+                                                                    const double* cost_eq,
+                                                                    const double* lower_eq,
+                                                                    const double* upper_eq,
+                                                                    RedView red) {
+  __shared__ double scratch[kMaxSums * (kBlock / 32)];
+  double a[2] = {0.0, 0.0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n + m; k += gridDim.x * blockDim.x) {
+    if (k < n) {
+      a[0] += cost_eq[k] * cost_eq[k];
+    } else {
+      const double lo = lower_eq[k];
+      const double up = upper_eq[k];
+      const double b = fmax(isfinite(lo) ? fabs(lo) : 0.0, isfinite(up) ? fabs(up) : 0.0);
+      a[1] += b * b;
+    }
+  }
+  grid_reduce<2>(a, red.partial, red.counter, scratch, [c](const double (&t)[2]) {
+    const double cn = sqrt(t[0]);
+    const double bn = sqrt(t[1]);
+    const double w = (cn > 1e-10 && bn > 1e-10) ? cn / bn : 1.0;
+    c->omega = w;
+    c->tau = c->eta / w;
+    c->sigma = c->eta * w;
+  });
 }
 
 int vec_grid(long long len) {
@@ -1044,36 +1102,39 @@ int vec_grid(long long len) {
 
 }  // namespace
 
-size_t tile_smem_bytes(int nv, bool fp64) {
-  if (fp64) return nv == 1 ? sizeof(TileSmem<double, 1>) : sizeof(TileSmem<double, 2>);
-  return nv == 1 ? sizeof(TileSmem<float, 1>) : sizeof(TileSmem<double, 2>);
+size_t tile_smem_bytes(const TileSet& ts, int nv, size_t acc_bytes) {
+  return tile_smem_size(nv, acc_bytes, ts.cap_nnz, ts.cap_rows);
 }
 
 void configure_kernels() {
-  const int big = static_cast<int>(sizeof(TileSmem<double, 2>));
-  const int one = static_cast<int>(sizeof(TileSmem<double, 1>));
+  // Opt in to large dynamic shared memory; the launch sizes themselves follow each operator's
+  // tile capacity, so occupancy is set by the actual size.
+  const int big = 200 * 1024;
   cudaFuncSetAttribute(eval_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(eval_cols_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(eval_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(eval_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_ray_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_ray_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(dual_step_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
-  cudaFuncSetAttribute(primal_step_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
-  cudaFuncSetAttribute(det_farkas_cols_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
-  cudaFuncSetAttribute(det_farkas_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
-  cudaFuncSetAttribute(max_norm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
-  cudaFuncSetAttribute(ruiz_norm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
-  cudaFuncSetAttribute(power_spmv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
-  cudaFuncSetAttribute(spmv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, one);
+  cudaFuncSetAttribute(dual_step_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(primal_step_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(dual_step_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(primal_step_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(det_farkas_cols_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(det_farkas_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(max_norm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(ruiz_norm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(power_spmv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(spmv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(abs_stat_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(abs_stat_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
 }
 
 template <typename T>
 void launch_dual_step(const Ctl* ctl, const OpView<T>& K, const IterView<T>& it, int j, int grid,
                       cudaStream_t s) {
   if (K.ts.ntiles == 0) return;
-  const size_t sm = std::is_same<T, double>::value ? sizeof(TileSmem<double, 1>)
-                                                   : sizeof(TileSmem<float, 1>);
+  const size_t sm = tile_smem_bytes(K.ts, 1, sizeof(T));
   dual_step_kernel<T><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
 }
 
@@ -1081,8 +1142,7 @@ template <typename T>
 void launch_primal_step(const Ctl* ctl, const OpView<T>& Kt, const IterView<T>& it, int j,
                         int grid, cudaStream_t s) {
   if (Kt.ts.ntiles == 0) return;
-  const size_t sm = std::is_same<T, double>::value ? sizeof(TileSmem<double, 1>)
-                                                   : sizeof(TileSmem<float, 1>);
+  const size_t sm = tile_smem_bytes(Kt.ts, 1, sizeof(T));
   primal_step_kernel<T><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
 }
 
@@ -1090,9 +1150,10 @@ template <typename T>
 void launch_eval(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
                  const EvalView& ev, const RedView& red, int grid_k, int grid_t,
                  int fixed_parity, cudaStream_t s) {
-  const size_t sm = sizeof(TileSmem<double, 2>);
-  eval_rows_kernel<T><<<grid_k, kBlock, sm, s>>>(ctl, K, it, ev, red, fixed_parity);
-  eval_cols_kernel<T><<<grid_t, kBlock, sm, s>>>(ctl, Kt, it, ev, red, fixed_parity);
+  eval_rows_kernel<T><<<grid_k, kBlock, tile_smem_bytes(K.ts, 2, 8), s>>>(ctl, K, it, ev, red,
+                                                                       fixed_parity);
+  eval_cols_kernel<T><<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 2, 8), s>>>(ctl, Kt, it, ev, red,
+                                                                         fixed_parity);
 }
 
 void launch_decide_a(Ctl* ctl, cudaStream_t s) { decide_a_kernel<<<1, 32, 0, s>>>(ctl); }
@@ -1112,12 +1173,12 @@ void launch_detect(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const Iter
   const int gn = vec_grid(it.n) < 1024 ? vec_grid(it.n) : 1024;
   const int gnt = vec_grid(it.n + it.m) < 1024 ? vec_grid(it.n + it.m) : 1024;
   det_farkas_rows_kernel<T><<<gm, kBlock, 0, s>>>(ctl, it, ev, red);
-  det_farkas_cols_kernel<T><<<grid_t, kBlock, sizeof(TileSmem<double, 1>), s>>>(ctl, Kt, it, ev,
+  det_farkas_cols_kernel<T><<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 1, 8), s>>>(ctl, Kt, it, ev,
                                                                                 red, scratch_n);
   det_farkas_bounds_kernel<T><<<gnt, kBlock, 0, s>>>(ctl, it, ev, red, scratch_n);
   det_ray_max_kernel<T><<<gnt, kBlock, 0, s>>>(ctl, it, red);
   det_ray_cols_kernel<T><<<gn, kBlock, 0, s>>>(ctl, it, ev, red, scratch_n);
-  det_ray_rows_kernel<T><<<grid_k, kBlock, sizeof(TileSmem<double, 2>), s>>>(ctl, K, it, ev, red,
+  det_ray_rows_kernel<T><<<grid_k, kBlock, tile_smem_bytes(K.ts, 2, 8), s>>>(ctl, K, it, ev, red,
                                                                              scratch_n);
 }
 
@@ -1131,10 +1192,15 @@ void launch_extract(const Ctl* ctl, const IterView<T>& it, const EvalView& ev, d
 void launch_setup_norms(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt,
                         const double* cost, const RedView& red, int grid_k, int grid_t,
                         cudaStream_t s) {
-  const size_t sm = sizeof(TileSmem<double, 1>);
   if (K.rows > 0) {
-    if (Kt.ts.ntiles > 0) max_norm_kernel<<<grid_t, kBlock, sm, s>>>(Kt, red, &ctl->a_norm_max_col);
-    if (K.ts.ntiles > 0) max_norm_kernel<<<grid_k, kBlock, sm, s>>>(K, red, &ctl->at_norm_max_row);
+    if (Kt.ts.ntiles > 0) {
+      max_norm_kernel<<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 1, 8), s>>>(Kt, red,
+                                                                         &ctl->a_norm_max_col);
+    }
+    if (K.ts.ntiles > 0) {
+      max_norm_kernel<<<grid_k, kBlock, tile_smem_bytes(K.ts, 1, 8), s>>>(K, red,
+                                                                        &ctl->at_norm_max_row);
+    }
   }
   const int nt = K.rows + Kt.rows;
   sum_sq_kernel<<<vec_grid(nt) < 1024 ? vec_grid(nt) : 1024, kBlock, 0, s>>>(cost, nt, red,
@@ -1144,13 +1210,43 @@ void launch_setup_norms(Ctl* ctl, const OpView<double>& K, const OpView<double>&
 void launch_ruiz_pass(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt, double* rs,
                       double* cs, double* rn, double* cn, const RedView& red, int grid_k,
                       int grid_t, cudaStream_t s) {
-  const size_t sm = sizeof(TileSmem<double, 1>);
   // Column norms (rows of K'), then row norms (rows of K), both with the old scales.
-  ruiz_norm_kernel<<<grid_t, kBlock, sm, s>>>(ctl, Kt, cs, rs, cn);
-  ruiz_norm_kernel<<<grid_k, kBlock, sm, s>>>(ctl, K, rs, cs, rn);
+  ruiz_norm_kernel<<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 1, 8), s>>>(ctl, Kt, cs, rs, cn);
+  ruiz_norm_kernel<<<grid_k, kBlock, tile_smem_bytes(K.ts, 1, 8), s>>>(ctl, K, rs, cs, rn);
   const int nt = K.rows + Kt.rows;
   ruiz_update_kernel<<<vec_grid(nt) < 1024 ? vec_grid(nt) : 1024, kBlock, 0, s>>>(
       ctl, Kt.rows, K.rows, cs, cn, rs, rn, red);
+}
+
+void launch_enhanced_scaling(const OpView<double>& K, const OpView<double>& Kt, double* rs,
+                             double* cs, double* rn, double* cn, int grid_k, int grid_t,
+                             cudaStream_t s) {
+  const int n = Kt.rows;
+  const int m = K.rows;
+  const int g = vec_grid(n + m);
+  for (int pass = 0; pass < 10; ++pass) {
+    if (Kt.ts.ntiles > 0) {
+      abs_stat_kernel<true><<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 1, 8), s>>>(Kt, cs, rs, cn);
+    }
+    if (K.ts.ntiles > 0) {
+      abs_stat_kernel<true><<<grid_k, kBlock, tile_smem_bytes(K.ts, 1, 8), s>>>(K, rs, cs, rn);
+    }
+    sqrt_rescale_kernel<<<g, kBlock, 0, s>>>(n, m, cs, cn, rs, rn);
+  }
+  if (Kt.ts.ntiles > 0) {
+    abs_stat_kernel<false><<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 1, 8), s>>>(Kt, cs, rs, cn);
+  }
+  if (K.ts.ntiles > 0) {
+    abs_stat_kernel<false><<<grid_k, kBlock, tile_smem_bytes(K.ts, 1, 8), s>>>(K, rs, cs, rn);
+  }
+  sqrt_rescale_kernel<<<g, kBlock, 0, s>>>(n, m, cs, cn, rs, rn);
+}
+
+void launch_primal_weight_init(Ctl* ctl, int n, int m, const double* cost_eq,
+                               const double* lower_eq, const double* upper_eq,
+                               const RedView& red, cudaStream_t s) {
+  const int g = vec_grid(n + m) < 1024 ? vec_grid(n + m) : 1024;
+  primal_weight_init_kernel<<<g, kBlock, 0, s>>>(ctl, n, m, cost_eq, lower_eq, upper_eq, red);
 }
 
 void launch_apply_scaling(const OpView<double>& K, const OpView<double>& Kt, const double* rs,
@@ -1172,13 +1268,16 @@ void launch_power_iteration(Ctl* ctl, const OpView<double>& K, const OpView<doub
                             int grid_t, cudaStream_t s) {
   const int m = K.rows;
   if (m > 0) {
-    const size_t sm = sizeof(TileSmem<double, 1>);
     const int gm = vec_grid(m) < 1024 ? vec_grid(m) : 1024;
     sum_sq_kernel<<<gm, kBlock, 0, s>>>(u, m, red, &ctl->power_unorm);
     scale_by_norm_kernel<<<gm, kBlock, 0, s>>>(ctl, u, m, 1);
     for (int it = 0; it < iters; ++it) {
-      if (Kt.ts.ntiles > 0) power_spmv_kernel<<<grid_t, kBlock, sm, s>>>(ctl, Kt, u, v, red, 0);
-      if (K.ts.ntiles > 0) power_spmv_kernel<<<grid_k, kBlock, sm, s>>>(ctl, K, v, u, red, 1);
+      if (Kt.ts.ntiles > 0) {
+        power_spmv_kernel<<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 1, 8), s>>>(ctl, Kt, u, v, red, 0);
+      }
+      if (K.ts.ntiles > 0) {
+        power_spmv_kernel<<<grid_k, kBlock, tile_smem_bytes(K.ts, 1, 8), s>>>(ctl, K, v, u, red, 1);
+      }
       scale_by_norm_kernel<<<gm, kBlock, 0, s>>>(ctl, u, m, 0);
     }
   }
@@ -1202,7 +1301,7 @@ void launch_convert(const Src* src, Dst* dst, long long count, cudaStream_t s) {
 
 void launch_spmv(const OpView<double>& A, const double* x, double* y, int grid, cudaStream_t s) {
   if (A.ts.ntiles == 0) return;
-  spmv_kernel<<<grid, kBlock, sizeof(TileSmem<double, 1>), s>>>(A, x, y);
+  spmv_kernel<<<grid, kBlock, tile_smem_bytes(A.ts, 1, 8), s>>>(A, x, y);
 }
 
 // Explicit instantiations.

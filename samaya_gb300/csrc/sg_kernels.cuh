@@ -81,6 +81,14 @@ void launch_setup_norms(Ctl* ctl, const OpView<double>& K, const OpView<double>&
 void launch_ruiz_pass(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt, double* rs,
                       double* cs, double* rn, double* cn, const RedView& red, int grid_k,
                       int grid_t, cudaStream_t s);
+// Enhanced preconditioning: 10 passes of infinity-norm Ruiz, then Pock-Chambolle (alpha = 1).
+void launch_enhanced_scaling(const OpView<double>& K, const OpView<double>& Kt, double* rs,
+                             double* cs, double* rn, double* cn, int grid_k, int grid_t,
+                             cudaStream_t s);
+// Initial primal weight |c_eq| / |b_eq| (sets omega, tau, sigma; needs eta).
+void launch_primal_weight_init(Ctl* ctl, int n, int m, const double* cost_eq,
+                               const double* lower_eq, const double* upper_eq,
+                               const RedView& red, cudaStream_t s);
 void launch_apply_scaling(const OpView<double>& K, const OpView<double>& Kt, const double* rs,
                           const double* cs, long long nnz, cudaStream_t s);
 void launch_scale_vectors(int n, int m, const double* cs, const double* rs, const double* cost,
@@ -100,7 +108,7 @@ void launch_convert(const Src* src, Dst* dst, long long count, cudaStream_t s);
 void launch_spmv(const OpView<double>& A, const double* x, double* y, int grid, cudaStream_t s);
 
 // Sizes of dynamic shared memory of the tile kernels.
-size_t tile_smem_bytes(int nv, bool fp64);
+size_t tile_smem_bytes(const TileSet& ts, int nv, size_t acc_bytes);
 void configure_kernels();
 
 }  // namespace sg

@@ -1,0 +1,285 @@
+// Mixed precision with iterative refinement (the engine's own addition; the reference is FP64
+// only). The FP64 point (v*, y*) of the equilibrated problem is refined by FP32 PDHG solves of
+// scaled correction problems (Gleixner, Steffy & Wolter's LP iterative refinement applied to
+// PDLP's computational form):
+//   correction:  min (dd d)'w  s.t.  [A_eq -I] w = dp b,  dp (l - v*) <= w <= dp (u - v*),
+//   with b = -[A_eq -I] v* (primal residual) and d = c + [A_eq -I]' y* (reduced costs), both in
+//   FP64 from the FP64 matrix; then v* += w / dp and y* += z / dd for the correction's duals z.
+// dp and dd are the inverse largest primal and dual violations (growth capped per round), so
+// every correction problem is well scaled for FP32 arithmetic.
+#include <math.h>
+
+#include "sg_kernels.cuh"
+#include "sg_refine.cuh"
+#include "sg_tile.cuh"
+
+namespace sg {
+
+namespace {
+
+__device__ __forceinline__ double bound_lambda(double g, double lo, double up) {
+  const bool hl = lo > -INFINITY;
+  const bool hu = up < INFINITY;
+  return hl && hu ? g : hl ? fmax(g, 0.0) : hu ? fmin(g, 0.0) : 0.0;
+}
+
+struct Gather64 {
+  const double* x;
+  __device__ __forceinline__ double operator()(int, double a, int j) const { return a * x[j]; }
+};
+
+// Rows: b_i = -(A_eq x* - r*)_i, the logicals' reduced cost d_{n+i} = c_{n+i} - y*_i and its
+// dual violation; max |b| and max violation.
+struct ResRowEpi {
+  const double* v;  // v* (n + m)
+  const double* y;
+  const double* cost;
+  const double* lower;
+  const double* upper;
+  double* bh;
+  double* d;
+  int n;
+  double acc[2];
+  double* long_terms;
+  __device__ __forceinline__ void terms(int i, double s, double (&a)[2]) {
+    const double b = -(s - v[n + i]);
+    bh[i] = b;
+    const double g = cost[n + i] - y[i];
+    d[n + i] = g;
+    const double viol = fabs(g - bound_lambda(g, lower[n + i], upper[n + i]));
+    a[0] = fmax(a[0], fabs(b));
+    a[1] = fmax(a[1], viol);
+  }
+  __device__ __forceinline__ void row(int i, const double (&s)[1]) { terms(i, s[0], acc); }
+  __device__ __forceinline__ void long_row(int lrow, int i, const double (&s)[1]) {
+    double a[2] = {0.0, 0.0};
+    terms(i, s[0], a);
+    long_terms[lrow * kMaxSums + 0] = a[0];
+    long_terms[lrow * kMaxSums + 1] = a[1];
+  }
+};
+
+// Columns: d_j = c_j + (A_eq' y*)_j and its dual violation.
+struct ResColEpi {
+  const double* cost;
+  const double* lower;
+  const double* upper;
+  double* d;
+  double acc[2];
+  double* long_terms;
+  __device__ __forceinline__ void terms(int j, double s, double (&a)[2]) {
+    const double g = cost[j] + s;
+    d[j] = g;
+    a[1] = fmax(a[1], fabs(g - bound_lambda(g, lower[j], upper[j])));
+  }
+  __device__ __forceinline__ void row(int j, const double (&s)[1]) { terms(j, s[0], acc); }
+  __device__ __forceinline__ void long_row(int lrow, int j, const double (&s)[1]) {
+    double a[2] = {0.0, 0.0};
+    terms(j, s[0], a);
+    long_terms[lrow * kMaxSums + 0] = a[0];
+    long_terms[lrow * kMaxSums + 1] = a[1];
+  }
+};
+
+__global__ void __launch_bounds__(kBlock) ir_rows_kernel(Ctl* c, OpView<double> K, IrView v) {
+  ResRowEpi epi;
+  epi.v = v.v;
+  epi.y = v.y;
+  epi.cost = v.cost_eq;
+  epi.lower = v.lower_eq;
+  epi.upper = v.upper_eq;
+  epi.bh = v.bh;
+  epi.d = v.d;
+  epi.n = v.n;
+  epi.acc[0] = epi.acc[1] = 0.0;
+  epi.long_terms = v.red.long_terms;
+  run_tiles<double, double, 1>(K.ts, K.ptr, K.idx, K.val, Gather64{v.v}, epi);
+  const int nlong = K.ts.nlong;
+  const double* lt = v.red.long_terms;
+  grid_reduce<2, 3u>(epi.acc, v.red.partial, v.red.counter, smem_red(),
+                     [c, nlong, lt](const double (&t)[2]) {
+    double p = t[0], d = t[1];
+    for (int l = 0; l < nlong; ++l) {
+      p = fmax(p, __ldcg(lt + l * kMaxSums));
+      d = fmax(d, __ldcg(lt + l * kMaxSums + 1));
+    }
+    c->ir_pmax = p;
+    c->ir_dmax = d;
+  });
+}
+
+__global__ void __launch_bounds__(kBlock) ir_cols_kernel(Ctl* c, OpView<double> Kt, IrView v) {
+  ResColEpi epi;
+  epi.cost = v.cost_eq;
+  epi.lower = v.lower_eq;
+  epi.upper = v.upper_eq;
+  epi.d = v.d;
+  epi.acc[0] = epi.acc[1] = 0.0;
+  epi.long_terms = v.red.long_terms;
+  run_tiles<double, double, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, Gather64{v.y}, epi);
+  const int nlong = Kt.ts.nlong;
+  const double* lt = v.red.long_terms;
+  grid_reduce<2, 3u>(epi.acc, v.red.partial, v.red.counter, smem_red(),
+                     [c, nlong, lt](const double (&t)[2]) {
+    double d = t[1];
+    for (int l = 0; l < nlong; ++l) d = fmax(d, __ldcg(lt + l * kMaxSums + 1));
+    c->ir_dmax = fmax(c->ir_dmax, d);
+  });
+}
+
+// Scale factors of the correction problem and its starting primal weight.
+__global__ void ir_scales_kernel(Ctl* c, int round, double growth) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (round == 0) {
+    c->ir_dp_prev = 1.0;
+    c->ir_dd_prev = 1.0;
+    c->ir_dp = 1.0;
+    c->ir_dd = 1.0;
+    c->omega = c->ir_omega0;
+  } else {
+    const double pm = fmax(c->ir_pmax, 1e-300);
+    const double dm = fmax(c->ir_dmax, 1e-300);
+    const double dp_prev = c->ir_dp;
+    const double dd_prev = c->ir_dd;
+    const double dp = fmin(1.0 / pm, dp_prev * growth);
+    const double dd = fmin(1.0 / dm, dd_prev * growth);
+    c->ir_dp_prev = dp_prev;
+    c->ir_dd_prev = dd_prev;
+    c->ir_dp = dp;
+    c->ir_dd = dd;
+    // The correction scales primal by dp and dual by dd: carry the weight over accordingly.
+    c->omega = c->omega * (dd / dd_prev) / (dp / dp_prev);
+  }
+  c->tau = c->eta / c->omega;
+  c->sigma = c->eta * c->omega;
+}
+
+// Builds the correction problem (FP64 evaluation copy and FP32 iteration copy) and zeroes the
+// FP32 iterates.
+__global__ void ir_build_kernel(const Ctl* __restrict__ c, IrView v, int round) {
+  const double dp = c->ir_dp;
+  const double dd = c->ir_dd;
+  const int n = v.n;
+  const int nt = n + v.m;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
+    double cc, lo, up;
+    if (round == 0) {
+      cc = v.cost_eq[k];
+      lo = v.lower_eq[k];
+      up = v.upper_eq[k];
+    } else {
+      cc = dd * v.d[k];
+      lo = dp * (v.lower_eq[k] - v.v[k]);
+      up = dp * (v.upper_eq[k] - v.v[k]);
+    }
+    v.cost_in[k] = cc;
+    v.lower_in[k] = lo;
+    v.upper_in[k] = up;
+    v.cost32[k] = static_cast<float>(cc);
+    v.lower32[k] = static_cast<float>(lo);
+    v.upper32[k] = static_cast<float>(up);
+    if (k >= n) {
+      const int i = k - n;
+      const double q = round == 0 ? 0.0 : dp * v.bh[i];
+      v.rhs_in[i] = q;
+      v.rhs32[i] = static_cast<float>(q);
+    }
+  }
+}
+
+// v* += w / dp, y* += z / dd from the FP32 answer (current or average iterate), then v* back
+// inside its bounds; round 0 takes the FP32 answer as the point.
+__global__ void ir_update_kernel(const Ctl* __restrict__ c32, IterView<float> it, IrView v,
+                                 int round) {
+  const int cur = static_cast<int>(c32->t & 1);
+  const bool avg = c32->result_average != 0;
+  const float* w = avg ? it.Verg : it.V[cur];
+  const float* z = avg ? it.Yerg : it.Y[cur];
+  const double dp = c32->ir_dp;
+  const double dd = c32->ir_dd;
+  const int nt = v.n + v.m;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
+    double nv = round == 0 ? static_cast<double>(w[k]) : v.v[k] + static_cast<double>(w[k]) / dp;
+    nv = fmin(fmax(nv, v.lower_eq[k]), v.upper_eq[k]);
+    v.v[k] = nv;
+    if (k < v.m) {
+      v.y[k] = round == 0 ? static_cast<double>(z[k]) : v.y[k] + static_cast<double>(z[k]) / dd;
+    }
+  }
+}
+
+// Resets the inner solve's control block for a new correction problem.
+__global__ void ir_reset_kernel(Ctl* c, double tol, long long max_iter) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  c->t = 0;
+  c->k = 0;
+  c->max_iter = max_iter;
+  c->tol = tol;
+  c->kkt_at_restart = INFINITY;
+  c->kkt_previous = INFINITY;
+  c->status = kRunning;
+  c->done = 0;
+  c->result_average = 0;
+  c->restart_pending = 0;
+  c->detect_pending = 0;
+  c->iterations = 0;
+  c->restarts = 0;
+  c->evaluations = 0;
+  c->no_detect = 1;
+}
+
+__global__ void __launch_bounds__(kBlock) norm_into_kernel(const double* x, int len, RedView red,
+                                                           double* out) {
+  __shared__ double scratch[kMaxSums * (kBlock / 32)];
+  double a[1] = {0.0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < len; k += gridDim.x * blockDim.x) {
+    a[0] += x[k] * x[k];
+  }
+  grid_reduce<1>(a, red.partial, red.counter, scratch,
+                 [out](const double (&t)[1]) { *out = sqrt(t[0]); });
+}
+
+int grid_for(long long len, int cap) {
+  long long g = (len + kBlock - 1) / kBlock;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return static_cast<int>(g);
+}
+
+}  // namespace
+
+void configure_refine_kernels() {
+  const int big = 200 * 1024;
+  cudaFuncSetAttribute(ir_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(ir_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+}
+
+void launch_ir_residual(Ctl* c32, const OpView<double>& K, const OpView<double>& Kt,
+                        const IrView& v, int grid_k, int grid_t, cudaStream_t s) {
+  ir_rows_kernel<<<grid_k, kBlock, tile_smem_bytes(K.ts, 1, 8), s>>>(c32, K, v);
+  ir_cols_kernel<<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 1, 8), s>>>(c32, Kt, v);
+}
+
+void launch_ir_scales(Ctl* c32, int round, double growth, cudaStream_t s) {
+  ir_scales_kernel<<<1, 32, 0, s>>>(c32, round, growth);
+}
+
+void launch_ir_build(const Ctl* c32, const IrView& v, int round, cudaStream_t s) {
+  ir_build_kernel<<<grid_for(v.n + v.m, 4096), kBlock, 0, s>>>(c32, v, round);
+}
+
+void launch_ir_update(const Ctl* c32, const IterView<float>& it, const IrView& v, int round,
+                      cudaStream_t s) {
+  ir_update_kernel<<<grid_for(v.n + v.m, 4096), kBlock, 0, s>>>(c32, it, v, round);
+}
+
+void launch_ir_reset(Ctl* c32, double tol, long long max_iter, cudaStream_t s) {
+  ir_reset_kernel<<<1, 32, 0, s>>>(c32, tol, max_iter);
+}
+
+void launch_norm_into(const double* x, long long len, const RedView& red, double* out,
+                      cudaStream_t s) {
+  norm_into_kernel<<<grid_for(len, 1024), kBlock, 0, s>>>(x, static_cast<int>(len), red, out);
+}
+
+}  // namespace sg

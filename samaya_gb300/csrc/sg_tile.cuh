@@ -5,35 +5,75 @@
 //            products prod(v, val, col) in shared memory;
 //   phase B  reduces each row's products inside the tile: `team` lanes per row (chosen from the
 //            tile's mean row length), lanes step by `team`, then a fixed shuffle tree;
-//   phase C  calls epi(row, sums) with one thread per row, so the epilogue's vector accesses
+//   phase C  calls epi.row(row, sums) with one thread per row, so the epilogue's vector accesses
 //            (iterates, bounds, averages) are coalesced across the CTA.
-// A row longer than kTileNnz is cut into consecutive segment tiles; each segment's block sum
-// goes to TileSet::seg_part and the last segment to arrive (counter) adds the segments in tile
-// order and runs the epilogue (epi.long_row). Every sum is taken in a fixed order, so results do
-// not depend on scheduling and a re-run is bit-identical.
+// A row longer than the tile capacity is cut into consecutive segment tiles; each segment's
+// block sum goes to TileSet::seg_part and the last segment to arrive (counter) adds the segments
+// in tile order (the whole CTA, fixed tree) and runs epi.long_row. Every sum is taken in a fixed
+// order, so results do not depend on scheduling and a re-run is bit-identical.
+//
+// Shared memory (dynamic): red[kMaxSums * 8] doubles | prod[NV][cap_nnz] ACC | rows[NV][cap_rows].
 #pragma once
 
 #include "sg_common.cuh"
 
 namespace sg {
 
+constexpr int kRedDoubles = kMaxSums * (kBlock / 32);
+
+__host__ __device__ constexpr size_t tile_smem_size(int nv, size_t acc_bytes, int cap_nnz,
+                                                    int cap_rows) {
+  return sizeof(double) * kRedDoubles + acc_bytes * nv * (static_cast<size_t>(cap_nnz) + cap_rows);
+}
+
 template <typename ACC, int NV>
 struct TileSmem {
-  ACC prod[NV][kTileNnz];
-  ACC rows[NV][kTileRows];
-  double red[kMaxSums * (kBlock / 32)];
+  double* red;
+  ACC* prod;  // [NV][cap_nnz]
+  ACC* rows;  // [NV][cap_rows]
+  int cap_nnz, cap_rows;
+  __device__ __forceinline__ ACC& p(int v, int q) { return prod[v * cap_nnz + q]; }
+  __device__ __forceinline__ ACC& r(int v, int q) { return rows[v * cap_rows + q]; }
 };
+
+template <typename ACC, int NV>
+__device__ __forceinline__ TileSmem<ACC, NV> tile_smem(const TileSet& ts) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TileSmem<ACC, NV> s;
+  s.red = reinterpret_cast<double*>(smem_raw);
+  s.prod = reinterpret_cast<ACC*>(smem_raw + sizeof(double) * kRedDoubles);
+  s.rows = s.prod + NV * ts.cap_nnz;
+  s.cap_nnz = ts.cap_nnz;
+  s.cap_rows = ts.cap_rows;
+  return s;
+}
 
 // Iterates over tiles. Prod: ACC operator()(int v, T val, int col) const.
 // Epi: void row(int r, const ACC (&s)[NV]) for rows of kind-0 tiles (called by one thread),
 //      void long_row(int lrow, int r, const ACC (&s)[NV]) for a split row (thread 0 of the CTA
 //      that completes it).
-template <typename T, typename ACC, int NV, typename Prod, typename Epi>
+__device__ __forceinline__ double* smem_red() {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  return reinterpret_cast<double*>(smem_raw);
+}
+
+template <bool MAXRED, typename ACC>
+__device__ __forceinline__ ACC combine(ACC a, ACC b) {
+  if constexpr (MAXRED) {
+    return a > b ? a : b;
+  } else {
+    return a + b;
+  }
+}
+
+// MAXRED: each row's products are combined by max instead of + (norm statistics).
+template <typename T, typename ACC, int NV, typename Prod, typename Epi, bool MAXRED = false>
 __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restrict__ ptr,
                                           const int* __restrict__ idx,
-                                          const T* __restrict__ val, const Prod& prod, Epi& epi,
-                                          TileSmem<ACC, NV>& sm) {
+                                          const T* __restrict__ val, const Prod& prod, Epi& epi) {
+  TileSmem<ACC, NV> sm = tile_smem<ACC, NV>(ts);
   const int tid = threadIdx.x;
+  __shared__ bool last_seg;
   for (int ti = blockIdx.x; ti < ts.ntiles; ti += gridDim.x) {
     const Tile tile = ts.tiles[ti];
     const int k0 = tile.k0;
@@ -53,17 +93,17 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
         const int j3 = ldg(idx + k0 + q + 3 * kBlock);
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-          sm.prod[v][q] = prod(v, a0, j0);
-          sm.prod[v][q + kBlock] = prod(v, a1, j1);
-          sm.prod[v][q + 2 * kBlock] = prod(v, a2, j2);
-          sm.prod[v][q + 3 * kBlock] = prod(v, a3, j3);
+          sm.p(v, q) = prod(v, a0, j0);
+          sm.p(v, q + kBlock) = prod(v, a1, j1);
+          sm.p(v, q + 2 * kBlock) = prod(v, a2, j2);
+          sm.p(v, q + 3 * kBlock) = prod(v, a3, j3);
         }
       }
       for (; q < len; q += kBlock) {
         const T a = ldg(val + k0 + q);
         const int j = ldg(idx + k0 + q);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) sm.prod[v][q] = prod(v, a, j);
+        for (int v = 0; v < NV; ++v) sm.p(v, q) = prod(v, a, j);
       }
     }
     __syncthreads();
@@ -85,16 +125,18 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
           const int e = ldg(ptr + tile.r0 + lr + 1) - k0;
           for (int q = b + lane; q < e; q += team) {
 #pragma unroll
-            for (int v = 0; v < NV; ++v) s[v] += sm.prod[v][q];
+            for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], sm.p(v, q));
           }
         }
         for (int o = team / 2; o > 0; o >>= 1) {
 #pragma unroll
-          for (int v = 0; v < NV; ++v) s[v] += __shfl_down_sync(0xffffffffu, s[v], o, team);
+          for (int v = 0; v < NV; ++v) {
+            s[v] = combine<MAXRED>(s[v], __shfl_down_sync(0xffffffffu, s[v], o, team));
+          }
         }
         if (lane == 0 && lr < nrows) {
 #pragma unroll
-          for (int v = 0; v < NV; ++v) sm.rows[v][lr] = s[v];
+          for (int v = 0; v < NV; ++v) sm.r(v, lr) = s[v];
         }
       }
       __syncthreads();
@@ -102,7 +144,7 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
       for (int lr = tid; lr < nrows; lr += kBlock) {
         ACC s[NV];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) s[v] = sm.rows[v][lr];
+        for (int v = 0; v < NV; ++v) s[v] = sm.r(v, lr);
         epi.row(tile.r0 + lr, s);
       }
     } else {
@@ -111,12 +153,11 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         ACC s = ACC(0);
-        for (int q = tid; q < len; q += kBlock) s += sm.prod[v][q];
+        for (int q = tid; q < len; q += kBlock) s = combine<MAXRED>(s, sm.p(v, q));
         part[v] = static_cast<double>(s);
       }
       double tot[NV];
-      block_sum<NV>(part, sm.red, tot);
-      __shared__ bool last_seg;
+      block_reduce<NV, MAXRED ? 0xFFu : 0u>(part, sm.red, tot);
       if (tid == 0) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) ts.seg_part[ti * kMaxVec + v] = tot[v];
@@ -125,18 +166,29 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
         last_seg = (prev == static_cast<unsigned>(tile.nseg - 1));
       }
       __syncthreads();
-      if (last_seg && tid == 0) {
+      if (last_seg) {
+        // The whole CTA adds the row's segments: thread t takes segments t, t + 256, ... in
+        // order, then the fixed block tree.
         __threadfence();
         const int first = ti - tile.seg;
-        ACC s[NV];
+        double acc[NV];
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-          double acc = 0.0;
-          for (int g = 0; g < tile.nseg; ++g) acc += __ldcg(ts.seg_part + (first + g) * kMaxVec + v);
-          s[v] = static_cast<ACC>(acc);
+          double a = 0.0;
+          for (int g = tid; g < tile.nseg; g += kBlock) {
+            a = combine<MAXRED>(a, __ldcg(ts.seg_part + (first + g) * kMaxVec + v));
+          }
+          acc[v] = a;
         }
-        ts.lcount[tile.lrow] = 0u;
-        epi.long_row(tile.lrow, tile.r0, s);
+        double sum[NV];
+        block_reduce<NV, MAXRED ? 0xFFu : 0u>(acc, sm.red, sum);
+        if (tid == 0) {
+          ACC s[NV];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) s[v] = static_cast<ACC>(sum[v]);
+          ts.lcount[tile.lrow] = 0u;
+          epi.long_row(tile.lrow, tile.r0, s);
+        }
       }
     }
     __syncthreads();

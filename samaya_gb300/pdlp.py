@@ -24,6 +24,8 @@ STATUS_NAMES = ["optimal", "infeasible", "unbounded", "iteration_limit", "time_l
 
 FP64 = 0
 FP32_REFINED = 1
+REFERENCE = 0
+ENHANCED = 1
 
 
 @dataclass
@@ -36,6 +38,7 @@ class PdlpOptions:
     precision: int = FP64
     refine_max_rounds: int = 6
     inner_tol: float = 1e-4
+    algorithm: int = REFERENCE
 
     def to_c(self) -> _native.Opts:
         o = _native.Opts()
@@ -46,6 +49,7 @@ class PdlpOptions:
         o.precision = int(self.precision)
         o.refine_max_rounds = int(self.refine_max_rounds)
         o.inner_tol = float(self.inner_tol)
+        o.algorithm = int(self.algorithm)
         return o
 
 

@@ -59,18 +59,26 @@ def test_random_feasible_objectives_and_iterations(engine):
 
 def test_against_reference_cpu_pdlp_at_1e4(engine):
     """pdlp_vs_simplex (tests/test_pdlp.cpp:234-400) LPs at 1e-4: same status as the reference's
-    CPU PDLP; optimal objectives within 1e-4 relative of the reference dual simplex."""
+    CPU PDLP and optimal objectives within 1e-4 relative of its objective. (At 1e-4 the
+    reference's own PDLP stops on two of these LPs with objectives far from the simplex optimum,
+    so agreement with the simplex is required only where the reference's PDLP has it.)"""
     bad = []
     for case in load_group("vs_simplex10"):
         r = solve(engine, case)
         if r.status != case.ref_status:
             bad.append(("status", case.k, r.status, case.ref_status))
             continue
-        if r.status == engine.OPTIMAL and case.simplex is not None and int(case.simplex[0]) == 0:
-            obj = model_objective(case, r.x)
-            ref_obj = float(case.simplex[1])
-            if abs(obj - ref_obj) > 1e-4 * (1 + abs(ref_obj)) * 10:
-                bad.append(("objective", case.k, obj, ref_obj))
+        if r.status != engine.OPTIMAL:
+            continue
+        obj = model_objective(case, r.x)
+        ref_obj = model_objective(case, case.ref_x)
+        if abs(obj - ref_obj) > 1e-4 * (1 + abs(ref_obj)):
+            bad.append(("vs reference pdlp", case.k, obj, ref_obj))
+        if case.simplex is not None and int(case.simplex[0]) == 0:
+            sx = float(case.simplex[1])
+            ref_close = abs(ref_obj - sx) <= 1e-3 * (1 + abs(sx))
+            if ref_close and abs(obj - sx) > 1e-3 * (1 + abs(sx)):
+                bad.append(("vs simplex", case.k, obj, sx))
     assert not bad, bad
 
 
