@@ -1,0 +1,328 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 PDLP engine: time to 1e-8 relative KKT on the transportation LP
+(1000 supplies x 2000 demands: 3000 equality rows, 2,000,000 columns, 4,000,000 nonzeros), with
+FP32 storage + FP64 iterative refinement (the headline) next to plain FP64 on the same GPU.
+
+One step = one full PDLP solve of the LP, inputs resident in HBM (the problem uploaded once);
+``e2e`` = the same solve through the public C ABI from pinned host buffers (upload, solve,
+download of x and y). ``roofline`` reports the dominant kernel (the primal step: A'y SpMV fused
+with the projected primal update and the running average) against the measured HBM copy
+bandwidth; ``cpu_baseline`` times the reference's CPU PDLP (the oracle port, 1 core) on a
+bounded run of the same LP.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With N > 1 (torchrun) every rank solves its own replica (replicas only; no collective on the
+data path); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PDLP time-to-1e-8 KKT (mixed vs FP64 GPU)"
+TOL = 1e-8
+CPU_CAP_S = 20.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="transport", choices=["transport", "powerlaw", "random"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    return ap.parse_args()
+
+
+def workload(name, seed=0):
+    from samaya_gb300 import generators as g
+    if name == "transport":
+        return g.transportation_lp(1000, 2000, seed=seed), {
+            "workload": "transportation LP 1000 supplies x 2000 demands", "rows": 3000,
+            "columns": 2_000_000, "nnz": 4_000_000, "seed": seed}
+    if name == "powerlaw":
+        return g.power_law_lp(seed=seed), {
+            "workload": "power-law LP 1e6 x 2e6, Zipf(1.5) rows", "rows": 1_000_000,
+            "columns": 2_000_000, "nnz": 12_000_000, "seed": seed}
+    return g.random_sparse_lp(2000, 5000, seed=seed), {
+        "workload": "random sparse LP 2000 x 5000", "rows": 2000, "columns": 5000,
+        "nnz": 30000, "seed": seed}
+
+
+def dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples of the SM clock and throttle reasons during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([s.strip() for s in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            if self.thread is not None:
+                self.thread.join(timeout=2)
+
+    def summary(self):
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                mhz.append(float(s[0]))
+                mx = float(s[1])
+                for k, name in enumerate(names):
+                    if s[3 + k].lower().startswith("active"):
+                        reasons.add(name)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_summary():
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def primal_step_bytes(lp, value_bytes):
+    """Compulsory bytes of one primal-step launch (rows of A' = the n columns): the nonzeros
+    (value + int32 index), the n + 1 row starts, the m duals gathered once, and the column
+    epilogue: c, l, u, x, x_avg read; x_new, x_bar, x_avg written (8 n-vectors)."""
+    n, m, nnz = lp.n, lp.m, lp.nnz
+    return nnz * (value_bytes + 4) + (n + 1) * 4 + m * value_bytes + 8 * n * value_bytes
+
+
+def dual_step_bytes(lp, value_bytes):
+    """Rows of A: nonzeros, m + 1 starts, x_bar gathered once (n), and the row epilogue:
+    y, r, r_bar, c_r, l_r, u_r, y_avg, r_avg read; y_new, r_new, r_bar, y_avg, r_avg written
+    (13 m-vectors; +1 with a right-hand side)."""
+    n, m, nnz = lp.n, lp.m, lp.nnz
+    return nnz * (value_bytes + 4) + (m + 1) * 4 + n * value_bytes + 14 * m * value_bytes
+
+
+def cpu_reference_run(lp, cap_s=CPU_CAP_S):
+    """The reference's CPU PDLP (oracle port of src/lp/pdlp.cpp, one core) on the LP to 1e-8
+    with a time cap: (seconds, converged, iterations, worst relative residual)."""
+    from oracle import oracle as o
+    t0 = time.perf_counter()
+    r = o.pdlp_solve(*lp.arrays(), tol=TOL, max_iter=-1, time_limit=cap_s)
+    dt = time.perf_counter() - t0
+    worst = max(r.primal_residual, r.dual_residual, abs(r.gap))
+    return dt, r.status == o.OPTIMAL, r.iterations, worst
+
+
+def run_reference(args):
+    world, rank, _ = dist()
+    if rank != 0:
+        return 0
+    model, cfg = workload(args.workload)
+    from samaya_gb300.problem import make_problem
+    lp, _ = make_problem(model)
+    times, info = [], None
+    for i in range(args.warmup + args.steps):
+        dt, conv, iters, worst = cpu_reference_run(lp)
+        if i >= args.warmup:
+            times.append(dt)
+            info = (conv, iters, worst)
+    value = sum(times) / len(times)
+    sample = (f"reference CPU PDLP (oracle port of samaya src/lp/pdlp.cpp, bit-identical to it) "
+              f"to 1e-8 capped at {CPU_CAP_S:.0f} s per step on the same LP; converged="
+              f"{info[0]}, {info[1]} iterations, worst relative residual {info[2]:.2e}")
+    line = {"metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": dict(cfg, tol=TOL), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "s", "cores": 1, "kind": "port",
+                             "sample": sample, "converged": info[0]},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    world, rank, local = dist()
+    import numpy as np
+    import samaya_gb300 as sg
+    from samaya_gb300.problem import make_problem
+    from samaya_gb300 import _native
+    _native.load()
+    torch = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", "0"))
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    model, cfg = workload(args.workload, seed=rank)
+    lp, scaling = make_problem(model)
+    mixed = args.precision == "mixed"
+    opts = sg.PdlpOptions(tol=TOL, algorithm=sg.ENHANCED,
+                          precision=sg.FP32_REFINED if mixed else sg.FP64)
+    opts64 = sg.PdlpOptions(tol=TOL, algorithm=sg.ENHANCED, precision=sg.FP64)
+    solver = sg.PdlpSolver(lp, opts)
+    for _ in range(args.warmup):
+        warm = solver.solve(download=False)
+    barrier()
+    results = []
+    with Clocks(local) as clk:
+        barrier()
+        for _ in range(args.steps):
+            results.append(solver.solve(download=False))
+        barrier()
+    dev_s = [r.device_ms / 1e3 for r in results]
+    t_step = sum(dev_s) / len(dev_s)
+    if world > 1:
+        t = torch.tensor([t_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(t.item())
+    last = results[-1]
+    # Plain FP64 GPU PDLP (same algorithm) on the same LP, for the mixed-vs-FP64 comparison.
+    fp64 = None
+    if mixed:
+        with sg.PdlpSolver(lp, opts64) as s64:
+            s64.solve(download=False)
+            r64 = [s64.solve(download=False) for _ in range(max(1, min(args.steps, 3)))]
+        fp64 = {"seconds": sum(r.device_ms for r in r64) / len(r64) / 1e3,
+                "iterations": r64[-1].iterations, "status": r64[-1].status_name}
+    # End to end through the C ABI from pinned host buffers.
+    e2e_times = []
+    h2d = (lp.colptr.nbytes + lp.rowidx.nbytes + lp.vals.nbytes + lp.cost.nbytes +
+           lp.lower.nbytes + lp.upper.nbytes)
+    d2h = 8 * (lp.n + lp.m) + 8 * lp.m
+    pinned = _pinned_problem(lp)
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        r = sg.solve_pdlp(pinned, opts)
+        e2e_times.append(time.perf_counter() - t0)
+        assert r.status == sg.OPTIMAL
+    # Roofline of the dominant kernel: event-timed launches on the engine's stream.
+    ms_dual, ms_primal, ms_eval = solver.time_kernels(20)
+    vb = 4 if mixed else 8
+    pbytes = primal_step_bytes(lp, vb)
+    dbytes = dual_step_bytes(lp, vb)
+    peak, peak_kind = peak_hbm()
+    ach = pbytes / (ms_primal * 1e-3) / 1e9
+    traffic = traffic_summary().get(f"{args.workload}_{'fp32' if mixed else 'fp64'}_primal_step")
+    line = {
+        "metric": METRIC, "value": t_step, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64",
+        "data": "synthetic",
+        "config": dict(cfg, tol=TOL, precision="fp32 storage + fp64 refinement" if mixed
+                       else "fp64", algorithm="enhanced (inf-norm Ruiz + Pock-Chambolle, "
+                       "primal weight |c|/|b|)", l2="inputs larger than L2 (~260 MB)"),
+        "status": last.status_name, "iterations": last.iterations,
+        "refinement_rounds": last.refinement_rounds,
+        "relative_kkt": [last.primal_residual, last.dual_residual, last.gap],
+        "fp64": fp64,
+        "e2e": {"value": min(e2e_times), "unit": "s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(sum(r.kernel_launches for r in results)),
+        "roofline": {"bound": "hbm", "kernel": "primal_step (A'y + projected update)",
+                     "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "bytes_per_launch": pbytes, "ms_per_launch": ms_primal,
+                     "dual_step": {"bytes_per_launch": dbytes, "ms_per_launch": ms_dual,
+                                   "achieved": dbytes / (ms_dual * 1e-3) / 1e9},
+                     "evaluation_ms": ms_eval},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1:
+        dt, conv, iters, worst = cpu_reference_run(lp)
+        line["cpu_baseline"] = {
+            "value": dt, "unit": "s", "cores": 1, "kind": "port",
+            "sample": f"reference CPU PDLP (oracle port of samaya src/lp/pdlp.cpp) to 1e-8 "
+                      f"capped at {CPU_CAP_S:.0f} s on the same LP: converged={conv}, "
+                      f"{iters} iterations, worst relative residual {worst:.2e} (value is a "
+                      f"lower bound of its time to 1e-8 when not converged)",
+            "converged": conv}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def _pinned_problem(lp):
+    """The LpProblem's arrays copied into page-locked host memory (torch), if available."""
+    try:
+        import torch
+        from samaya_gb300.model import LpProblem
+
+        def pin(a):
+            t = torch.from_numpy(a.copy()).pin_memory()
+            return t.numpy()
+        return LpProblem(m=lp.m, n=lp.n, colptr=pin(lp.colptr), rowidx=pin(lp.rowidx),
+                         vals=pin(lp.vals), cost=pin(lp.cost), lower=pin(lp.lower),
+                         upper=pin(lp.upper))
+    except Exception:
+        return lp
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -93,6 +93,7 @@ typedef struct sg_pdlp_result {
   double step_size;         /* 0.99 / ||[A -I]|| estimate */
   double primal_weight;     /* final omega */
   long long kernel_launches;
+  double device_ms;         /* CUDA-event time of the whole solve on the engine's stream */
 } sg_pdlp_result;
 
 /* Fills the defaults (tol 1e-8, automatic iteration limit, no time limit, FP64). */
@@ -154,6 +155,33 @@ int sg_pdhg_restart_to(sg_pdlp* handle, int which);
 /* PdhgDevice::download (pdhg_core.cu:382-402); any pointer may be NULL. */
 int sg_pdhg_download(sg_pdlp* handle, double* v, double* v_new, double* y, double* y_new,
                      double* v_erg, double* y_erg);
+
+/* Device time of the engine's hot kernels, measured with CUDA events on the engine's own stream
+ * after a solve: the average milliseconds of one dual step (rows of A), one primal step
+ * (rows of A') and one evaluation pair, over `reps` launches each. Diagnostics for the
+ * roofline report; the iterate is left unusable (the next solve starts afresh). */
+int sg_pdlp_time_kernels(sg_pdlp* handle, int reps, double* ms_dual, double* ms_primal,
+                         double* ms_eval);
+
+/* Model -> LpProblem: samaya's power-of-two scaling and computational form, as
+ * compute_scaling + make_problem compute them (reference src/linalg/scaling.cpp:130-200,
+ * src/lp/lp_solver.cpp:28-51). The model is min/max obj'x s.t. row_lower <= A x <= row_upper,
+ * col_lower <= x <= col_upper with A in CSC form. Writes the scaled A (lp_colptr n + 1,
+ * lp_rowidx/lp_val sized by the model's nonzeros; *lp_nnz set), cost/lower/upper (n + m) and
+ * the scale factors (col n, row m). Host only; no GPU needed. */
+int sg_scale_model(int m, int n, const int64_t* a_colptr, const int32_t* a_rowidx,
+                   const double* a_val, const double* obj, const double* col_lower,
+                   const double* col_upper, const double* row_lower, const double* row_upper,
+                   int maximize, int64_t* lp_colptr, int32_t* lp_rowidx, double* lp_val,
+                   double* cost, double* lower, double* upper, double* col_scale,
+                   double* row_scale, int64_t* lp_nnz);
+
+/* A PDLP answer (LpProblem space, x_lp n + m, y_lp m) back to the model, as samaya's
+ * solve_pdlp_lp maps it (reference src/core/solver.cpp:415-432): column values x (n), row
+ * activities (m), and row duals with the convention d = c - A'y (m). Any output may be NULL. */
+int sg_unscale_solution(int m, int n, const double* col_scale, const double* row_scale,
+                        int maximize, const double* x_lp, const double* y_lp, double* x,
+                        double* row_activity, double* row_dual);
 
 /* y = A x (transpose = 0, x: n, y: m) or y = A'x (transpose = 1) with the engine's
  * load-balanced tile kernel on the uploaded values; replaces gpu::csr_spmv (reference

@@ -34,7 +34,7 @@ class Result(ctypes.Structure):
                 ("has_dual_ray", ctypes.c_int), ("has_primal_ray", ctypes.c_int),
                 ("setup_seconds", ctypes.c_double), ("solve_seconds", ctypes.c_double),
                 ("step_size", ctypes.c_double), ("primal_weight", ctypes.c_double),
-                ("kernel_launches", ctypes.c_longlong)]
+                ("kernel_launches", ctypes.c_longlong), ("device_ms", ctypes.c_double)]
 
 
 _lib = None
@@ -103,6 +103,13 @@ def _declare(lib):
         "sg_pdhg_download": (I, [P, c_double_p, c_double_p, c_double_p, c_double_p, c_double_p,
                                  c_double_p]),
         "sg_spmv": (I, [P, I, c_double_p, c_double_p]),
+        "sg_pdlp_time_kernels": (I, [P, I, c_double_p, c_double_p, c_double_p]),
+        "sg_scale_model": (I, [I, I, c_int64_p, c_int32_p, c_double_p, c_double_p, c_double_p,
+                               c_double_p, c_double_p, c_double_p, I, c_int64_p, c_int32_p,
+                               c_double_p, c_double_p, c_double_p, c_double_p, c_double_p,
+                               c_double_p, c_int64_p]),
+        "sg_unscale_solution": (I, [I, I, c_double_p, c_double_p, I, c_double_p, c_double_p,
+                                    c_double_p, c_double_p, c_double_p]),
     }
     for name, (res, args) in sig.items():
         if hasattr(lib, name):

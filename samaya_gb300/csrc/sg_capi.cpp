@@ -118,6 +118,7 @@ int sg_pdlp_solve(sg_pdlp* handle, sg_pdlp_result* result, double* x, double* y,
     result->step_size = info.step_size;
     result->primal_weight = info.omega;
     result->kernel_launches = info.kernel_launches;
+    result->device_ms = info.device_ms;
     return SG_OK;
   } catch (const std::bad_alloc&) {
     return fail(SG_ERR_OUT_OF_MEMORY, "host allocation failed");
@@ -215,6 +216,14 @@ int sg_pdhg_restart_to(sg_pdlp* handle, int which) {
 int sg_pdhg_download(sg_pdlp* handle, double* v, double* v_new, double* y, double* y_new,
                      double* v_erg, double* y_erg) {
   SG_SEAM(handle->engine->seam_download(v, v_new, y, y_new, v_erg, y_erg));
+}
+
+int sg_pdlp_time_kernels(sg_pdlp* handle, int reps, double* ms_dual, double* ms_primal,
+                         double* ms_eval) {
+  if (ms_dual == nullptr || ms_primal == nullptr || ms_eval == nullptr || reps <= 0) {
+    return fail(SG_ERR_INVALID_ARGUMENT, "bad arguments");
+  }
+  SG_SEAM(handle->engine->time_kernels(reps, ms_dual, ms_primal, ms_eval));
 }
 
 int sg_spmv(sg_pdlp* handle, int transpose, const double* x, double* y) {

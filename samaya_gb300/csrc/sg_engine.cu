@@ -639,8 +639,20 @@ int Engine::solve(SolveInfo* info, double* x, double* y, double* dual_ray, doubl
                   std::string* err) {
   *info = SolveInfo();
   seam_mode_ = false;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, stream_);
   int rc = fp32_ ? solve_refined(info, x, y, dual_ray, primal_ray)
                  : solve_fp64(info, x, y, dual_ray, primal_ray);
+  cudaEventRecord(e1, stream_);
+  if (cudaEventSynchronize(e1) == cudaSuccess) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    info->device_ms = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   if (rc != kOk && err) *err = std::string("solve failed: ") + cudaGetErrorString(cudaGetLastError());
   return rc;
 }
@@ -1024,6 +1036,72 @@ int Engine::seam_download(double* v, double* v_new, double* y, double* y_new, do
   if (y_new && m) SG_TRY(cudaMemcpy(y_new, it64_.Y[p ^ 1], m * sizeof(double), cudaMemcpyDeviceToHost));
   if (v_erg) SG_TRY(cudaMemcpy(v_erg, it64_.Verg, nt * sizeof(double), cudaMemcpyDeviceToHost));
   if (y_erg && m) SG_TRY(cudaMemcpy(y_erg, it64_.Yerg, m * sizeof(double), cudaMemcpyDeviceToHost));
+  return kOk;
+}
+
+namespace {
+
+template <typename T>
+int time_steps(Ctl* c, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
+               const EvalView& ev, const RedView& red, int gsk, int gst, int gk, int gt,
+               int reps, cudaStream_t s, double* ms) {
+  cudaEvent_t e[4];
+  for (auto& x : e) {
+    if (cudaEventCreate(&x) != cudaSuccess) return kErrCuda;
+  }
+  for (int r = 0; r < 2; ++r) {
+    launch_dual_step(c, K, it, r, gsk, s);
+    launch_primal_step(c, Kt, it, r, gst, s);
+  }
+  cudaEventRecord(e[0], s);
+  for (int r = 0; r < reps; ++r) launch_dual_step(c, K, it, r & 1, gsk, s);
+  cudaEventRecord(e[1], s);
+  for (int r = 0; r < reps; ++r) launch_primal_step(c, Kt, it, r & 1, gst, s);
+  cudaEventRecord(e[2], s);
+  for (int r = 0; r < reps; ++r) launch_eval(c, K, Kt, it, ev, red, gk, gt, 0, s);
+  cudaEventRecord(e[3], s);
+  const cudaError_t err = cudaEventSynchronize(e[3]);
+  float a = 0, b = 0, d = 0;
+  cudaEventElapsedTime(&a, e[0], e[1]);
+  cudaEventElapsedTime(&b, e[1], e[2]);
+  cudaEventElapsedTime(&d, e[2], e[3]);
+  ms[0] = a / reps;
+  ms[1] = b / reps;
+  ms[2] = d / reps;
+  for (auto& x : e) cudaEventDestroy(x);
+  return err == cudaSuccess ? kOk : kErrCuda;
+}
+
+}  // namespace
+
+int Engine::time_kernels(int reps, double* ms_dual, double* ms_primal, double* ms_eval) {
+  std::string* err = nullptr;
+  Ctl* c = fp32_ ? ctl32_ : ctl_;
+  SG_TRY(cudaStreamSynchronize(stream_));
+  Ctl h;
+  SG_TRY(cudaMemcpy(&h, c, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  h.done = 0;
+  h.t = 0;
+  h.k = 0;
+  h.max_iter = std::numeric_limits<long long>::max();
+  SG_TRY(cudaMemcpy(c, &h, sizeof(Ctl), cudaMemcpyHostToDevice));
+  double ms[3] = {0, 0, 0};
+  int rc;
+  if (fp32_) {
+    IterView<float> it = iter_view(it32_);
+    it.rhs = it32_.rhs;
+    rc = time_steps(c, K_.view32(), Kt_.view32(), it, inner_eval_view(), red_view(),
+                    grid_step_k_, grid_step_t_, grid_k_, grid_t_, reps, stream_, ms);
+  } else {
+    rc = time_steps(c, K_.view64(), Kt_.view64(), iter_view(it64_), eval_view(), red_view(),
+                    grid_step_k_, grid_step_t_, grid_k_, grid_t_, reps, stream_, ms);
+  }
+  if (rc != kOk) return rc;
+  *ms_dual = ms[0];
+  *ms_primal = ms[1];
+  *ms_eval = ms[2];
+  h.done = 1;
+  SG_TRY(cudaMemcpy(c, &h, sizeof(Ctl), cudaMemcpyHostToDevice));
   return kOk;
 }
 

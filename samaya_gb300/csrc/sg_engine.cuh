@@ -48,6 +48,7 @@ struct SolveInfo {
   int has_dual_ray = 0, has_primal_ray = 0;
   long long graph_launches = 0;
   long long kernel_launches = 0;
+  double device_ms = 0;
 };
 
 // A device operator by rows with its tiles.
@@ -127,6 +128,10 @@ class Engine {
                     double* y_erg);
   // y = K x (rows of A) or y = K' x through the tile kernel (FP64).
   int spmv(int transpose, const double* x, double* y);
+  // Average device milliseconds of the step kernels and the evaluation (CUDA events).
+  int time_kernels(int reps, double* ms_dual, double* ms_primal, double* ms_eval);
+  int tile_capacity(int transpose) const { return transpose ? Kt_.cap_nnz : K_.cap_nnz; }
+  bool fp32() const { return fp32_; }
 
   int m() const { return m_; }
   int n() const { return n_; }

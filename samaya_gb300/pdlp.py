@@ -75,6 +75,7 @@ class PdlpResult:
     step_size: float = 0.0
     primal_weight: float = 1.0
     kernel_launches: int = 0
+    device_ms: float = 0.0
 
     @property
     def status_name(self) -> str:
@@ -108,8 +109,31 @@ class PdlpSolver:
             _ptr(lp.cost, ctypes.c_double), _ptr(lp.lower, ctypes.c_double),
             _ptr(lp.upper, ctypes.c_double), ctypes.byref(o)), "sg_pdlp_create")
 
-    def solve(self, x_out: np.ndarray | None = None, y_out: np.ndarray | None = None) -> PdlpResult:
+    def time_kernels(self, reps: int = 20):
+        """Average device ms of one dual step, one primal step and one evaluation (CUDA events
+        on the engine's stream); the next solve starts afresh."""
+        a, b, c = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
+        _native.check(self._lib.sg_pdlp_time_kernels(self._h, reps, ctypes.byref(a),
+                                                     ctypes.byref(b), ctypes.byref(c)),
+                      "sg_pdlp_time_kernels")
+        return a.value, b.value, c.value
+
+    def solve(self, x_out: np.ndarray | None = None, y_out: np.ndarray | None = None,
+              download: bool = True) -> PdlpResult:
+        """Solves; with ``download=False`` the answer stays on the device (x, y empty)."""
         lp = self.lp
+        if not download:
+            r = _native.Result()
+            _native.check(self._lib.sg_pdlp_solve(self._h, ctypes.byref(r), None, None, None,
+                                                  None), "sg_pdlp_solve")
+            return PdlpResult(status=r.status, iterations=r.iterations,
+                              primal_residual=r.primal_residual, dual_residual=r.dual_residual,
+                              gap=r.gap, primal_objective=r.primal_objective,
+                              dual_objective=r.dual_objective, restarts=r.restarts,
+                              evaluations=r.evaluations, refinement_rounds=r.refinement_rounds,
+                              setup_seconds=r.setup_seconds, solve_seconds=r.solve_seconds,
+                              step_size=r.step_size, primal_weight=r.primal_weight,
+                              kernel_launches=r.kernel_launches, device_ms=r.device_ms)
         x = x_out if x_out is not None else np.zeros(lp.n + lp.m)
         y = y_out if y_out is not None else np.zeros(max(lp.m, 1))
         dr = np.zeros(max(lp.m, 1))
@@ -125,7 +149,7 @@ class PdlpSolver:
                          evaluations=r.evaluations, refinement_rounds=r.refinement_rounds,
                          setup_seconds=r.setup_seconds, solve_seconds=r.solve_seconds,
                          step_size=r.step_size, primal_weight=r.primal_weight,
-                         kernel_launches=r.kernel_launches)
+                         kernel_launches=r.kernel_launches, device_ms=r.device_ms)
         if r.has_dual_ray:
             out.dual_ray = dr[:lp.m].copy()
         if r.has_primal_ray:

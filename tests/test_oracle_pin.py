@@ -95,3 +95,17 @@ def test_oracle_against_live_reference(oracle):
             b = oracle.pdlp_solve(*args, tol=1e-6, max_iter=20000)
             assert a["status"] == b.status and a["iterations"] == b.iterations
             assert np.array_equal(a["x"], b.x) and np.array_equal(a["y"], b.y)
+
+
+@pytest.mark.parametrize("group", GROUPS)
+def test_engine_host_scaling_matches_reference_fixtures(group):
+    """The engine library's host-side compute_scaling + make_problem (C++, no GPU) gives the
+    reference's scaled LpProblem bit-for-bit."""
+    from samaya_gb300 import _native
+    _native.load(build_if_missing=True)
+    from samaya_gb300.problem import make_problem
+    for c in load_group(group):
+        lp, sc = make_problem(c.model)
+        assert np.array_equal(sc.col, c.col_scale) and np.array_equal(sc.row, c.row_scale)
+        for k in ("colptr", "rowidx", "vals", "cost", "lower", "upper"):
+            assert np.array_equal(getattr(lp, k), getattr(c.lp, k)), (group, c.k, k)
