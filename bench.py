@@ -162,7 +162,9 @@ def cpu_reference_run(lp, cap_s=CPU_CAP_S):
     t0 = time.perf_counter()
     r = o.pdlp_solve(*lp.arrays(), tol=TOL, max_iter=-1, time_limit=cap_s)
     dt = time.perf_counter() - t0
-    worst = max(r.primal_residual, r.dual_residual, abs(r.gap))
+    last = r.stats.get("last", (r.primal_residual, r.dual_residual, r.gap))
+    worst = max(last[0], last[1], abs(last[2])) if r.status != o.OPTIMAL else max(
+        r.primal_residual, r.dual_residual, abs(r.gap))
     return dt, r.status == o.OPTIMAL, r.iterations, worst
 
 

@@ -43,7 +43,7 @@ def build(force: bool = False) -> str:
 class _Stats(ctypes.Structure):
     _fields_ = [("restarts", ctypes.c_longlong), ("evaluations", ctypes.c_longlong),
                 ("omega", ctypes.c_double), ("step_size", ctypes.c_double),
-                ("operator_norm", ctypes.c_double)]
+                ("operator_norm", ctypes.c_double), ("last", ctypes.c_double * 3)]
 
 
 _lib = None
@@ -105,7 +105,8 @@ def pdlp_solve(m, n, colptr, rowidx, vals, cost, lower, upper, tol=1e-8, max_ite
     return OracleResult(status, iters.value, res[0], res[1], res[2], x, y[:m],
                         dr[:m] if flags[0] else None, pr[:n] if flags[1] else None,
                         dict(restarts=st.restarts, evaluations=st.evaluations, omega=st.omega,
-                             step_size=st.step_size, operator_norm=st.operator_norm))
+                             step_size=st.step_size, operator_norm=st.operator_norm,
+                             last=tuple(st.last)))
 
 
 def compute_scaling(m, n, colptr, rowidx, vals):

@@ -661,6 +661,7 @@ typedef struct {
   double omega;
   double step_size; /* eta = 0.99 / L */
   double operator_norm;
+  double last[3]; /* relative primal, dual, gap of the current iterate at the last evaluation */
 } orc_stats_t;
 
 /* The CPU branch of solve_pdlp_once (src/lp/pdlp.cpp:250-1193). A is the LpProblem's CSC
@@ -771,6 +772,7 @@ int orc_pdlp_solve(int m, int n, const int64_t* colptr, const int32_t* rowidx, c
 
   double kkt_at_restart = ORC_INF, kkt_previous = ORC_INF;
   long long restarts = 0, evaluations = 0;
+  measure_t last_meas = {ORC_INF, ORC_INF, ORC_INF, 0.0, 0.0, 0.0};
   int done = 0;
   for (long long iter = 0; iter < max_iter && !done; ++iter) {
     if (has_limit && now_seconds() - t_start > time_limit) {
@@ -822,6 +824,7 @@ int orc_pdlp_solve(int m, int n, const int64_t* colptr, const int32_t* rowidx, c
     ++evaluations;
     measure_t cur = finish(&e, eval_sums(&e, v_new, y_new));
     measure_t avg = finish(&e, eval_sums(&e, v_erg, y_erg));
+    last_meas = cur;
     if (cur.rel_primal < tol && cur.rel_dual < tol && fabs(cur.rel_gap) < tol) {
       status = ORC_OPTIMAL;
       result_iterations = iter + 1;
@@ -927,6 +930,9 @@ int orc_pdlp_solve(int m, int n, const int64_t* colptr, const int32_t* rowidx, c
     stats->omega = omega;
     stats->step_size = eta;
     stats->operator_norm = L;
+    stats->last[0] = last_meas.rel_primal;
+    stats->last[1] = last_meas.rel_dual;
+    stats->last[2] = last_meas.rel_gap;
   }
 
   free(e.x_orig); free(e.r_orig); free(e.y_orig); free(e.ax); free(e.aty);
