@@ -44,17 +44,20 @@ std::vector<double> power_start(int m) {
 
 }  // namespace
 
-// Tiles: consecutive rows while the tile holds at most tile_nnz nonzeros and tile_rows rows; a
-// row longer than tile_nnz becomes ceil(len / tile_nnz) segment tiles of its own.
+// Tiles: a row longer than tile_nnz / 8 is reduced by a whole CTA, as ceil(len / tile_nnz)
+// segment tiles of its own; the other rows go consecutively into tiles of at most tile_nnz
+// nonzeros and tile_rows rows, with team = the power of two nearest below half the tile's mean
+// row length (1..32 lanes per row).
 void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, std::vector<Tile>* out,
                  int* nlong) {
   out->clear();
   *nlong = 0;
   const int rows = static_cast<int>(ptr.size()) - 1;
+  const int long_len = std::max(64, tile_nnz / 8);
   int r = 0;
   while (r < rows) {
     const int len = ptr[r + 1] - ptr[r];
-    if (len > tile_nnz) {
+    if (len > long_len) {
       const int nseg = (len + tile_nnz - 1) / tile_nnz;
       for (int s = 0; s < nseg; ++s) {
         Tile t{};
@@ -76,7 +79,7 @@ void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, std::
     const int r0 = r;
     while (r < rows && r - r0 < tile_rows) {
       const int l = ptr[r + 1] - ptr[r];
-      if (l > tile_nnz) break;
+      if (l > long_len) break;
       if (ptr[r + 1] - ptr[r0] > tile_nnz) break;
       ++r;
     }
@@ -88,7 +91,7 @@ void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, std::
     t.kind = 0;
     const double mean = static_cast<double>(t.k1 - t.k0) / std::max(1, r - r0);
     int team = 1;
-    while (team < 32 && team < mean) team *= 2;
+    while (team < 32 && 2 * team * 2 <= mean) team *= 2;
     t.team = team;
     t.seg = 0;
     t.nseg = 1;
