@@ -54,36 +54,58 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
   for (int ti = blockIdx.x; ti < ts.ntiles; ti += gridDim.x) {
     const Tile tile = ts.tiles[ti];
     if (tile.kind == 0) {
-      const int team = tile.team;
-      const int nteams = kBlock / team;
-      const int my_team = tid / team;
-      const int lane = tid % team;
+      // One thread per row; a row longer than a warp is taken over by its whole warp (ballot
+      // queue), so skewed row lengths inside a tile cost no serial tail.
+      const int lane = tid & 31;
       const int nrows = tile.r1 - tile.r0;
-      const int rounds = (nrows + nteams - 1) / nteams;
+      const int rounds = (nrows + kBlock - 1) / kBlock;
       for (int rr = 0; rr < rounds; ++rr) {
-        const int lr = rr * nteams + my_team;
+        const int lr = rr * kBlock + tid;
         const bool valid = lr < nrows;
-        ACC s[NV];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) s[v] = ACC(0);
+        int b = 0, e = 0;
         if (valid) {
-          const int b = ldg(ptr + tile.r0 + lr);
-          const int e = ldg(ptr + tile.r0 + lr + 1);
+          b = ldg(ptr + tile.r0 + lr);
+          e = ldg(ptr + tile.r0 + lr + 1);
+        }
+        const bool shortrow = valid && e - b <= 32;
+        if (shortrow) {
+          ACC s[NV];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) s[v] = ACC(0);
 #pragma unroll 4
-          for (int q = b + lane; q < e; q += team) {
+          for (int q = b; q < e; ++q) {
             const T a = ldg(val + q);
             const int j = ldg(idx + q);
 #pragma unroll
             for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
           }
+          epi.row(tile.r0 + lr, s);
         }
-        for (int o = team / 2; o > 0; o >>= 1) {
+        unsigned pending = __ballot_sync(0xffffffffu, valid && !shortrow);
+        while (pending != 0u) {
+          const int src = __ffs(pending) - 1;
+          pending &= pending - 1u;
+          const int rb = __shfl_sync(0xffffffffu, b, src);
+          const int re = __shfl_sync(0xffffffffu, e, src);
+          ACC s[NV];
 #pragma unroll
-          for (int v = 0; v < NV; ++v) {
-            s[v] = combine<MAXRED>(s[v], __shfl_down_sync(0xffffffffu, s[v], o, team));
+          for (int v = 0; v < NV; ++v) s[v] = ACC(0);
+#pragma unroll 4
+          for (int q = rb + lane; q < re; q += 32) {
+            const T a = ldg(val + q);
+            const int j = ldg(idx + q);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
           }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+              s[v] = combine<MAXRED>(s[v], __shfl_down_sync(0xffffffffu, s[v], o));
+            }
+          }
+          if (lane == 0) epi.row(tile.r0 + rr * kBlock + (tid & ~31) + src, s);
         }
-        if (lane == 0 && valid) epi.row(tile.r0 + lr, s);
       }
     } else {
       // A segment of a long row: strided sums, then the fixed block tree.
@@ -104,6 +126,16 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
       }
       double tot[NV];
       block_reduce<NV, MAXRED ? 0xFFu : 0u>(part, red, tot);
+      if (tile.nseg == 1) {
+        // The whole row in one tile: no partials to combine.
+        if (tid == 0) {
+          ACC s[NV];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) s[v] = static_cast<ACC>(tot[v]);
+          epi.long_row(tile.lrow, tile.r0, s);
+        }
+        continue;
+      }
       if (tid == 0) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) ts.seg_part[ti * kMaxVec + v] = tot[v];
