@@ -828,7 +828,7 @@ int Engine::solve_refined(SolveInfo* info, double* x, double* y, double* dual_ra
     if (round > 0) {
       launch_ir_residual(ctl32_, K_.view64(), Kt_.view64(), irv, grid_k_, grid_t_, s);
     }
-    launch_ir_scales(ctl32_, round, 1e6, s);
+    launch_ir_scales(ctl32_, round, 1e4, s);
     launch_ir_build(ctl32_, irv, round, s);
     for (float* p : {it32_.V[0], it32_.V[1], it32_.Vbar, it32_.Verg, it32_.Vrst}) {
       SG_TRY(cudaMemsetAsync(p, 0, nt * sizeof(float), s));

@@ -17,10 +17,16 @@ namespace sg {
 
 namespace {
 
-__device__ __forceinline__ double bound_lambda(double g, double lo, double up) {
-  const bool hl = lo > -INFINITY;
-  const bool hu = up < INFINITY;
-  return hl && hu ? g : hl ? fmax(g, 0.0) : hu ? fmin(g, 0.0) : 0.0;
+// Dual violation of a reduced cost g at a point v in [lo, up]: the part of g that the point's
+// active bounds cannot absorb (a positive g needs v at its lower bound, a negative g v at its
+// upper bound). This covers dual infeasibility and complementarity, so a correction problem is
+// scaled to what is still wrong even when every variable is boxed.
+__device__ __forceinline__ double dual_violation(double g, double v, double lo, double up) {
+  const bool at_lo = lo > -INFINITY && v <= lo;
+  const bool at_up = up < INFINITY && v >= up;
+  if (g > 0.0) return at_lo ? 0.0 : g;
+  if (g < 0.0) return at_up ? 0.0 : -g;
+  return 0.0;
 }
 
 struct Gather64 {
@@ -46,7 +52,7 @@ struct ResRowEpi {
     bh[i] = b;
     const double g = cost[n + i] - y[i];
     d[n + i] = g;
-    const double viol = fabs(g - bound_lambda(g, lower[n + i], upper[n + i]));
+    const double viol = dual_violation(g, v[n + i], lower[n + i], upper[n + i]);
     a[0] = fmax(a[0], fabs(b));
     a[1] = fmax(a[1], viol);
   }
@@ -61,6 +67,7 @@ struct ResRowEpi {
 
 // Columns: d_j = c_j + (A_eq' y*)_j and its dual violation.
 struct ResColEpi {
+  const double* v;
   const double* cost;
   const double* lower;
   const double* upper;
@@ -70,7 +77,7 @@ struct ResColEpi {
   __device__ __forceinline__ void terms(int j, double s, double (&a)[2]) {
     const double g = cost[j] + s;
     d[j] = g;
-    a[1] = fmax(a[1], fabs(g - bound_lambda(g, lower[j], upper[j])));
+    a[1] = fmax(a[1], dual_violation(g, v[j], lower[j], upper[j]));
   }
   __device__ __forceinline__ void row(int j, const double (&s)[1]) { terms(j, s[0], acc); }
   __device__ __forceinline__ void long_row(int lrow, int j, const double (&s)[1]) {
@@ -110,6 +117,7 @@ __global__ void __launch_bounds__(kBlock) ir_rows_kernel(Ctl* c, OpView<double> 
 
 __global__ void __launch_bounds__(kBlock) ir_cols_kernel(Ctl* c, OpView<double> Kt, IrView v) {
   ResColEpi epi;
+  epi.v = v.v;
   epi.cost = v.cost_eq;
   epi.lower = v.lower_eq;
   epi.upper = v.upper_eq;
@@ -147,8 +155,10 @@ __global__ void ir_scales_kernel(Ctl* c, int round, double growth) {
     c->ir_dd_prev = dd_prev;
     c->ir_dp = dp;
     c->ir_dd = dd;
-    // The correction scales primal by dp and dual by dd: carry the weight over accordingly.
-    c->omega = c->omega * (dd / dd_prev) / (dp / dp_prev);
+    // The correction scales primal by dp and dual by dd: carry the weight over accordingly,
+    // within four orders of magnitude of the first round's.
+    const double w = c->omega * (dd / dd_prev) / (dp / dp_prev);
+    c->omega = fmin(fmax(w, 1e-4 * c->ir_omega0), 1e4 * c->ir_omega0);
   }
   c->tau = c->eta / c->omega;
   c->sigma = c->eta * c->omega;

@@ -39,6 +39,7 @@ class PdlpOptions:
     refine_max_rounds: int = 6
     inner_tol: float = 1e-4
     algorithm: int = REFERENCE
+    verbose: int = 0
 
     def to_c(self) -> _native.Opts:
         o = _native.Opts()
@@ -50,6 +51,7 @@ class PdlpOptions:
         o.refine_max_rounds = int(self.refine_max_rounds)
         o.inner_tol = float(self.inner_tol)
         o.algorithm = int(self.algorithm)
+        o.verbose = int(self.verbose)
         return o
 
 
