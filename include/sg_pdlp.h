@@ -188,6 +188,23 @@ int sg_unscale_solution(int m, int n, const double* col_scale, const double* row
  * src/gpu/spmv.cu:91-120) for the parity tests. */
 int sg_spmv(sg_pdlp* handle, int transpose, const double* x, double* y);
 
+/* ---- Allocation-free SpMV. This entry point has no counterpart in the reference: it is for
+ * callers that cannot call cudaMalloc (work recorded into a CUDA graph, a memory pool or budget
+ * that forbids driver allocations, device memory handed out by another runtime). It computes
+ * y = A x for A in CSR form (m rows, nnz nonzeros, 32-bit row starts) where every array is a
+ * DEVICE pointer owned by the caller, on `stream` (a cudaStream_t; NULL for the default
+ * stream), and allocates nothing: its only scratch is a file-scope device array of
+ * SG_SPMV_NOALLOC_MAX_CHUNKS carry records (16 bytes each, 1 MiB) that every GPU loading the
+ * library holds until the process exits. Matrices with more than
+ * SG_SPMV_NOALLOC_MAX_CHUNKS * 2048 nonzeros are refused with SG_ERR_TOO_LARGE.
+ * The first call on a device looks the scratch's device address up (once per device); make
+ * that first call before any stream capture. All calls share the scratch, so calls that
+ * overlap on the GPU (concurrent streams, or several host threads) race; serialise them.
+ * Deterministic: a re-run gives the same bits. Returns SG_OK or an SG_ERR_* code. */
+#define SG_SPMV_NOALLOC_MAX_CHUNKS 65536
+int sg_spmv_noalloc(int m, long long nnz, const int* d_row_ptr, const int* d_col_idx,
+                    const double* d_val, const double* d_x, double* d_y, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
