@@ -67,19 +67,35 @@ struct DualEpi {
   T* yerg;
   T* verg_r;
   ACC sigma, tau, alpha, beta;
-  __device__ __forceinline__ void row(int i, const ACC (&s)[1]) {
-    ACC res = s[0] - static_cast<ACC>(vbar_r[i]);
-    if (q != nullptr) res -= static_cast<ACC>(q[i]);
-    const ACC yn = static_cast<ACC>(y[i]) + sigma * res;
-    y_new[i] = static_cast<T>(yn);
-    const ACC r = static_cast<ACC>(vr[i]);
-    ACC rn = r - tau * (static_cast<ACC>(c[i]) - yn);
-    rn = clampv<ACC>(rn, static_cast<ACC>(l[i]), static_cast<ACC>(u[i]));
-    vr_new[i] = static_cast<T>(rn);
-    vbar_r[i] = static_cast<T>(rn + (rn - r));
-    yerg[i] = static_cast<T>(beta * static_cast<ACC>(yerg[i]) + alpha * yn);
-    verg_r[i] = static_cast<T>(beta * static_cast<ACC>(verg_r[i]) + alpha * rn);
+  struct Pre {
+    ACC rbar, q, y, r, c, l, u, yerg, rerg;
+  };
+  __device__ __forceinline__ Pre load(int i) const {
+    Pre p;
+    p.rbar = static_cast<ACC>(vbar_r[i]);
+    p.q = q != nullptr ? static_cast<ACC>(q[i]) : ACC(0);
+    p.y = static_cast<ACC>(y[i]);
+    p.r = static_cast<ACC>(vr[i]);
+    p.c = static_cast<ACC>(c[i]);
+    p.l = static_cast<ACC>(l[i]);
+    p.u = static_cast<ACC>(u[i]);
+    p.yerg = static_cast<ACC>(yerg[i]);
+    p.rerg = static_cast<ACC>(verg_r[i]);
+    return p;
   }
+  __device__ __forceinline__ void row(int i, const ACC (&s)[1], const Pre& p) {
+    ACC res = s[0] - p.rbar;
+    if (q != nullptr) res -= p.q;
+    const ACC yn = p.y + sigma * res;
+    y_new[i] = static_cast<T>(yn);
+    ACC rn = p.r - tau * (p.c - yn);
+    rn = clampv<ACC>(rn, p.l, p.u);
+    vr_new[i] = static_cast<T>(rn);
+    vbar_r[i] = static_cast<T>(rn + (rn - p.r));
+    yerg[i] = static_cast<T>(beta * p.yerg + alpha * yn);
+    verg_r[i] = static_cast<T>(beta * p.rerg + alpha * rn);
+  }
+  __device__ __forceinline__ void row(int i, const ACC (&s)[1]) { row(i, s, load(i)); }
   __device__ __forceinline__ void long_row(int, int i, const ACC (&s)[1]) { row(i, s); }
 };
 
@@ -93,14 +109,26 @@ struct PrimalEpi {
   const T* u;
   T* xerg;
   ACC tau, alpha, beta;
-  __device__ __forceinline__ void row(int j, const ACC (&s)[1]) {
-    const ACC xo = static_cast<ACC>(x[j]);
-    ACC xn = xo - tau * (static_cast<ACC>(c[j]) + s[0]);
-    xn = clampv<ACC>(xn, static_cast<ACC>(l[j]), static_cast<ACC>(u[j]));
-    x_new[j] = static_cast<T>(xn);
-    xbar[j] = static_cast<T>(xn + (xn - xo));
-    xerg[j] = static_cast<T>(beta * static_cast<ACC>(xerg[j]) + alpha * xn);
+  struct Pre {
+    ACC x, c, l, u, xerg;
+  };
+  __device__ __forceinline__ Pre load(int j) const {
+    Pre p;
+    p.x = static_cast<ACC>(x[j]);
+    p.c = static_cast<ACC>(c[j]);
+    p.l = static_cast<ACC>(l[j]);
+    p.u = static_cast<ACC>(u[j]);
+    p.xerg = static_cast<ACC>(xerg[j]);
+    return p;
   }
+  __device__ __forceinline__ void row(int j, const ACC (&s)[1], const Pre& p) {
+    ACC xn = p.x - tau * (p.c + s[0]);
+    xn = clampv<ACC>(xn, p.l, p.u);
+    x_new[j] = static_cast<T>(xn);
+    xbar[j] = static_cast<T>(xn + (xn - p.x));
+    xerg[j] = static_cast<T>(beta * p.xerg + alpha * xn);
+  }
+  __device__ __forceinline__ void row(int j, const ACC (&s)[1]) { row(j, s, load(j)); }
   __device__ __forceinline__ void long_row(int, int j, const ACC (&s)[1]) { row(j, s); }
 };
 

@@ -14,6 +14,8 @@
 // bit-identical.
 #pragma once
 
+#include <type_traits>
+
 #include "sg_common.cuh"
 
 namespace sg {
@@ -38,6 +40,39 @@ __device__ __forceinline__ ACC combine(ACC a, ACC b) {
     return a + b;
   }
 }
+
+// Epilogues that declare `struct Pre` split the row update into `Pre load(r)` (the row's own
+// vector entries, independent of the dot product) and `row(r, s, pre)`: the loads are issued
+// before the dot product so their latency overlaps it.
+template <typename E, typename = void>
+struct has_pre : std::false_type {};
+template <typename E>
+struct has_pre<E, std::void_t<typename E::Pre>> : std::true_type {};
+
+// 16-byte loads of four consecutive nonzeros (values and indices) at a 4-aligned position.
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+  __device__ __forceinline__ static void load(const float* v, int q, float (&out)[4]) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(v + q));
+    out[0] = a.x;
+    out[1] = a.y;
+    out[2] = a.z;
+    out[3] = a.w;
+  }
+};
+template <>
+struct Vec4<double> {
+  __device__ __forceinline__ static void load(const double* v, int q, double (&out)[4]) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(v + q));
+    const double2 b = __ldg(reinterpret_cast<const double2*>(v + q + 2));
+    out[0] = a.x;
+    out[1] = a.y;
+    out[2] = b.x;
+    out[3] = b.y;
+  }
+};
 
 // Prod: ACC operator()(int v, T val, int col) const — the v-th product of a nonzero.
 // Epi: void row(int r, const ACC (&s)[NV]) for rows of kind-0 tiles (lane 0 of the row's team),
@@ -68,18 +103,36 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
           e = ldg(ptr + tile.r0 + lr + 1);
         }
         const bool shortrow = valid && e - b <= 32;
-        if (shortrow) {
-          ACC s[NV];
+        if constexpr (has_pre<Epi>::value) {
+          typename Epi::Pre pre;
+          if (shortrow) pre = epi.load(tile.r0 + lr);
+          if (shortrow) {
+            ACC s[NV];
 #pragma unroll
-          for (int v = 0; v < NV; ++v) s[v] = ACC(0);
+            for (int v = 0; v < NV; ++v) s[v] = ACC(0);
 #pragma unroll 4
-          for (int q = b; q < e; ++q) {
-            const T a = ldg(val + q);
-            const int j = ldg(idx + q);
+            for (int q = b; q < e; ++q) {
+              const T a = ldg(val + q);
+              const int j = ldg(idx + q);
 #pragma unroll
-            for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
+              for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
+            }
+            epi.row(tile.r0 + lr, s, pre);
           }
-          epi.row(tile.r0 + lr, s);
+        } else {
+          if (shortrow) {
+            ACC s[NV];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) s[v] = ACC(0);
+#pragma unroll 4
+            for (int q = b; q < e; ++q) {
+              const T a = ldg(val + q);
+              const int j = ldg(idx + q);
+#pragma unroll
+              for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
+            }
+            epi.row(tile.r0 + lr, s);
+          }
         }
         unsigned pending = __ballot_sync(0xffffffffu, valid && !shortrow);
         while (pending != 0u) {
@@ -114,8 +167,33 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
         ACC s[NV];
 #pragma unroll
         for (int v = 0; v < NV; ++v) s[v] = ACC(0);
-#pragma unroll 4
-        for (int q = tile.k0 + tid; q < tile.k1; q += kBlock) {
+        // Head up to a 4-aligned position, then 16-byte loads of four nonzeros per thread,
+        // then the tail (scalar).
+        const int k0 = tile.k0;
+        const int k1 = tile.k1;
+        const int a0 = min(k1, (k0 + 3) & ~3);
+        const int a1 = max(a0, k1 & ~3);
+        if (k0 + tid < a0) {
+          const int q = k0 + tid;
+          const T a = ldg(val + q);
+          const int j = ldg(idx + q);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
+        }
+#pragma unroll 2
+        for (int q = a0 + 4 * tid; q < a1; q += 4 * kBlock) {
+          T a[4];
+          Vec4<T>::load(val, q, a);
+          const int4 j = __ldg(reinterpret_cast<const int4*>(idx + q));
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            s[v] = combine<MAXRED>(s[v], prod(v, a[0], j.x));
+            s[v] = combine<MAXRED>(s[v], prod(v, a[1], j.y));
+            s[v] = combine<MAXRED>(s[v], prod(v, a[2], j.z));
+            s[v] = combine<MAXRED>(s[v], prod(v, a[3], j.w));
+          }
+        }
+        for (int q = a1 + tid; q < k1; q += kBlock) {
           const T a = ldg(val + q);
           const int j = ldg(idx + q);
 #pragma unroll
