@@ -212,9 +212,12 @@ __device__ __forceinline__ void block_reduce(double (&v)[K], double* scratch, do
 // fixed order (thread t takes CTAs t, t + 256, ... in order, then the fixed block tree) and
 // calls `fin(totals)` from thread 0. The counter is reset by the last CTA so the kernel can be
 // replayed from a CUDA graph. Must be reached by every thread of every CTA.
+// `extra` (nextra records of stride kMaxSums, e.g. the terms of rows split over several CTAs)
+// is added by the last CTA too, spread over its threads in a fixed order.
 template <int K, unsigned MAXMASK = 0u, typename Fin>
 __device__ __forceinline__ void grid_reduce(double (&mine)[K], double* partial,
-                                            unsigned* counter, double* scratch, Fin fin) {
+                                            unsigned* counter, double* scratch, Fin fin,
+                                            const double* extra = nullptr, int nextra = 0) {
   __shared__ bool last;
   double blk[K];
   block_reduce<K, MAXMASK>(mine, scratch, blk);
@@ -235,6 +238,13 @@ __device__ __forceinline__ void grid_reduce(double (&mine)[K], double* partial,
 #pragma unroll
     for (int q = 0; q < K; ++q) {
       const double p = __ldcg(&partial[b * K + q]);
+      acc[q] = ((MAXMASK >> q) & 1u) ? fmax(acc[q], p) : acc[q] + p;
+    }
+  }
+  for (int l = threadIdx.x; l < nextra; l += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      const double p = __ldcg(&extra[l * kMaxSums + q]);
       acc[q] = ((MAXMASK >> q) & 1u) ? fmax(acc[q], p) : acc[q] + p;
     }
   }

@@ -288,17 +288,11 @@ struct EvalColEpi {
   }
 };
 
-// Adds the split rows' terms (in split-row order) to the grid totals and stores them.
+// Stores the grid totals (the split rows' terms are added by grid_reduce).
 struct EvalFin {
   double* out;
-  const double* long_terms;
-  int nlong;
   __device__ __forceinline__ void operator()(const double (&tot)[kEvalSums]) const {
-    for (int q = 0; q < kEvalSums; ++q) {
-      double s = tot[q];
-      for (int l = 0; l < nlong; ++l) s += __ldcg(long_terms + l * kMaxSums + q);
-      out[q] = s;
-    }
+    for (int q = 0; q < kEvalSums; ++q) out[q] = tot[q];
   }
 };
 
@@ -330,8 +324,9 @@ __global__ void __launch_bounds__(kBlock) eval_rows_kernel(Ctl* ctl, OpView<T> K
   for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0;
   Gather2<T> g{it.V[cur], it.Verg};
   run_tiles<T, double, 2>(K.ts, K.ptr, K.idx, K.val, g, epi);
-  EvalFin fin{ctl->eval_r, red.long_terms, K.ts.nlong};
-  grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, smem_red(), fin);
+  EvalFin fin{ctl->eval_r};
+  grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, smem_red(), fin, red.long_terms,
+                         K.ts.nlong);
 }
 
 template <typename T>
@@ -351,8 +346,9 @@ __global__ void __launch_bounds__(kBlock) eval_cols_kernel(Ctl* ctl, OpView<T> K
   for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0;
   Gather2<T> g{it.Y[cur], it.Yerg};
   run_tiles<T, double, 2>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
-  EvalFin fin{ctl->eval_c, red.long_terms, Kt.ts.nlong};
-  grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, smem_red(), fin);
+  EvalFin fin{ctl->eval_c};
+  grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, smem_red(), fin, red.long_terms,
+                         Kt.ts.nlong);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -590,7 +586,7 @@ struct FarkasColEpi {
   __device__ __forceinline__ void long_row(int lrow, int j, const double (&s)[1]) {
     const double a = s[0] / cs[j];
     aty[j] = a;
-    long_abs[lrow] = fabs(a);
+    long_abs[lrow * kMaxSums] = fabs(a);
   }
   double* long_abs;
 };
@@ -612,14 +608,10 @@ __global__ void __launch_bounds__(kBlock) det_farkas_cols_kernel(Ctl* c, OpView<
     }
   } g{it.Yerg};
   run_tiles<T, double, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
-  const int nlong = Kt.ts.nlong;
-  const double* la = red.long_terms;
-  grid_reduce<1>(epi.acc, red.partial, red.counter, smem_red(), [c, nlong, la](const double (&t)[1]) {
-    double s = t[0];
-    for (int l = 0; l < nlong; ++l) s += __ldcg(la + l);
+  grid_reduce<1>(epi.acc, red.partial, red.counter, smem_red(), [c](const double (&t)[1]) {
     // w_scale: columns first, then the logicals' |yf| (pdlp.cpp:761-767).
-    c->det[1] = s + c->det[1];
-  });
+    c->det[1] = t[0] + c->det[1];
+  }, red.long_terms, Kt.ts.nlong);
 }
 
 template <typename T>
@@ -799,23 +791,17 @@ __global__ void __launch_bounds__(kBlock) det_ray_rows_kernel(Ctl* c, OpView<T> 
   } g{epi.vn, epi.vo, ray_x, ev.cs, v_max};
   epi.inv_vmax = 1.0 / v_max;
   run_tiles<T, double, 2>(K.ts, K.ptr, K.idx, K.val, g, epi);
-  const int nlong = K.ts.nlong;
-  const double* lt = red.long_terms;
   grid_reduce<3, 4u>(epi.acc, red.partial, red.counter, smem_red(),
-                     [c, nlong, lt](const double (&t)[3]) {
-    double pf = t[0], cd = t[1], fail = t[2];
-    for (int l = 0; l < nlong; ++l) {
-      pf += __ldcg(lt + l * kMaxSums + 0);
-      cd += __ldcg(lt + l * kMaxSums + 1);
-      fail = fmax(fail, __ldcg(lt + l * kMaxSums + 2));
-    }
-    const double primal_feas = sqrt(pf);
+                     [c](const double (&t)[3]) {
+    const double cd = t[1];
+    const double fail = t[2];
+    const double primal_feas = sqrt(t[0]);
     const double cost_dir = c->det[7] + cd;
     c->det[6] = primal_feas;
     c->det[7] = cost_dir;
     const bool ok = c->det_flags[4] != 0 && !(fail > 0.0);
     c->det_flags[1] = (c->det[5] > 1e-6 && primal_feas < 1e-6 && cost_dir < -1e-8 && ok) ? 1 : 0;
-  });
+  }, red.long_terms, K.ts.nlong);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -968,13 +954,9 @@ __global__ void __launch_bounds__(kBlock) power_spmv_kernel(Ctl* c, OpView<doubl
   epi.acc[0] = 0.0;
   epi.long_terms = red.long_terms;
   run_tiles<double, double, 1>(A.ts, A.ptr, A.idx, A.val, Gather1<double, double>{x}, epi);
-  const int nlong = A.ts.nlong;
-  const double* lt = red.long_terms;
   grid_reduce<1>(epi.acc, red.partial, red.counter, smem_red(),
-                 [c, nlong, lt, which](const double (&t)[1]) {
-    double s = t[0];
-    for (int l = 0; l < nlong; ++l) s += __ldcg(lt + l * kMaxSums);
-    const double nrm = sqrt(s);
+                 [c, which](const double (&t)[1]) {
+    const double nrm = sqrt(t[0]);
     if (which == 0) {
       c->power_vnorm = nrm;
       if (nrm == 0.0) c->power_done = 1;
@@ -986,7 +968,7 @@ __global__ void __launch_bounds__(kBlock) power_spmv_kernel(Ctl* c, OpView<doubl
         c->power_sigma = nrm / c->power_vnorm;
       }
     }
-  });
+  }, red.long_terms, A.ts.nlong);
 }
 
 __global__ void scale_by_norm_kernel(const Ctl* c, double* u, int m, int first) {

@@ -101,18 +101,11 @@ __global__ void __launch_bounds__(kBlock) ir_rows_kernel(Ctl* c, OpView<double> 
   epi.acc[0] = epi.acc[1] = 0.0;
   epi.long_terms = v.red.long_terms;
   run_tiles<double, double, 1>(K.ts, K.ptr, K.idx, K.val, Gather64{v.v}, epi);
-  const int nlong = K.ts.nlong;
-  const double* lt = v.red.long_terms;
   grid_reduce<2, 3u>(epi.acc, v.red.partial, v.red.counter, smem_red(),
-                     [c, nlong, lt](const double (&t)[2]) {
-    double p = t[0], d = t[1];
-    for (int l = 0; l < nlong; ++l) {
-      p = fmax(p, __ldcg(lt + l * kMaxSums));
-      d = fmax(d, __ldcg(lt + l * kMaxSums + 1));
-    }
-    c->ir_pmax = p;
-    c->ir_dmax = d;
-  });
+                     [c](const double (&t)[2]) {
+    c->ir_pmax = t[0];
+    c->ir_dmax = t[1];
+  }, v.red.long_terms, K.ts.nlong);
 }
 
 __global__ void __launch_bounds__(kBlock) ir_cols_kernel(Ctl* c, OpView<double> Kt, IrView v) {
@@ -125,14 +118,10 @@ __global__ void __launch_bounds__(kBlock) ir_cols_kernel(Ctl* c, OpView<double> 
   epi.acc[0] = epi.acc[1] = 0.0;
   epi.long_terms = v.red.long_terms;
   run_tiles<double, double, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, Gather64{v.y}, epi);
-  const int nlong = Kt.ts.nlong;
-  const double* lt = v.red.long_terms;
   grid_reduce<2, 3u>(epi.acc, v.red.partial, v.red.counter, smem_red(),
-                     [c, nlong, lt](const double (&t)[2]) {
-    double d = t[1];
-    for (int l = 0; l < nlong; ++l) d = fmax(d, __ldcg(lt + l * kMaxSums + 1));
-    c->ir_dmax = fmax(c->ir_dmax, d);
-  });
+                     [c](const double (&t)[2]) {
+    c->ir_dmax = fmax(c->ir_dmax, t[1]);
+  }, v.red.long_terms, Kt.ts.nlong);
 }
 
 // Scale factors of the correction problem and its starting primal weight.
