@@ -188,6 +188,40 @@ int sg_unscale_solution(int m, int n, const double* col_scale, const double* row
  * src/gpu/spmv.cu:91-120) for the parity tests. */
 int sg_spmv(sg_pdlp* handle, int transpose, const double* x, double* y);
 
+/* ---- Batched PDLP: many LPs in one persistent launch (no counterpart in the reference, which
+ * solves one LP at a time; each instance follows samaya::solve_pdlp's algorithm,
+ * src/lp/pdlp.cpp:250-1193, with per-instance restarts and termination; infeasibility and
+ * unboundedness detection are not run in the batch). Matrices (nmat of them, m_g x n_g, CSC)
+ * are given concatenated: mat_colptr holds n_g + 1 local column starts per matrix, mat_rowidx
+ * and mat_val the nonzeros of each matrix in turn. Instance i uses matrix inst_mat[i] (several
+ * instances may share one: branch-and-bound node relaxations) and its own cost/lower/upper
+ * (n_g + m_g each, concatenated in instance order). x (n_g + m_g per instance) and y (m_g per
+ * instance) are returned concatenated in instance order. */
+typedef struct sg_batch sg_batch;
+
+typedef struct sg_batch_result {
+  int status;              /* SG_STATUS_* */
+  int pad;
+  long long iterations;
+  double primal_residual;  /* relative, as sg_pdlp_result */
+  double dual_residual;
+  double gap;
+  double primal_objective;
+  double dual_objective;
+  long long restarts;
+} sg_batch_result;
+
+int sg_batch_create(sg_batch** handle, int nmat, const int* mat_m, const int* mat_n,
+                    const int64_t* mat_colptr, const int32_t* mat_rowidx, const double* mat_val,
+                    int count, const int* inst_mat, const double* cost, const double* lower,
+                    const double* upper, const sg_pdlp_opts* opts);
+/* Solves every instance; results[count]; x, y may be NULL; *device_ms (may be NULL) gets the
+ * CUDA-event time of the launch. */
+int sg_batch_solve(sg_batch* handle, sg_batch_result* results, double* x, double* y,
+                   double* device_ms);
+void sg_batch_destroy(sg_batch* handle);
+const char* sg_batch_last_error(void);
+
 /* ---- Allocation-free SpMV. This entry point has no counterpart in the reference: it is for
  * callers that cannot call cudaMalloc (work recorded into a CUDA graph, a memory pool or budget
  * that forbids driver allocations, device memory handed out by another runtime). It computes

@@ -1,0 +1,671 @@
+// Batched PDLP: many LPs in one persistent launch (the engine's own; the reference solves one
+// LP at a time). Instances are stored as a segmented concatenated CSR: matrices (each by rows,
+// A, and by columns, A') concatenated with offsets, several instances may share one matrix
+// (branch-and-bound node relaxations: one A, many bound vectors), and every instance has its
+// own cost and bounds.
+//
+// Two kernels:
+//   batch_setup_kernel   one CTA per matrix: the residual-scale norms of A, Ruiz (or the
+//                        enhanced preconditioning), A_eq in place, and ||[A_eq -I]|| by power
+//                        iteration — shared by every instance of that matrix;
+//   batch_solve_kernel   persistent CTAs pull instances from a work queue (largest first) and
+//                        run the whole PDLP of one instance inside the CTA: the fused steps, the
+//                        evaluation every 64 iterations, the termination test, the restarts and
+//                        the primal-weight update of the single-LP engine (the reference's rules,
+//                        pdlp.cpp:493-541, 674-713, 1069-1131), per instance.
+// Row sums: one thread per row, a warp per row longer than 32 nonzeros (ballot queue), fixed
+// order, so a re-run is bit-identical.
+#include <math.h>
+#include <stdint.h>
+
+#include "sg_batch.cuh"
+
+namespace sg {
+
+namespace {
+
+constexpr int kBT = 512;  // threads per CTA of the batched kernels
+constexpr int kBWarps = kBT / 32;
+
+__device__ __forceinline__ double bsum(double v, double* sh) {
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < kBWarps; ++w) t += sh[w];
+    sh[kBWarps] = t;
+  }
+  __syncthreads();
+  return sh[kBWarps];
+}
+
+// K sums at once (fixed order), result broadcast to every thread.
+template <int K>
+__device__ __forceinline__ void bsums(double (&v)[K], double* sh) {
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+  }
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) sh[q * kBWarps + warp] = v[q];
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double t = 0.0;
+    for (int w = 0; w < kBWarps; ++w) t += sh[threadIdx.x * kBWarps + w];
+    sh[K * kBWarps + threadIdx.x] = t;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < K; ++q) v[q] = sh[K * kBWarps + q];
+  __syncthreads();
+}
+
+__device__ __forceinline__ double bmax(double v, double* sh) {
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = sh[0];
+    for (int w = 1; w < kBWarps; ++w) t = fmax(t, sh[w]);
+    sh[kBWarps] = t;
+  }
+  __syncthreads();
+  return sh[kBWarps];
+}
+
+// For every row r < rows of a CSR (ptr, idx, val): s = sum_k prod(val_k, idx_k) (or max), then
+// f(r, s). Thread per row; rows longer than 32 nonzeros by their warp.
+template <bool MAXRED, typename T, typename Prod, typename F>
+__device__ __forceinline__ void block_rows(int rows, const int* __restrict__ ptr,
+                                           const int* __restrict__ idx, const T* __restrict__ val,
+                                           const Prod& prod, F& f) {
+  const int lane = threadIdx.x & 31;
+  for (int base = 0; base < rows; base += kBT) {
+    const int r = base + threadIdx.x;
+    const bool valid = r < rows;
+    int b = 0, e = 0;
+    if (valid) {
+      b = ptr[r];
+      e = ptr[r + 1];
+    }
+    const bool shortrow = valid && e - b <= 32;
+    if (shortrow) {
+      double s = 0.0;
+      for (int q = b; q < e; ++q) {
+        const double p = prod(val[q], idx[q]);
+        s = MAXRED ? fmax(s, p) : s + p;
+      }
+      f(r, s);
+    }
+    unsigned pending = __ballot_sync(0xffffffffu, valid && !shortrow);
+    while (pending != 0u) {
+      const int src = __ffs(pending) - 1;
+      pending &= pending - 1u;
+      const int rb = __shfl_sync(0xffffffffu, b, src);
+      const int re = __shfl_sync(0xffffffffu, e, src);
+      double s = 0.0;
+      for (int q = rb + lane; q < re; q += 32) {
+        const double p = prod(val[q], idx[q]);
+        s = MAXRED ? fmax(s, p) : s + p;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double t = __shfl_down_sync(0xffffffffu, s, o);
+        s = MAXRED ? fmax(s, t) : s + t;
+      }
+      if (lane == 0) f(base + (threadIdx.x & ~31) + src, s);
+    }
+  }
+}
+
+__device__ __forceinline__ double lam_of(double g, double lo, double up) {
+  const bool hl = lo > -INFINITY;
+  const bool hu = up < INFINITY;
+  return hl && hu ? g : hl ? fmax(g, 0.0) : hu ? fmin(g, 0.0) : 0.0;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+// Setup: one CTA per matrix.
+__global__ void __launch_bounds__(kBT) batch_setup_kernel(BatchView b) {
+  __shared__ double sh[32 * (kBWarps + 1)];
+  const int g = blockIdx.x;
+  if (g >= b.nmat) return;
+  const int m = b.mat_m[g];
+  const int n = b.mat_n[g];
+  const long long nz = b.mat_nnz_off[g];
+  const long long nnz = b.mat_nnz_off[g + 1] - nz;
+  const int* kp = b.k_ptr + b.mat_kptr_off[g];
+  const int* ki = b.k_idx + nz;
+  double* kv = b.k_val + nz;
+  const double* kv0 = b.k_val0 + nz;
+  const int* tp = b.t_ptr + b.mat_tptr_off[g];
+  const int* ti = b.t_idx + nz;
+  double* tv = b.t_val + nz;
+  const double* tv0 = b.t_val0 + nz;
+  double* cs = b.cs + b.mat_col_off[g];
+  double* rs = b.rs + b.mat_row_off[g];
+  double* cn = b.cn + b.mat_col_off[g];
+  double* rn = b.rn + b.mat_row_off[g];
+  double* pu = b.pu + b.mat_row_off[g];
+  double* pv = b.pv + b.mat_col_off[g];
+  MatInfo* info = b.info + g;
+  for (long long k = threadIdx.x; k < nnz; k += kBT) {
+    kv[k] = kv0[k];
+    tv[k] = tv0[k];
+  }
+  for (int j = threadIdx.x; j < n; j += kBT) cs[j] = 1.0;
+  for (int i = threadIdx.x; i < m; i += kBT) rs[i] = 1.0;
+  __syncthreads();
+  // Relative-residual scales of the original matrix (pdlp.cpp:377-394).
+  double amc = 0.0, amr = 0.0;
+  if (m > 0) {
+    struct Sq {
+      __device__ double operator()(double a, int) const { return a * a; }
+    } sq;
+    double loc = 0.0;
+    auto colmax = [&](int, double s) { loc = fmax(loc, sqrt(s)); };
+    block_rows<false>(n, tp, ti, tv, sq, colmax);
+    amc = bmax(loc, sh);
+    loc = 0.0;
+    auto rowmax = [&](int, double s) { loc = fmax(loc, sqrt(s)); };
+    block_rows<false>(m, kp, ki, kv, sq, rowmax);
+    amr = bmax(loc, sh);
+  }
+  // Preconditioning.
+  if (m > 0 && n > 0) {
+    if (b.algorithm == 1) {
+      for (int pass = 0; pass < 11; ++pass) {
+        const bool ruiz = pass < 10;
+        struct Abs {
+          const double* o;
+          __device__ double operator()(double a, int j) const { return fabs(a) * o[j]; }
+        };
+        Abs pc{rs};
+        Abs pr{cs};
+        if (ruiz) {
+          auto fc = [&](int j, double s) { cn[j] = s * cs[j]; };
+          block_rows<true>(n, tp, ti, tv, pc, fc);
+          auto fr = [&](int i, double s) { rn[i] = s * rs[i]; };
+          block_rows<true>(m, kp, ki, kv, pr, fr);
+        } else {
+          auto fc = [&](int j, double s) { cn[j] = s * cs[j]; };
+          block_rows<false>(n, tp, ti, tv, pc, fc);
+          auto fr = [&](int i, double s) { rn[i] = s * rs[i]; };
+          block_rows<false>(m, kp, ki, kv, pr, fr);
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += kBT) {
+          if (cn[j] > 0.0) cs[j] = cs[j] / sqrt(cn[j]);
+        }
+        for (int i = threadIdx.x; i < m; i += kBT) {
+          if (rn[i] > 0.0) rs[i] = rs[i] / sqrt(rn[i]);
+        }
+        __syncthreads();
+      }
+    } else {
+      // The reference's L2 Ruiz (pdlp.cpp:109-187).
+      for (int pass = 0; pass < 10; ++pass) {
+        struct Sq2 {
+          const double* o;
+          __device__ double operator()(double a, int j) const {
+            const double v = a * o[j];
+            return v * v;
+          }
+        };
+        Sq2 pc{rs};
+        Sq2 pr{cs};
+        auto fc = [&](int j, double s) { cn[j] = sqrt(s) * cs[j]; };
+        block_rows<false>(n, tp, ti, tv, pc, fc);
+        auto fr = [&](int i, double s) { rn[i] = sqrt(s) * rs[i]; };
+        block_rows<false>(m, kp, ki, kv, pr, fr);
+        __syncthreads();
+        double changed = 0.0;
+        for (int k = threadIdx.x; k < n + m; k += kBT) {
+          double* sc = k < n ? cs + k : rs + (k - n);
+          const double nv = k < n ? cn[k] : rn[k - n];
+          if (nv > 0) {
+            const double old = *sc;
+            double s = old / nv;
+            s = fmax(1e-8, fmin(1e8, s));
+            if (fabs(s - old) / fmax(fabs(old), 1.0) > 0.1) changed = 1.0;
+            *sc = s;
+          }
+        }
+        if (bmax(changed, sh) == 0.0) break;
+      }
+    }
+  }
+  __syncthreads();
+  // A_eq in place: K entries (a rs_i) cs_j, K' entries (a cs_j) rs_i.
+  for (int i = threadIdx.x; i < m; i += kBT) {
+    for (int q = kp[i]; q < kp[i + 1]; ++q) kv[q] = kv[q] * rs[i] * cs[ki[q]];
+  }
+  for (int j = threadIdx.x; j < n; j += kBT) {
+    for (int q = tp[j]; q < tp[j + 1]; ++q) tv[q] = tv[q] * cs[j] * rs[ti[q]];
+  }
+  __syncthreads();
+  // Power iteration (pdlp.cpp:36-103).
+  double L = 1.0;
+  if (m > 0) {
+    for (int i = threadIdx.x; i < m; i += kBT) pu[i] = b.power_start[i];
+    __syncthreads();
+    double ss = 0.0;
+    for (int i = threadIdx.x; i < m; i += kBT) ss += pu[i] * pu[i];
+    double un = sqrt(bsum(ss, sh));
+    for (int i = threadIdx.x; i < m; i += kBT) pu[i] = pu[i] / un;
+    __syncthreads();
+    double sigma = 0.0;
+    bool zero = false;
+    struct G {
+      const double* x;
+      __device__ double operator()(double a, int j) const { return a * x[j]; }
+    };
+    for (int it = 0; it < 20 && !zero; ++it) {
+      double acc = 0.0;
+      G gu{pu};
+      auto fv = [&](int j, double s) { pv[j] = s; acc += s * s; };
+      block_rows<false>(n, tp, ti, tv, gu, fv);
+      const double vn = sqrt(bsum(acc, sh));
+      if (vn == 0.0) {
+        zero = true;
+        break;
+      }
+      acc = 0.0;
+      G gv{pv};
+      auto fu = [&](int i, double s) { pu[i] = s; acc += s * s; };
+      block_rows<false>(m, kp, ki, kv, gv, fu);
+      un = sqrt(bsum(acc, sh));
+      if (un == 0.0) {
+        zero = true;
+        break;
+      }
+      sigma = un / vn;
+      for (int i = threadIdx.x; i < m; i += kBT) pu[i] = pu[i] / un;
+      __syncthreads();
+    }
+    if (!zero) {
+      const double la = sigma * 1.01;
+      L = sqrt(la * la + 1.0);
+    }
+  }
+  if (threadIdx.x == 0) {
+    info->eta = 0.99 / L;
+    info->a_norm_max_col = amc;
+    info->at_norm_max_row = amr;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Solve: persistent CTAs, one instance at a time.
+
+namespace {
+
+struct Meas {
+  double rp, rd, rg, pobj, dobj;
+};
+
+__device__ __forceinline__ Meas finish7(const double* s, double amc, double amr, double cnorm,
+                                        int m) {
+  Meas r;
+  const double ps = 1.0 + amc * sqrt(s[4]) + sqrt(s[5]);
+  const double ds = 1.0 + amr * sqrt(s[6]) + cnorm;
+  const double gs = 1.0 + fabs(s[2]) + fabs(s[3]);
+  r.rp = m > 0 ? sqrt(s[0]) / ps : 0.0;
+  r.rd = m > 0 ? sqrt(s[1]) / ds : 0.0;
+  r.rg = (s[2] - s[3]) / gs;
+  r.pobj = s[2];
+  r.dobj = s[3];
+  return r;
+}
+
+__device__ __forceinline__ double kkt_w(double w, const Meas& e) {
+  return sqrt(w * w * e.rp * e.rp + e.rd * e.rd / (w * w) + e.rg * e.rg);
+}
+
+template <typename T>
+__device__ void solve_instance(const BatchView& b, int inst, double* sh) {
+  const int g = b.inst_mat[inst];
+  const int m = b.mat_m[g];
+  const int n = b.mat_n[g];
+  const int nt = n + m;
+  const long long nz = b.mat_nnz_off[g];
+  const int* kp = b.k_ptr + b.mat_kptr_off[g];
+  const int* ki = b.k_idx + nz;
+  const int* tp = b.t_ptr + b.mat_tptr_off[g];
+  const int* ti = b.t_idx + nz;
+  const T* kv = reinterpret_cast<const T*>(b.fp32 ? static_cast<const void*>(b.k_val32 + nz)
+                                                  : static_cast<const void*>(b.k_val + nz));
+  const T* tv = reinterpret_cast<const T*>(b.fp32 ? static_cast<const void*>(b.t_val32 + nz)
+                                                  : static_cast<const void*>(b.t_val + nz));
+  const double* cs = b.cs + b.mat_col_off[g];
+  const double* rs = b.rs + b.mat_row_off[g];
+  const MatInfo mi = b.info[g];
+  const long long vo = b.vec_off[inst];
+  const long long yo = b.row_off[inst];
+  const double* cost0 = b.cost + vo;
+  const double* lo0 = b.lower + vo;
+  const double* up0 = b.upper + vo;
+  T* st = reinterpret_cast<T*>(b.state) + b.state_off[inst];
+  // Per-instance state (storage type T): V0 V1 Vbar Verg Vrst c l u (nt each), Y0 Y1 Yerg Yrst
+  // (m each).
+  T* V[2] = {st, st + nt};
+  T* Vbar = st + 2 * nt;
+  T* Verg = st + 3 * nt;
+  T* Vrst = st + 4 * nt;
+  T* ce = st + 5 * nt;
+  T* le = st + 6 * nt;
+  T* ue = st + 7 * nt;
+  T* Y[2] = {st + 8 * nt, st + 8 * nt + m};
+  T* Yerg = st + 8 * nt + 2 * m;
+  T* Yrst = st + 8 * nt + 3 * m;
+  // Scaled problem, zero iterates, ||c||.
+  double cc = 0.0, c2 = 0.0, b2 = 0.0;
+  for (int k = threadIdx.x; k < nt; k += kBT) {
+    double c, l, u;
+    if (k < n) {
+      c = cost0[k] * cs[k];
+      l = lo0[k] / cs[k];
+      u = up0[k] / cs[k];
+      c2 += c * c;
+    } else {
+      const double r = rs[k - n];
+      c = cost0[k] * r;
+      l = lo0[k] * r;
+      u = up0[k] * r;
+      const double bb = fmax(isfinite(l) ? fabs(l) : 0.0, isfinite(u) ? fabs(u) : 0.0);
+      b2 += bb * bb;
+    }
+    ce[k] = static_cast<T>(c);
+    le[k] = static_cast<T>(l);
+    ue[k] = static_cast<T>(u);
+    cc += cost0[k] * cost0[k];
+    V[0][k] = V[1][k] = Vbar[k] = Verg[k] = Vrst[k] = T(0);
+    if (k < m) Y[0][k] = Y[1][k] = Yerg[k] = Yrst[k] = T(0);
+  }
+  double nrm[3] = {cc, c2, b2};
+  bsums<3>(nrm, sh);
+  const double c_norm = sqrt(nrm[0]);
+  double omega = 1.0;
+  if (b.algorithm == 1) {
+    const double cn = sqrt(nrm[1]), bn = sqrt(nrm[2]);
+    omega = (cn > 1e-10 && bn > 1e-10) ? cn / bn : 1.0;
+  }
+  const double eta = mi.eta;
+  double tau = eta / omega, sigma = eta * omega;
+  long long max_iter = b.max_iter;
+  if (max_iter <= 0) {
+    max_iter = 10000LL * nt / 10;
+    if (max_iter < 10000LL) max_iter = 10000LL;
+    if (max_iter > 1000000LL) max_iter = 1000000LL;
+  }
+  double kar = INFINITY, kprev = INFINITY;
+  long long t = 0, k_since = 0, restarts = 0;
+  int status = kIterationLimit;
+  int result_avg = 0;
+  Meas final_meas{0, 0, 0, 0, 0};
+  __syncthreads();
+  while (t < max_iter) {
+    const int p = static_cast<int>(t & 1);
+    const double alpha = 1.0 / static_cast<double>(k_since + 1);
+    const T ta = static_cast<T>(alpha), tb = static_cast<T>(1.0 - alpha);
+    const T tsig = static_cast<T>(sigma), ttau = static_cast<T>(tau);
+    // Dual step (rows of A_eq) with the logicals' primal update.
+    {
+      struct G {
+        const T* x;
+        __device__ double operator()(T a, int j) const {
+          return static_cast<double>(a) * static_cast<double>(x[j]);
+        }
+      } gx{Vbar};
+      const T* yv = Y[p];
+      T* yn = Y[p ^ 1];
+      const T* vr = V[p] + n;
+      T* vrn = V[p ^ 1] + n;
+      T* vbr = Vbar + n;
+      auto f = [&](int i, double s) {
+        const T res = static_cast<T>(s) - vbr[i];
+        const T ynew = yv[i] + tsig * res;
+        yn[i] = ynew;
+        const T r = vr[i];
+        T rn = r - ttau * (ce[n + i] - ynew);
+        rn = fmin(fmax(rn, le[n + i]), ue[n + i]);
+        vrn[i] = rn;
+        vbr[i] = rn + (rn - r);
+        Yerg[i] = tb * Yerg[i] + ta * ynew;
+        Verg[n + i] = tb * Verg[n + i] + ta * rn;
+      };
+      block_rows<false>(m, kp, ki, kv, gx, f);
+    }
+    __syncthreads();
+    // Primal step (rows of A_eq').
+    {
+      struct G {
+        const T* y;
+        __device__ double operator()(T a, int i) const {
+          return static_cast<double>(a) * static_cast<double>(y[i]);
+        }
+      } gy{Y[p ^ 1]};
+      const T* x = V[p];
+      T* xn = V[p ^ 1];
+      auto f = [&](int j, double s) {
+        const T xo = x[j];
+        T v = xo - ttau * (ce[j] + static_cast<T>(s));
+        v = fmin(fmax(v, le[j]), ue[j]);
+        xn[j] = v;
+        Vbar[j] = v + (v - xo);
+        Verg[j] = tb * Verg[j] + ta * v;
+      };
+      block_rows<false>(n, tp, ti, tv, gy, f);
+    }
+    __syncthreads();
+    ++t;
+    ++k_since;
+    if (t % 64 != 0 && t != max_iter) continue;
+    // Evaluation of the current and the average iterate (pdlp.cpp:411-488), original space.
+    const int cur = static_cast<int>(t & 1);
+    double a[18];
+#pragma unroll
+    for (int q = 0; q < 18; ++q) a[q] = 0.0;
+    {
+      struct G2 {
+        const T* x;
+        __device__ double operator()(T v, int j) const {
+          return static_cast<double>(v) * static_cast<double>(x[j]);
+        }
+      };
+      for (int w = 0; w < 2; ++w) {
+        const T* vv = w == 0 ? V[cur] : Verg;
+        const T* yy = w == 0 ? Y[cur] : Yerg;
+        G2 gx{vv};
+        auto fr = [&](int i, double s) {
+          const double r_s = rs[i];
+          const double value = static_cast<double>(vv[n + i]) / r_s;
+          const double yo2 = static_cast<double>(yy[i]) * r_s;
+          const double c = cost0[n + i];
+          const double g2 = c - yo2;
+          const double e = s / r_s - value;
+          a[w * 7 + 0] += e * e;
+          a[w * 7 + 5] += value * value;
+          a[w * 7 + 6] += yo2 * yo2;
+          a[w * 7 + 2] += c * value;
+          const double lam = lam_of(g2, lo0[n + i], up0[n + i]);
+          a[w * 7 + 1] += (g2 - lam) * (g2 - lam);
+          if (lam > 0.0) a[w * 7 + 3] += lam * lo0[n + i];
+          if (lam < 0.0) a[w * 7 + 3] += lam * up0[n + i];
+          const double dv = static_cast<double>(vv[n + i]) - static_cast<double>(Vrst[n + i]);
+          const double dy = static_cast<double>(yy[i]) - static_cast<double>(Yrst[i]);
+          a[14 + 2 * w] += dv * dv;
+          a[15 + 2 * w] += dy * dy;
+        };
+        block_rows<false>(m, kp, ki, kv, gx, fr);
+        G2 gy{yy};
+        auto fc = [&](int j, double s) {
+          const double c_s = cs[j];
+          const double value = static_cast<double>(vv[j]) * c_s;
+          const double c = cost0[j];
+          const double g2 = c + (m > 0 ? s / c_s : 0.0);
+          a[w * 7 + 4] += value * value;
+          a[w * 7 + 2] += c * value;
+          const double lam = lam_of(g2, lo0[j], up0[j]);
+          a[w * 7 + 1] += (g2 - lam) * (g2 - lam);
+          if (lam > 0.0) a[w * 7 + 3] += lam * lo0[j];
+          if (lam < 0.0) a[w * 7 + 3] += lam * up0[j];
+          const double dv = static_cast<double>(vv[j]) - static_cast<double>(Vrst[j]);
+          a[14 + 2 * w] += dv * dv;
+        };
+        block_rows<false>(n, tp, ti, tv, gy, fc);
+      }
+    }
+    bsums<18>(a, sh);
+    const Meas mc = finish7(a, mi.a_norm_max_col, mi.at_norm_max_row, c_norm, m);
+    const Meas ma = finish7(a + 7, mi.a_norm_max_col, mi.at_norm_max_row, c_norm, m);
+    const double tol = b.tol;
+    if (mc.rp < tol && mc.rd < tol && fabs(mc.rg) < tol) {
+      status = kOptimal;
+      final_meas = mc;
+      break;
+    }
+    if (ma.rp < tol && ma.rd < tol && fabs(ma.rg) < tol) {
+      status = kOptimal;
+      result_avg = 1;
+      final_meas = ma;
+      break;
+    }
+    final_meas = mc;
+    // Restart (pdlp.cpp:1069-1131).
+    const double kc = kkt_w(omega, mc), ka = kkt_w(omega, ma);
+    const bool to_avg = ka < kc;
+    const double cand = fmin(kc, ka);
+    if (!(kar < INFINITY)) kar = cand;
+    const bool restart = cand <= 0.2 * kar || (cand <= 0.8 * kar && cand > kprev) ||
+                         static_cast<double>(k_since) >= 0.36 * static_cast<double>(t);
+    kprev = cand;
+    if (restart) {
+      const double dx = sqrt(a[to_avg ? 16 : 14]);
+      const double dy = sqrt(a[to_avg ? 17 : 15]);
+      if (dx > 1e-10 && dy > 1e-10) {
+        omega = exp(0.5 * log(dy / dx) + 0.5 * log(omega));
+        tau = eta / omega;
+        sigma = eta * omega;
+      }
+      const T* vc = to_avg ? Verg : V[cur];
+      const T* yc = to_avg ? Yerg : Y[cur];
+      for (int k = threadIdx.x; k < nt; k += kBT) {
+        const T v = vc[k];
+        Vrst[k] = v;
+        V[0][k] = v;
+        V[1][k] = v;
+        Vbar[k] = v;
+        if (k < m) {
+          const T y = yc[k];
+          Yrst[k] = y;
+          Y[0][k] = y;
+          Y[1][k] = y;
+        }
+      }
+      __syncthreads();
+      k_since = 0;
+      kar = cand;
+      kprev = INFINITY;
+      ++restarts;
+    }
+    const unsigned long long deadline = *b.deadline;
+    if (deadline != 0ull) {
+      unsigned long long now;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+      if (now > deadline) {
+        status = kTimeLimit;
+        break;
+      }
+    }
+  }
+  // Answer in the LpProblem's space.
+  const int cur = static_cast<int>(t & 1);
+  const T* vv = result_avg ? Verg : V[cur];
+  const T* yy = result_avg ? Yerg : Y[cur];
+  double* xo = b.x_out + vo;
+  double* yo2 = b.y_out + yo;
+  for (int k = threadIdx.x; k < nt; k += kBT) {
+    xo[k] = k < n ? static_cast<double>(vv[k]) * cs[k] : static_cast<double>(vv[k]) / rs[k - n];
+    if (k < m) yo2[k] = static_cast<double>(yy[k]) * rs[k];
+  }
+  if (threadIdx.x == 0) {
+    InstResult& r = b.results[inst];
+    r.status = status;
+    r.iterations = status == kIterationLimit ? max_iter : t;
+    r.rel_primal = final_meas.rp;
+    r.rel_dual = final_meas.rd;
+    r.rel_gap = final_meas.rg;
+    r.primal_obj = final_meas.pobj;
+    r.dual_obj = final_meas.dobj;
+    r.restarts = restarts;
+  }
+  __syncthreads();
+}
+
+}  // namespace
+
+template <typename T>
+__global__ void __launch_bounds__(kBT) batch_solve_kernel(BatchView b) {
+  __shared__ double sh[32 * (kBWarps + 1)];
+  __shared__ int next;
+  for (;;) {
+    if (threadIdx.x == 0) next = static_cast<int>(atomicAdd(b.queue, 1u));
+    __syncthreads();
+    const int q = next;
+    __syncthreads();
+    if (q >= b.count) break;
+    solve_instance<T>(b, b.order[q], sh);
+  }
+}
+
+__global__ void to_fp32_kernel(const double* a, float* o, long long count) {
+  for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < count;
+       k += static_cast<long long>(gridDim.x) * blockDim.x) {
+    o[k] = static_cast<float>(a[k]);
+  }
+}
+
+__global__ void batch_deadline_kernel(unsigned long long* word, unsigned long long budget_ns) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned long long now;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+  *word = budget_ns == 0ull ? 0ull : now + budget_ns;
+}
+
+void launch_batch(const BatchView& b, int solve_grid, unsigned long long budget_ns,
+                  cudaStream_t s) {
+  batch_deadline_kernel<<<1, 32, 0, s>>>(const_cast<unsigned long long*>(b.deadline), budget_ns);
+  cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
+  batch_setup_kernel<<<b.nmat, kBT, 0, s>>>(b);
+  if (b.fp32) {
+    const long long nnz = b.total_nnz;
+    const int g = static_cast<int>(nnz / 256 + 1 < 4096 ? nnz / 256 + 1 : 4096);
+    to_fp32_kernel<<<g, 256, 0, s>>>(b.k_val, b.k_val32, nnz);
+    to_fp32_kernel<<<g, 256, 0, s>>>(b.t_val, b.t_val32, nnz);
+    batch_solve_kernel<float><<<solve_grid, kBT, 0, s>>>(b);
+  } else {
+    batch_solve_kernel<double><<<solve_grid, kBT, 0, s>>>(b);
+  }
+}
+
+int batch_threads() { return kBT; }
+
+}  // namespace sg

@@ -136,7 +136,7 @@ template <typename T>
 using Acc = T;  // FP64 storage accumulates in FP64, FP32 storage in FP32.
 
 template <typename T>
-__global__ void __launch_bounds__(kBlock) dual_step_kernel(const Ctl* __restrict__ ctl,
+__global__ void __launch_bounds__(kBlock, 6) dual_step_kernel(const Ctl* __restrict__ ctl,
                                                            OpView<T> K, IterView<T> it, int j) {
   if (ctl->done) return;
   const long long t = ctl->t + j;
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(kBlock) dual_step_kernel(const Ctl* __restrict
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kBlock) primal_step_kernel(const Ctl* __restrict__ ctl,
+__global__ void __launch_bounds__(kBlock, 6) primal_step_kernel(const Ctl* __restrict__ ctl,
                                                              OpView<T> Kt, IterView<T> it, int j) {
   if (ctl->done) return;
   const long long t = ctl->t + j;
