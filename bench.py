@@ -42,7 +42,26 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="transport", choices=["transport", "powerlaw", "random"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--profile", action="store_true",
+                    help="one solve of the workload and nothing else (for profilers)")
+    ap.add_argument("--max-iterations", type=int, default=-1,
+                    help="iteration cap of the --profile solve (-1: none)")
     return ap.parse_args()
+
+
+def run_profile(args):
+    """One solve of the workload (no baselines, no JSON): the command profilers wrap."""
+    import samaya_gb300 as sg
+    from samaya_gb300.problem import make_problem
+    model, cfg = workload(args.workload)
+    lp, _ = make_problem(model)
+    mixed = args.precision == "mixed"
+    opts = sg.PdlpOptions(tol=TOL, algorithm=sg.ENHANCED, max_iterations=args.max_iterations,
+                          precision=sg.FP32_REFINED if mixed else sg.FP64)
+    r = sg.solve_pdlp(lp, opts)
+    print(f"{cfg['workload']}: {r.status_name} {r.iterations} iterations "
+          f"{r.device_ms:.1f} ms", flush=True)
+    return 0
 
 
 def workload(name, seed=0):
@@ -201,6 +220,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile:
+        return run_profile(args)
     world, rank, local = dist()
     import numpy as np
     import samaya_gb300 as sg

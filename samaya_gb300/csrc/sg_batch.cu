@@ -95,59 +95,40 @@ __device__ __forceinline__ void block_rows(int rows, const int* __restrict__ ptr
                                            const int* __restrict__ idx, const T* __restrict__ val,
                                            const Prod& prod, F& f) {
   const int lane = threadIdx.x & 31;
-  constexpr int U = 4;  // rows in flight per thread (independent load chains)
-  for (int base = 0; base < rows; base += U * kBT) {
-    int b[U], e[U], len[U];
-    int maxlen = 0;
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int r = base + u * kBT + threadIdx.x;
-      b[u] = 0;
-      e[u] = 0;
-      if (r < rows) {
-        b[u] = ptr[r];
-        e[u] = ptr[r + 1];
-      }
-      len[u] = e[u] - b[u] <= 32 ? e[u] - b[u] : 0;
-      maxlen = len[u] > maxlen ? len[u] : maxlen;
+  for (int base = 0; base < rows; base += kBT) {
+    const int r = base + threadIdx.x;
+    const bool valid = r < rows;
+    int b = 0, e = 0;
+    if (valid) {
+      b = ptr[r];
+      e = ptr[r + 1];
     }
-    double s[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) s[u] = 0.0;
-    for (int t = 0; t < maxlen; ++t) {
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        if (t < len[u]) {
-          const int q = b[u] + t;
-          const double p = prod(val[q], idx[q]);
-          s[u] = MAXRED ? fmax(s[u], p) : s[u] + p;
-        }
+    const bool shortrow = valid && e - b <= 32;
+    if (shortrow) {
+      double s = 0.0;
+      for (int q = b; q < e; ++q) {
+        const double p = prod(val[q], idx[q]);
+        s = MAXRED ? fmax(s, p) : s + p;
       }
+      f(r, s);
     }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int r = base + u * kBT + threadIdx.x;
-      const bool valid = r < rows;
-      const bool shortrow = valid && e[u] - b[u] <= 32;
-      if (shortrow) f(r, s[u]);
-      unsigned pending = __ballot_sync(0xffffffffu, valid && !shortrow);
-      while (pending != 0u) {
-        const int src = __ffs(pending) - 1;
-        pending &= pending - 1u;
-        const int rb = __shfl_sync(0xffffffffu, b[u], src);
-        const int re = __shfl_sync(0xffffffffu, e[u], src);
-        double sl = 0.0;
-        for (int q = rb + lane; q < re; q += 32) {
-          const double p = prod(val[q], idx[q]);
-          sl = MAXRED ? fmax(sl, p) : sl + p;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const double tt = __shfl_down_sync(0xffffffffu, sl, o);
-          sl = MAXRED ? fmax(sl, tt) : sl + tt;
-        }
-        if (lane == 0) f(base + u * kBT + (threadIdx.x & ~31) + src, sl);
+    unsigned pending = __ballot_sync(0xffffffffu, valid && !shortrow);
+    while (pending != 0u) {
+      const int src = __ffs(pending) - 1;
+      pending &= pending - 1u;
+      const int rb = __shfl_sync(0xffffffffu, b, src);
+      const int re = __shfl_sync(0xffffffffu, e, src);
+      double s = 0.0;
+      for (int q = rb + lane; q < re; q += 32) {
+        const double p = prod(val[q], idx[q]);
+        s = MAXRED ? fmax(s, p) : s + p;
       }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double t = __shfl_down_sync(0xffffffffu, s, o);
+        s = MAXRED ? fmax(s, t) : s + t;
+      }
+      if (lane == 0) f(base + (threadIdx.x & ~31) + src, s);
     }
   }
 }
