@@ -48,6 +48,8 @@ struct TileSet {
 };
 
 constexpr int kMaxVec = 2;
+constexpr int kWarpRowMin = 128;             // rows longer than this get a warp (tile kind 2)
+constexpr int kWarpsPerTile = kBlock / 32;   // rows of a kind-2 tile
 
 // Status values (the reference's SimplexStatus, src/lp/simplex.hpp:28-35) plus "running".
 enum : int {

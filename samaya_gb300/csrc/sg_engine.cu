@@ -53,10 +53,31 @@ void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, std::
   out->clear();
   *nlong = 0;
   const int rows = static_cast<int>(ptr.size()) - 1;
-  const int long_len = std::max(64, tile_nnz / 8);
+  // Rows longer than a tile are split into CTA segments (kind 1); rows of more than
+  // kWarpRowMin nonzeros get a warp each, kWarpsPerTile rows per tile (kind 2).
+  const int long_len = std::max(tile_nnz, kWarpRowMin);
   int r = 0;
   while (r < rows) {
     const int len = ptr[r + 1] - ptr[r];
+    if (len > kWarpRowMin && len <= long_len) {
+      Tile t{};
+      t.r0 = r;
+      while (r < rows && r - t.r0 < kWarpsPerTile) {
+        const int l = ptr[r + 1] - ptr[r];
+        if (l <= kWarpRowMin || l > long_len) break;
+        ++r;
+      }
+      t.r1 = r;
+      t.k0 = ptr[t.r0];
+      t.k1 = ptr[r];
+      t.kind = 2;
+      t.team = 32;
+      t.seg = 0;
+      t.nseg = 1;
+      t.lrow = -1;
+      out->push_back(t);
+      continue;
+    }
     if (len > long_len) {
       const int nseg = (len + tile_nnz - 1) / tile_nnz;
       for (int s = 0; s < nseg; ++s) {
@@ -79,7 +100,7 @@ void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, std::
     const int r0 = r;
     while (r < rows && r - r0 < tile_rows) {
       const int l = ptr[r + 1] - ptr[r];
-      if (l > long_len) break;
+      if (l > kWarpRowMin) break;
       if (ptr[r + 1] - ptr[r0] > tile_nnz) break;
       ++r;
     }

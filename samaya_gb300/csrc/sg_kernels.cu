@@ -351,6 +351,168 @@ __global__ void __launch_bounds__(kBlock) eval_cols_kernel(Ctl* ctl, OpView<T> K
                          Kt.ts.nlong);
 }
 
+// The same sums for an FP32 operator, which is always an inner problem already in its own
+// equilibrated space (unit scales) with its own FP32 cost, bounds and right-hand side: FP32
+// products, row sums and terms (GB300's FP64 rate is a small fraction of its FP32 rate, and FP64
+// terms made these kernels arithmetic-bound), FP64 grid totals. Precision ~1e-6 relative is
+// ample for the inner tolerance; the refined point is judged by the FP64 evaluation above.
+
+__device__ __forceinline__ float bound_part32(float g, float lo, float up) {
+  const bool hl = lo > -INFINITY;
+  const bool hu = up < INFINITY;
+  return hl && hu ? g : hl ? fmaxf(g, 0.0f) : hu ? fminf(g, 0.0f) : 0.0f;
+}
+
+struct Gather2f {
+  const float* x0;
+  const float* x1;
+  __device__ __forceinline__ float operator()(int v, float a, int j) const {
+    return a * ldg((v == 0 ? x0 : x1) + j);
+  }
+};
+
+struct EvalRowEpi32 {
+  const float* vr[2];
+  const float* y[2];
+  const float* vr_rst;
+  const float* y_rst;
+  const float* c;  // row parts (n offset applied)
+  const float* l;
+  const float* u;
+  const float* q;
+  float acc[kEvalSums];
+  double* long_terms;
+  __device__ __forceinline__ void terms(int i, const float (&s)[2], float (&a)[kEvalSums]) {
+    const float c_i = c[i];
+    const float lo = l[i];
+    const float up = u[i];
+    const float q_i = q != nullptr ? q[i] : 0.0f;
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+      const float value = vr[w][i];
+      const float yv = y[w][i];
+      const float g = c_i - yv;
+      const float e = s[w] - value - q_i;
+      a[w * 7 + 0] += e * e;
+      a[w * 7 + 5] += value * value;
+      a[w * 7 + 6] += yv * yv;
+      a[w * 7 + 2] += c_i * value;
+      const float lam = bound_part32(g, lo, up);
+      a[w * 7 + 1] += (g - lam) * (g - lam);
+      if (lam > 0.0f) a[w * 7 + 3] += lam * lo;
+      if (lam < 0.0f) a[w * 7 + 3] += lam * up;
+      a[w * 7 + 3] -= yv * q_i;
+      const float dv = value - vr_rst[i];
+      const float dy = yv - y_rst[i];
+      a[14 + 2 * w] += dv * dv;
+      a[15 + 2 * w] += dy * dy;
+    }
+  }
+  __device__ __forceinline__ void row(int i, const float (&s)[2]) { terms(i, s, acc); }
+  __device__ __forceinline__ void long_row(int lrow, int i, const float (&s)[2]) {
+    float a[kEvalSums];
+#pragma unroll
+    for (int q2 = 0; q2 < kEvalSums; ++q2) a[q2] = 0.0f;
+    terms(i, s, a);
+#pragma unroll
+    for (int q2 = 0; q2 < kEvalSums; ++q2) long_terms[lrow * kMaxSums + q2] = a[q2];
+  }
+};
+
+struct EvalColEpi32 {
+  const float* x[2];
+  const float* x_rst;
+  const float* c;
+  const float* l;
+  const float* u;
+  int m;
+  float acc[kEvalSums];
+  double* long_terms;
+  __device__ __forceinline__ void terms(int j, const float (&s)[2], float (&a)[kEvalSums]) {
+    const float c_j = c[j];
+    const float lo = l[j];
+    const float up = u[j];
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+      const float value = x[w][j];
+      const float g = c_j + (m > 0 ? s[w] : 0.0f);
+      a[w * 7 + 4] += value * value;
+      a[w * 7 + 2] += c_j * value;
+      const float lam = bound_part32(g, lo, up);
+      a[w * 7 + 1] += (g - lam) * (g - lam);
+      if (lam > 0.0f) a[w * 7 + 3] += lam * lo;
+      if (lam < 0.0f) a[w * 7 + 3] += lam * up;
+      const float dv = value - x_rst[j];
+      a[14 + 2 * w] += dv * dv;
+    }
+  }
+  __device__ __forceinline__ void row(int j, const float (&s)[2]) { terms(j, s, acc); }
+  __device__ __forceinline__ void long_row(int lrow, int j, const float (&s)[2]) {
+    float a[kEvalSums];
+#pragma unroll
+    for (int q2 = 0; q2 < kEvalSums; ++q2) a[q2] = 0.0f;
+    terms(j, s, a);
+#pragma unroll
+    for (int q2 = 0; q2 < kEvalSums; ++q2) long_terms[lrow * kMaxSums + q2] = a[q2];
+  }
+};
+
+__global__ void __launch_bounds__(kBlock) eval_rows32_kernel(Ctl* ctl, OpView<float> K,
+                                                             IterView<float> it, RedView red,
+                                                             int fixed_parity) {
+  if (fixed_parity < 0 && ctl->done) return;
+  const int cur = eval_parity(ctl, fixed_parity);
+  const int n = it.n;
+  EvalRowEpi32 epi;
+  epi.vr[0] = it.V[cur] + n;
+  epi.vr[1] = it.Verg + n;
+  epi.y[0] = it.Y[cur];
+  epi.y[1] = it.Yerg;
+  epi.vr_rst = it.Vrst + n;
+  epi.y_rst = it.Yrst;
+  epi.c = it.cost + n;
+  epi.l = it.lower + n;
+  epi.u = it.upper + n;
+  epi.q = it.rhs;
+  epi.long_terms = red.long_terms;
+#pragma unroll
+  for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0f;
+  Gather2f g{it.V[cur], it.Verg};
+  run_tiles<float, float, 2>(K.ts, K.ptr, K.idx, K.val, g, epi);
+  double acc[kEvalSums];
+#pragma unroll
+  for (int q = 0; q < kEvalSums; ++q) acc[q] = epi.acc[q];
+  EvalFin fin{ctl->eval_r};
+  grid_reduce<kEvalSums>(acc, red.partial, red.counter, smem_red(), fin, red.long_terms,
+                         K.ts.nlong);
+}
+
+__global__ void __launch_bounds__(kBlock) eval_cols32_kernel(Ctl* ctl, OpView<float> Kt,
+                                                             IterView<float> it, RedView red,
+                                                             int fixed_parity) {
+  if (fixed_parity < 0 && ctl->done) return;
+  const int cur = eval_parity(ctl, fixed_parity);
+  EvalColEpi32 epi;
+  epi.x[0] = it.V[cur];
+  epi.x[1] = it.Verg;
+  epi.x_rst = it.Vrst;
+  epi.c = it.cost;
+  epi.l = it.lower;
+  epi.u = it.upper;
+  epi.m = it.m;
+  epi.long_terms = red.long_terms;
+#pragma unroll
+  for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0f;
+  Gather2f g{it.Y[cur], it.Yerg};
+  run_tiles<float, float, 2>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
+  double acc[kEvalSums];
+#pragma unroll
+  for (int q = 0; q < kEvalSums; ++q) acc[q] = epi.acc[q];
+  EvalFin fin{ctl->eval_c};
+  grid_reduce<kEvalSums>(acc, red.partial, red.counter, smem_red(), fin, red.long_terms,
+                         Kt.ts.nlong);
+}
+
 // ------------------------------------------------------------------------------------------
 // Decisions (pdlp.cpp:493-541, 674-713, 1069-1131), one thread.
 
@@ -1160,10 +1322,19 @@ template <typename T>
 void launch_eval(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
                  const EvalView& ev, const RedView& red, int grid_k, int grid_t,
                  int fixed_parity, cudaStream_t s) {
-  eval_rows_kernel<T><<<grid_k, kBlock, tile_smem_bytes(K.ts, 2, 8), s>>>(ctl, K, it, ev, red,
-                                                                       fixed_parity);
-  eval_cols_kernel<T><<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 2, 8), s>>>(ctl, Kt, it, ev, red,
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32 operators carry their own (equilibrated) data: `ev` is not used.
+    (void)ev;
+    eval_rows32_kernel<<<grid_k, kBlock, tile_smem_bytes(K.ts, 2, 8), s>>>(ctl, K, it, red,
                                                                          fixed_parity);
+    eval_cols32_kernel<<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 2, 8), s>>>(ctl, Kt, it, red,
+                                                                           fixed_parity);
+  } else {
+    eval_rows_kernel<T><<<grid_k, kBlock, tile_smem_bytes(K.ts, 2, 8), s>>>(ctl, K, it, ev, red,
+                                                                         fixed_parity);
+    eval_cols_kernel<T><<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 2, 8), s>>>(ctl, Kt, it, ev,
+                                                                           red, fixed_parity);
+  }
 }
 
 void launch_decide_a(Ctl* ctl, cudaStream_t s) { decide_a_kernel<<<1, 32, 0, s>>>(ctl); }

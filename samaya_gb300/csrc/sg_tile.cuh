@@ -2,11 +2,12 @@
 //
 // The rows of an operator are cut into tiles of bounded nonzeros and rows (host, once). A CTA
 // processes tiles in a persistent loop:
-//   kind 0 (whole rows): `team` lanes per row, chosen from the tile's mean row length (1, 2, 4,
-//     ..., 32). A team reads its row's nonzeros straight from global memory with the lanes
-//     stepping by `team` (consecutive teams cover consecutive rows, so a warp's loads are
-//     coalesced whatever the team size), combines them with a fixed shuffle tree, and its
-//     lane 0 runs epi.row(row, sums) — the fused update of the row's entries.
+//   kind 0 (short rows, at most 128 nonzeros): one thread per row, which sums the row and runs
+//     epi.row(row, sums) — the fused update of the row's entries; a row longer than 32
+//     nonzeros is taken over by its whole warp (ballot queue, fixed shuffle tree).
+//   kind 2 (up to 8 rows of medium length, 128 < nonzeros <= the tile capacity): one warp per
+//     row, 16-byte loads of four nonzeros per lane, a fixed shuffle tree, lane 0 runs
+//     epi.row(row, sums). A CTA per row would spend most of its time on the block tree.
 //   kind 1 (a segment of a row longer than the tile capacity): the CTA sums the segment
 //     (strided, then the fixed block tree) into TileSet::seg_part; the last segment to arrive
 //     (counter) adds the row's segments in tile order and runs epi.long_row.
@@ -159,6 +160,55 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
           }
           if (lane == 0) epi.row(tile.r0 + rr * kBlock + (tid & ~31) + src, s);
         }
+      }
+    } else if (tile.kind == 2) {
+      // Rows of medium length, one warp each: head up to a 4-aligned position, 16-byte loads
+      // of four nonzeros per lane, tail, then the fixed shuffle tree; lane 0 updates the row.
+      const int lane = tid & 31;
+      const int r = tile.r0 + (tid >> 5);
+      if (r < tile.r1) {
+        const int b = ldg(ptr + r);
+        const int e = ldg(ptr + r + 1);
+        ACC s[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) s[v] = ACC(0);
+        const int a0 = min(e, (b + 3) & ~3);
+        const int a1 = max(a0, e & ~3);
+        if (b + lane < a0) {
+          const int q = b + lane;
+          const T a = ldg(val + q);
+          const int j = ldg(idx + q);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
+        }
+#pragma unroll 4
+        for (int q = a0 + 4 * lane; q < a1; q += 128) {
+          T a[4];
+          Vec4<T>::load(val, q, a);
+          const int4 j = __ldg(reinterpret_cast<const int4*>(idx + q));
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            s[v] = combine<MAXRED>(s[v], prod(v, a[0], j.x));
+            s[v] = combine<MAXRED>(s[v], prod(v, a[1], j.y));
+            s[v] = combine<MAXRED>(s[v], prod(v, a[2], j.z));
+            s[v] = combine<MAXRED>(s[v], prod(v, a[3], j.w));
+          }
+        }
+        if (a1 + lane < e) {
+          const int q = a1 + lane;
+          const T a = ldg(val + q);
+          const int j = ldg(idx + q);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            s[v] = combine<MAXRED>(s[v], __shfl_down_sync(0xffffffffu, s[v], o));
+          }
+        }
+        if (lane == 0) epi.row(r, s);
       }
     } else {
       // A segment of a long row: strided sums, then the fixed block tree.
