@@ -47,7 +47,8 @@ enum {
 /* Precision of the iterations. */
 enum {
   SG_PRECISION_FP64 = 0,         /* FP64 storage and arithmetic (the reference's precision) */
-  SG_PRECISION_FP32_REFINED = 1  /* FP32 A and iterates, FP64 residuals + outer refinement */
+  SG_PRECISION_FP32_REFINED = 1, /* FP32 A and iterates, FP64 residuals + outer refinement */
+  SG_PRECISION_FP32_THEN_FP64 = 2 /* FP32 PDLP to inner_tol, then FP64 PDLP from that point */
 };
 
 typedef struct sg_pdlp sg_pdlp;
@@ -60,7 +61,7 @@ typedef struct sg_pdlp_opts {
   double time_limit;         /* seconds; <= 0: none */
   int precision;             /* SG_PRECISION_* */
   int refine_max_rounds;     /* outer refinement rounds of the FP32 path (default 6) */
-  double inner_tol;          /* tolerance of each FP32 inner solve (default 1e-4) */
+  double inner_tol;          /* tolerance of each FP32 solve or FP32 phase (default 1e-4) */
   int verbose;               /* 0 silent */
   int algorithm;             /* SG_ALGORITHM_* (default SG_ALGORITHM_REFERENCE) */
 } sg_pdlp_opts;

@@ -115,6 +115,11 @@ struct Ctl {
   double ir_omega0;
   int no_detect;  // 1: no infeasibility/unboundedness checks (the refinement's inner solves)
   int pad1;
+  // Stall test of the FP32 solves: stop when the better iterate's largest relative residual has
+  // not fallen below 0.8 x its best for stall_limit evaluations (0: off).
+  double stall_best;
+  int stall_evals;
+  int stall_limit;
 };
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {

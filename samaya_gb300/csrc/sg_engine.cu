@@ -259,7 +259,8 @@ int Engine::create(Engine** out, int m, int n, const int64_t* colptr, const int3
   e->n_ = n;
   e->nnz_ = nnz;
   e->opt_ = opt;
-  e->fp32_ = opt.precision == 1;
+  e->fp32_ = opt.precision == 1 || opt.precision == 2;
+  e->switch_ = opt.precision == 2;
   // K' = A^T by rows is the CSC of A; K = A by rows, by a stable counting sort.
   std::vector<int> tptr(static_cast<size_t>(n) + 1);
   for (int j = 0; j <= n; ++j) tptr[j] = static_cast<int>(colptr[j]);
@@ -667,8 +668,9 @@ int Engine::solve(SolveInfo* info, double* x, double* y, double* dual_ray, doubl
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, stream_);
-  int rc = fp32_ ? solve_refined(info, x, y, dual_ray, primal_ray)
-                 : solve_fp64(info, x, y, dual_ray, primal_ray);
+  int rc = switch_ ? solve_switched(info, x, y, dual_ray, primal_ray)
+           : fp32_ ? solve_refined(info, x, y, dual_ray, primal_ray)
+                   : solve_fp64(info, x, y, dual_ray, primal_ray);
   cudaEventRecord(e1, stream_);
   if (cudaEventSynchronize(e1) == cudaSuccess) {
     float ms = 0.0f;
@@ -683,7 +685,6 @@ int Engine::solve(SolveInfo* info, double* x, double* y, double* dual_ray, doubl
 
 int Engine::solve_fp64(SolveInfo* info, double* x, double* y, double* dual_ray,
                        double* primal_ray) {
-  std::string* err = nullptr;
   const double t0 = now_s();
   int rc = setup_device(nullptr);
   if (rc != kOk) return rc;
@@ -696,14 +697,22 @@ int Engine::solve_fp64(SolveInfo* info, double* x, double* y, double* dual_ray,
   info->setup_seconds = t_setup - t0;
   rc = run_loop(deadline, info, chunk_exec_, ctl_, chunk_kernels_, max_iterations());
   if (rc != kOk) return rc;
+  return finish_fp64(info, t0, 0, x, y, dual_ray, primal_ray);
+}
+
+// Status, residuals and the answer of the FP64 loop that has just ended (its control block is
+// in ctl_host_); `iterations_before` iterations of an earlier phase are added to the count.
+int Engine::finish_fp64(SolveInfo* info, double t0, long long iterations_before, double* x,
+                        double* y, double* dual_ray, double* primal_ray) {
+  std::string* err = nullptr;
   const Ctl& c = *ctl_host_;
   if (c.done == 0) {
     // The host's own time limit ended the loop.
     info->status = kTimeLimit;
-    info->iterations = c.t;
+    info->iterations = iterations_before + c.t;
   } else {
     info->status = c.status;
-    info->iterations = c.iterations;
+    info->iterations = iterations_before + c.iterations;
   }
   info->rel_primal = c.res[0];
   info->rel_dual = c.res[1];
@@ -778,26 +787,17 @@ void finish_host(const Ctl& c, const double* s, double* rp, double* rd, double* 
 
 }  // namespace
 
-// FP32 storage and arithmetic in the iterations, FP64 for the point, the residuals, the scale
-// factors and every decision: round 0 solves the problem itself in FP32 to the inner
-// tolerance, every later round an FP32 correction problem built from the FP64 residuals; the
-// FP64 point stops when it meets the reference's relative KKT test at the requested tolerance.
-int Engine::solve_refined(SolveInfo* info, double* x, double* y, double* dual_ray,
-                          double* primal_ray) {
-  (void)dual_ray;
-  (void)primal_ray;
+// Device setup of the FP32 paths: the FP64 setup (equilibration, operator norm), FP32 copies
+// of the equilibrated operators, the FP32 control block (the FP64 one's step size and initial
+// weight, the norms of the equilibrated matrix for its relative residuals), its chunk graph.
+int Engine::prepare_fp32() {
   std::string* err = nullptr;
-  const double t0 = now_s();
   cudaStream_t s = stream_;
   int rc = setup_device(nullptr);
   if (rc != kOk) return rc;
-  const size_t nt = static_cast<size_t>(n_) + m_;
-  const size_t nb = static_cast<size_t>(nnz_);
-  // FP32 copies of the equilibrated operators.
-  launch_convert(K_.val, K_.val32, static_cast<long long>(nb), s);
-  launch_convert(Kt_.val, Kt_.val32, static_cast<long long>(nb), s);
-  // The inner solves' control block: the outer one's step size and initial weight, the norms of
-  // the equilibrated matrix for their relative residuals.
+  const long long nb = nnz_;
+  launch_convert(K_.val, K_.val32, nb, s);
+  launch_convert(Kt_.val, Kt_.val32, nb, s);
   SG_TRY(cudaMemcpyAsync(ctl32_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToDevice, s));
   launch_setup_norms(ctl32_, K_.view64(), Kt_.view64(), it64_.cost, red_view(), grid_k_, grid_t_,
                      s);
@@ -809,13 +809,11 @@ int Engine::solve_refined(SolveInfo* info, double* x, double* y, double* dual_ra
     h.q_norm = 0.0;
     SG_TRY(cudaMemcpy(ctl32_, &h, sizeof(Ctl), cudaMemcpyHostToDevice));
   }
-  rc = capture_chunk32();
-  if (rc != kOk) return rc;
-  // The FP64 point starts at zero.
-  SG_TRY(cudaMemsetAsync(it64_.V[0], 0, nt * sizeof(double), s));
-  SG_TRY(cudaMemsetAsync(it64_.Y[0], 0, static_cast<size_t>(m_) * sizeof(double), s));
-  SG_TRY(cudaMemsetAsync(it64_.Vrst, 0, nt * sizeof(double), s));
-  SG_TRY(cudaMemsetAsync(it64_.Yrst, 0, static_cast<size_t>(m_) * sizeof(double), s));
+  return capture_chunk32();
+}
+
+// The correction-problem view of the refinement kernels over the engine's buffers.
+IrView Engine::ir_view() {
   IrView irv;
   irv.v = it64_.V[0];
   irv.y = it64_.Y[0];
@@ -835,6 +833,79 @@ int Engine::solve_refined(SolveInfo* info, double* x, double* y, double* dual_ra
   irv.red = red_view();
   irv.n = n_;
   irv.m = m_;
+  return irv;
+}
+
+// Precision switch: FP32 PDLP on the equilibrated problem (FP32 operators, iterates and
+// evaluation) to the inner tolerance, then the FP64 PDLP restarted at its answer with its
+// primal weight. The FP32 phase does the bulk of the iterations at half the bytes and with FP32
+// arithmetic; the FP64 phase meets the reference's relative KKT test at the requested
+// tolerance (and runs its infeasibility checks).
+int Engine::solve_switched(SolveInfo* info, double* x, double* y, double* dual_ray,
+                           double* primal_ray) {
+  std::string* err = nullptr;
+  const double t0 = now_s();
+  cudaStream_t s = stream_;
+  int rc = prepare_fp32();
+  if (rc != kOk) return rc;
+  rc = capture_chunk();
+  if (rc != kOk) return rc;
+  const size_t nt = static_cast<size_t>(n_) + m_;
+  // FP32 phase: the correction problem of round 0 is the equilibrated problem itself.
+  const IrView irv = ir_view();
+  launch_ir_scales(ctl32_, 0, 1e4, s);
+  launch_ir_build(ctl32_, irv, 0, s);
+  for (float* p : {it32_.V[0], it32_.V[1], it32_.Vbar, it32_.Verg, it32_.Vrst}) {
+    SG_TRY(cudaMemsetAsync(p, 0, nt * sizeof(float), s));
+  }
+  for (float* p : {it32_.Y[0], it32_.Y[1], it32_.Yerg, it32_.Yrst}) {
+    SG_TRY(cudaMemsetAsync(p, 0, static_cast<size_t>(m_) * sizeof(float), s));
+  }
+  launch_norm_into(cost_in_, static_cast<long long>(nt), red_view(), &ctl32_->c_norm, s);
+  launch_norm_into(rhs_in_, m_, red_view(), &ctl32_->q_norm, s);
+  const long long max_iter = max_iterations();
+  launch_ir_reset(ctl32_, std::max(opt_.inner_tol, opt_.tol), max_iter, kStallEvaluations, s);
+  if (opt_.time_limit > 0) launch_set_deadline(ctl32_, opt_.time_limit - (now_s() - t0), s);
+  const double deadline = opt_.time_limit > 0 ? t0 + opt_.time_limit : 0.0;
+  info->setup_seconds = now_s() - t0;
+  rc = run_loop(deadline, info, chunk32_exec_, ctl32_, chunk32_kernels_, max_iter);
+  if (rc != kOk) return rc;
+  const long long fp32_iters = ctl_host_->t;
+  const long long fp32_restarts = ctl_host_->restarts;
+  const long long fp32_evals = ctl_host_->evaluations;
+  // FP64 phase from the FP32 answer.
+  IterView<float> it32 = iter_view(it32_);
+  launch_switch(ctl_, ctl32_, it32, iter_view(it64_), max_iter - fp32_iters, s);
+  if (opt_.time_limit > 0) launch_set_deadline(ctl_, opt_.time_limit - (now_s() - t0), s);
+  rc = run_loop(deadline, info, chunk_exec_, ctl_, chunk_kernels_, max_iter - fp32_iters);
+  if (rc != kOk) return rc;
+  rc = finish_fp64(info, t0, fp32_iters, x, y, dual_ray, primal_ray);
+  info->restarts += fp32_restarts;
+  info->evaluations += fp32_evals;
+  info->refinement_rounds = 1;
+  return rc;
+}
+
+// FP32 storage and arithmetic in the iterations, FP64 for the point, the residuals, the scale
+// factors and every decision: round 0 solves the problem itself in FP32 to the inner
+// tolerance, every later round an FP32 correction problem built from the FP64 residuals; the
+// FP64 point stops when it meets the reference's relative KKT test at the requested tolerance.
+int Engine::solve_refined(SolveInfo* info, double* x, double* y, double* dual_ray,
+                          double* primal_ray) {
+  (void)dual_ray;
+  (void)primal_ray;
+  std::string* err = nullptr;
+  const double t0 = now_s();
+  cudaStream_t s = stream_;
+  int rc = prepare_fp32();
+  if (rc != kOk) return rc;
+  const size_t nt = static_cast<size_t>(n_) + m_;
+  // The FP64 point starts at zero.
+  SG_TRY(cudaMemsetAsync(it64_.V[0], 0, nt * sizeof(double), s));
+  SG_TRY(cudaMemsetAsync(it64_.Y[0], 0, static_cast<size_t>(m_) * sizeof(double), s));
+  SG_TRY(cudaMemsetAsync(it64_.Vrst, 0, nt * sizeof(double), s));
+  SG_TRY(cudaMemsetAsync(it64_.Yrst, 0, static_cast<size_t>(m_) * sizeof(double), s));
+  const IrView irv = ir_view();
   IterView<float> it32 = iter_view(it32_);
   it32.rhs = it32_.rhs;
   const IterView<double> master = master_view();
@@ -845,10 +916,18 @@ int Engine::solve_refined(SolveInfo* info, double* x, double* y, double* dual_ra
   double rp = INFINITY, rd = INFINITY, rg = INFINITY, pobj = 0.0, dobj = 0.0;
   int status = kIterationLimit;
   int rounds = 0;
+  // A correction round gets at most four times the first round's iterations; a round that
+  // stalls hands the refined point to the FP64 PDLP (below).
+  long long round0_iters = 0;
+  double round0_omega = 1.0;
+  bool stalled = false;
   for (int round = 0; round < opt_.refine_max_rounds; ++round) {
+    long long budget = inner_max - total_iters;
     if (round > 0) {
+      budget = std::min(budget, std::max<long long>(10000, 4 * round0_iters));
       launch_ir_residual(ctl32_, K_.view64(), Kt_.view64(), irv, grid_k_, grid_t_, s);
     }
+    if (budget <= 0) break;
     launch_ir_scales(ctl32_, round, 1e4, s);
     launch_ir_build(ctl32_, irv, round, s);
     for (float* p : {it32_.V[0], it32_.V[1], it32_.Vbar, it32_.Verg, it32_.Vrst}) {
@@ -859,11 +938,17 @@ int Engine::solve_refined(SolveInfo* info, double* x, double* y, double* dual_ra
     }
     launch_norm_into(cost_in_, static_cast<long long>(nt), red_view(), &ctl32_->c_norm, s);
     launch_norm_into(rhs_in_, m_, red_view(), &ctl32_->q_norm, s);
-    launch_ir_reset(ctl32_, opt_.inner_tol, inner_max, s);
+    launch_ir_reset(ctl32_, opt_.inner_tol, budget, kStallEvaluations, s);
     if (opt_.time_limit > 0) launch_set_deadline(ctl32_, opt_.time_limit - (now_s() - t0), s);
-    rc = run_loop(deadline, info, chunk32_exec_, ctl32_, chunk32_kernels_, inner_max);
+    rc = run_loop(deadline, info, chunk32_exec_, ctl32_, chunk32_kernels_, budget);
     if (rc != kOk) return rc;
     total_iters += ctl_host_->t;
+    if (round == 0) {
+      round0_iters = ctl_host_->t;
+      round0_omega = ctl_host_->omega;
+    } else if (ctl_host_->status != kOptimal) {
+      stalled = true;
+    }
     info->restarts += ctl_host_->restarts;
     info->evaluations += ctl_host_->evaluations;
     info->omega = ctl_host_->omega;
@@ -893,6 +978,24 @@ int Engine::solve_refined(SolveInfo* info, double* x, double* y, double* dual_ra
       status = kTimeLimit;
       break;
     }
+    if (stalled) break;
+  }
+  if (status == kIterationLimit && total_iters < inner_max) {
+    // The refinement did not reach the tolerance: the FP64 PDLP continues from the refined
+    // point (restarted there, with the first round's primal weight).
+    rc = capture_chunk();
+    if (rc != kOk) return rc;
+    const long long left = inner_max - total_iters;
+    launch_restart_at_point(ctl_, round0_omega, iter_view(it64_), left, s);
+    if (opt_.time_limit > 0) launch_set_deadline(ctl_, opt_.time_limit - (now_s() - t0), s);
+    rc = run_loop(deadline, info, chunk_exec_, ctl_, chunk_kernels_, left);
+    if (rc != kOk) return rc;
+    const long long restarts = info->restarts, evaluations = info->evaluations;
+    rc = finish_fp64(info, t0, total_iters, x, y, dual_ray, primal_ray);
+    info->restarts += restarts;
+    info->evaluations += evaluations;
+    info->refinement_rounds = rounds;
+    return rc;
   }
   info->status = status;
   info->iterations = total_iters;

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "sg_kernels.cuh"
+#include "sg_refine.cuh"
 
 namespace sg {
 
@@ -29,7 +30,7 @@ struct Options {
   double tol = 1e-8;
   long long max_iterations = -1;
   double time_limit = 0.0;  // seconds; <= 0: none
-  int precision = 0;        // 0 FP64, 1 FP32 storage + FP64 refinement
+  int precision = 0;        // 0 FP64, 1 FP32 storage + FP64 refinement, 2 FP32 then FP64
   int refine_max_rounds = 6;
   double inner_tol = 1e-4;
   int verbose = 0;
@@ -154,6 +155,11 @@ class Engine {
   EvalView inner_eval_view() const;
   int solve_fp64(SolveInfo* info, double* x, double* y, double* dual_ray, double* primal_ray);
   int solve_refined(SolveInfo* info, double* x, double* y, double* dual_ray, double* primal_ray);
+  int solve_switched(SolveInfo* info, double* x, double* y, double* dual_ray, double* primal_ray);
+  int prepare_fp32();
+  IrView ir_view();
+  int finish_fp64(SolveInfo* info, double t0, long long iterations_before, double* x, double* y,
+                  double* dual_ray, double* primal_ray);
   void enqueue_chunk_body();
   int check(cudaError_t e, const char* what);
 
@@ -163,6 +169,7 @@ class Engine {
   int grid_k_ = 1, grid_t_ = 1, grid_step_k_ = 1, grid_step_t_ = 1;
   int sm_count_ = 148;
   bool fp32_ = false;
+  bool switch_ = false;   // FP32 PDLP, then FP64 PDLP from its answer
   DevOp K_, Kt_;
   DevIter<double> it64_;
   DevIter<float> it32_;

@@ -591,6 +591,19 @@ __global__ void decide_a_kernel(Ctl* c) {
     c->t = t_new;
     return;
   }
+  if (c->stall_limit > 0) {
+    const double ec = fmax(fmax(cur.rp, cur.rd), fabs(cur.rg));
+    const double ea = fmax(fmax(avg.rp, avg.rd), fabs(avg.rg));
+    const double e = fmin(ec, ea);
+    if (e < 0.8 * c->stall_best) {
+      c->stall_best = e;
+      c->stall_evals = 0;
+    } else if (++c->stall_evals >= c->stall_limit) {
+      set_answer(c, kIterationLimit, ea < ec ? avg : cur, t_new, ea < ec ? 1 : 0);
+      c->t = t_new;
+      return;
+    }
+  }
   c->detect_pending =
       (!c->no_detect && iter > 1000 && c->m > 0 && ((iter + 1) / kCheckFrequency) % 8 == 0) ? 1
                                                                                               : 0;

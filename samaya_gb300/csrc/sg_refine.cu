@@ -208,8 +208,11 @@ __global__ void ir_update_kernel(const Ctl* __restrict__ c32, IterView<float> it
 }
 
 // Resets the inner solve's control block for a new correction problem.
-__global__ void ir_reset_kernel(Ctl* c, double tol, long long max_iter) {
+__global__ void ir_reset_kernel(Ctl* c, double tol, long long max_iter, int stall_limit) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  c->stall_best = INFINITY;
+  c->stall_evals = 0;
+  c->stall_limit = stall_limit;
   c->t = 0;
   c->k = 0;
   c->max_iter = max_iter;
@@ -225,6 +228,70 @@ __global__ void ir_reset_kernel(Ctl* c, double tol, long long max_iter) {
   c->restarts = 0;
   c->evaluations = 0;
   c->no_detect = 1;
+}
+
+__global__ void switch_vectors_kernel(const Ctl* __restrict__ c32, IterView<float> it32,
+                                      IterView<double> it64) {
+  const int cur = static_cast<int>(c32->t & 1);
+  const bool avg = c32->result_average != 0;
+  const float* w = avg ? it32.Verg : it32.V[cur];
+  const float* z = avg ? it32.Yerg : it32.Y[cur];
+  const int nt = it64.n + it64.m;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
+    const double v = static_cast<double>(w[k]);
+    it64.V[0][k] = v;
+    it64.V[1][k] = v;
+    it64.Vbar[k] = v;
+    it64.Verg[k] = v;
+    it64.Vrst[k] = v;
+    if (k < it64.m) {
+      const double yv = static_cast<double>(z[k]);
+      it64.Y[0][k] = yv;
+      it64.Y[1][k] = yv;
+      it64.Yerg[k] = yv;
+      it64.Yrst[k] = yv;
+    }
+  }
+}
+
+// The FP64 iterates, average and restart point = the FP64 point V[0], Y[0].
+__global__ void point_vectors_kernel(IterView<double> it) {
+  const int nt = it.n + it.m;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
+    const double v = it.V[0][k];
+    it.V[1][k] = v;
+    it.Vbar[k] = v;
+    it.Verg[k] = v;
+    it.Vrst[k] = v;
+    if (k < it.m) {
+      const double yv = it.Y[0][k];
+      it.Y[1][k] = yv;
+      it.Yerg[k] = yv;
+      it.Yrst[k] = yv;
+    }
+  }
+}
+
+// Restarted FP64 control block; the primal weight from c32 when given, else `omega`.
+__global__ void switch_ctl_kernel(Ctl* c, const Ctl* __restrict__ c32, double omega,
+                                  long long max_iter) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  c->t = 0;
+  c->k = 0;
+  c->max_iter = max_iter > 0 ? max_iter : 1;
+  c->kkt_at_restart = INFINITY;
+  c->kkt_previous = INFINITY;
+  c->status = kRunning;
+  c->done = 0;
+  c->result_average = 0;
+  c->restart_pending = 0;
+  c->detect_pending = 0;
+  c->iterations = 0;
+  c->restarts = 0;
+  c->evaluations = 0;
+  c->omega = c32 != nullptr ? c32->omega : omega;
+  c->tau = c->eta / c->omega;
+  c->sigma = c->eta * c->omega;
 }
 
 __global__ void __launch_bounds__(kBlock) norm_into_kernel(const double* x, int len, RedView red,
@@ -272,8 +339,23 @@ void launch_ir_update(const Ctl* c32, const IterView<float>& it, const IrView& v
   ir_update_kernel<<<grid_for(v.n + v.m, 4096), kBlock, 0, s>>>(c32, it, v, round);
 }
 
-void launch_ir_reset(Ctl* c32, double tol, long long max_iter, cudaStream_t s) {
-  ir_reset_kernel<<<1, 32, 0, s>>>(c32, tol, max_iter);
+void launch_ir_reset(Ctl* c32, double tol, long long max_iter, int stall_limit,
+                     cudaStream_t s) {
+  ir_reset_kernel<<<1, 32, 0, s>>>(c32, tol, max_iter, stall_limit);
+}
+
+void launch_switch(Ctl* c64, const Ctl* c32, const IterView<float>& it32,
+                   const IterView<double>& it64, long long max_iter, cudaStream_t s) {
+  switch_vectors_kernel<<<grid_for(static_cast<long long>(it64.n) + it64.m, 4096), kBlock, 0,
+                          s>>>(c32, it32, it64);
+  switch_ctl_kernel<<<1, 32, 0, s>>>(c64, c32, 1.0, max_iter);
+}
+
+void launch_restart_at_point(Ctl* c64, double omega, const IterView<double>& it64,
+                             long long max_iter, cudaStream_t s) {
+  point_vectors_kernel<<<grid_for(static_cast<long long>(it64.n) + it64.m, 4096), kBlock, 0,
+                         s>>>(it64);
+  switch_ctl_kernel<<<1, 32, 0, s>>>(c64, nullptr, omega, max_iter);
 }
 
 void launch_norm_into(const double* x, long long len, const RedView& red, double* out,

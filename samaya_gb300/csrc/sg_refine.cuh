@@ -33,8 +33,19 @@ void launch_ir_scales(Ctl* c32, int round, double growth, cudaStream_t s);
 void launch_ir_build(const Ctl* c32, const IrView& v, int round, cudaStream_t s);
 void launch_ir_update(const Ctl* c32, const IterView<float>& it, const IrView& v, int round,
                       cudaStream_t s);
-void launch_ir_reset(Ctl* c32, double tol, long long max_iter, cudaStream_t s);
+// Restarts the FP32 control block for a solve to `tol` within `max_iter` iterations, with the
+// stall test after `stall_limit` evaluations without progress (0: off).
+void launch_ir_reset(Ctl* c32, double tol, long long max_iter, int stall_limit,
+                     cudaStream_t s);
+constexpr int kStallEvaluations = 64;
 void launch_norm_into(const double* x, long long len, const RedView& red, double* out,
                       cudaStream_t s);
+// Precision switch: the FP64 iterates, average and restart point = the FP32 answer; the FP64
+// control block restarted (t = k = 0, no restart history) with the FP32 solve's primal weight.
+void launch_switch(Ctl* c64, const Ctl* c32, const IterView<float>& it32,
+                   const IterView<double>& it64, long long max_iter, cudaStream_t s);
+// The same from the FP64 point V[0], Y[0] of it64 with primal weight `omega`.
+void launch_restart_at_point(Ctl* c64, double omega, const IterView<double>& it64,
+                             long long max_iter, cudaStream_t s);
 
 }  // namespace sg

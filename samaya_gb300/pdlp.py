@@ -24,6 +24,7 @@ STATUS_NAMES = ["optimal", "infeasible", "unbounded", "iteration_limit", "time_l
 
 FP64 = 0
 FP32_REFINED = 1
+FP32_THEN_FP64 = 2
 REFERENCE = 0
 ENHANCED = 1
 

@@ -147,3 +147,40 @@ def test_random_sparse_lp_objective_vs_dual_simplex(engine):
         ref_obj = float(case.simplex[1])
         obj = model_objective(case, r.x)
         assert abs(obj - ref_obj) <= 1e-4 * (1 + abs(ref_obj)), (obj, ref_obj)
+
+
+@pytest.mark.parametrize("precision", ["FP32_REFINED", "FP32_THEN_FP64"])
+def test_mixed_precision_reaches_fp64_tolerance(engine, precision):
+    """The FP32 paths (refinement; FP32 phase then FP64 phase) on the 200 x 500 random sparse LPs
+    at 1e-8: the FP64 relative KKT of the answer meets 1e-8, and the objective agrees with the
+    reference dual simplex to 1e-6 relative."""
+    for case in load_group("config0_small"):
+        opts = engine.PdlpOptions(tol=1e-8, precision=getattr(engine, precision),
+                                  algorithm=engine.ENHANCED)
+        r = engine.solve_pdlp(case.lp, opts)
+        assert r.status == engine.OPTIMAL, (precision, r.status_name, r.iterations)
+        assert max(r.primal_residual, r.dual_residual, abs(r.gap)) < 1e-8
+        ref_obj = float(case.simplex[1])
+        obj = model_objective(case, r.x)
+        assert abs(obj - ref_obj) <= 1e-6 * (1 + abs(ref_obj)), (obj, ref_obj)
+
+
+def test_transport_mixed_precision_matches_fp64():
+    """A 100 x 200 transportation LP at 1e-8: both FP32 paths reach the FP64 path's objective to
+    1e-7 relative, and repeated runs of each path are bit-identical."""
+    import samaya_gb300 as sg
+    from samaya_gb300.generators import transportation_lp
+    from samaya_gb300.problem import make_problem
+    lp, _ = make_problem(transportation_lp(100, 200, seed=3))
+    base = sg.PdlpOptions(tol=1e-8, algorithm=sg.ENHANCED)
+    r64 = sg.solve_pdlp(lp, base)
+    assert r64.status == sg.OPTIMAL
+    o64 = float(np.dot(lp.cost, r64.x))
+    for prec in (sg.FP32_REFINED, sg.FP32_THEN_FP64):
+        opts = sg.PdlpOptions(tol=1e-8, algorithm=sg.ENHANCED, precision=prec)
+        a = sg.solve_pdlp(lp, opts)
+        b = sg.solve_pdlp(lp, opts)
+        assert a.status == sg.OPTIMAL, (prec, a.status_name)
+        assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)
+        o = float(np.dot(lp.cost, a.x))
+        assert abs(o - o64) <= 1e-7 * (1 + abs(o64)), (prec, o, o64)
