@@ -223,6 +223,21 @@ int sg_batch_solve(sg_batch* handle, sg_batch_result* results, double* x, double
 void sg_batch_destroy(sg_batch* handle);
 const char* sg_batch_last_error(void);
 
+/* ---- Differentiable layer (no counterpart in the reference, whose PDLP has no adjoint).
+ * sg_batch_unroll runs, for every instance of an FP64 batch, `iterations` iterations of the
+ * fixed-step PDHG of the reference's step rule (src/lp/pdlp.cpp:574-641) — tau = sigma =
+ * 0.99 / ||[A_eq -I]||, primal weight 1, no restarts, no averaging — from zero on the
+ * instance's equilibrated problem, saving the state every `checkpoint_every` iterations, and
+ * writes v_K = (x_K, r_K) in the LpProblem's space to v_out (n_i + m_i doubles per instance,
+ * in instance order; may be NULL). The map is piecewise linear in cost and bounds.
+ * sg_batch_unroll_adjoint takes dL/dv_K in the same layout and writes dL/dcost, dL/dlower and
+ * dL/dupper (same layout; the row entries of lower/upper are the row bounds) by the
+ * transposed recurrences, recomputing each checkpointed segment. Returns SG_ERR_NOT_READY
+ * before an unroll, SG_ERR_INVALID_ARGUMENT for an FP32 batch. */
+int sg_batch_unroll(sg_batch* handle, int iterations, int checkpoint_every, double* v_out);
+int sg_batch_unroll_adjoint(sg_batch* handle, const double* grad_v, double* grad_cost,
+                            double* grad_lower, double* grad_upper);
+
 /* ---- Allocation-free SpMV. This entry point has no counterpart in the reference: it is for
  * callers that cannot call cudaMalloc (work recorded into a CUDA graph, a memory pool or budget
  * that forbids driver allocations, device memory handed out by another runtime). It computes

@@ -636,6 +636,274 @@ __global__ void __launch_bounds__(kBT) batch_solve_kernel(BatchView b) {
   }
 }
 
+// ------------------------------------------------------------------------------------------
+// Unrolled PDHG and its adjoint (the differentiable layer). Per instance (one CTA), K iterations
+// of the fixed-step PDHG — tau = sigma = eta, primal weight 1, no restarts and no averaging —
+// from zero on the equilibrated problem (the reference's step, pdlp.cpp:574-641):
+//   y+ = y + sigma (A x_bar - r_bar);  v+ = P(v - tau (c + [A -I]' y+));  v_bar+ = 2 v+ - v
+// with v = (x, r) and P the projection on [l, u]. The state (v, v_bar, y) is saved every
+// `every` iterations. The adjoint recomputes each segment forward from its checkpoint, keeping
+// for every projection which bound it met, then runs the transposed recurrences backwards:
+//   V = v_hat + 2 b_hat;  z_hat = [l < z < u] V;  l_hat += [z <= l] V;  u_hat += [z >= u] V
+//   v_hat' = z_hat - b_hat;  g_hat = -tau z_hat;  c_hat += g_hat
+//   y_hat' = y_hat + [A -I] g_hat;  b_hat' = [A -I]' (sigma y_hat')
+// (the costs, bounds and iterates map to the LpProblem's space by the column and row scales).
+
+namespace {
+
+struct UnrollPtrs {
+  int m, n, nt;
+  const int* kp;
+  const int* ki;
+  const double* kv;
+  const int* tp;
+  const int* ti;
+  const double* tv;
+  const double* cs;
+  const double* rs;
+  double eta;
+  double* st;  // the instance's state storage (8 (n+m) + 4 m doubles)
+  long long vo;
+};
+
+__device__ __forceinline__ UnrollPtrs unroll_ptrs(const BatchView& b, int inst) {
+  UnrollPtrs p;
+  const int g = b.inst_mat[inst];
+  p.m = b.mat_m[g];
+  p.n = b.mat_n[g];
+  p.nt = p.n + p.m;
+  const long long nz = b.mat_nnz_off[g];
+  p.kp = b.k_ptr + b.mat_kptr_off[g];
+  p.ki = b.k_idx + nz;
+  p.kv = b.k_val + nz;
+  p.tp = b.t_ptr + b.mat_tptr_off[g];
+  p.ti = b.t_idx + nz;
+  p.tv = b.t_val + nz;
+  p.cs = b.cs + b.mat_col_off[g];
+  p.rs = b.rs + b.mat_row_off[g];
+  p.eta = b.info[g].eta;
+  p.st = reinterpret_cast<double*>(b.state) + b.state_off[inst];
+  p.vo = b.vec_off[inst];
+  return p;
+}
+
+// The equilibrated cost and bounds of an instance into ce, le, ue.
+__device__ void unroll_problem(const BatchView& b, const UnrollPtrs& p, double* ce, double* le,
+                               double* ue) {
+  const double* c0 = b.cost + p.vo;
+  const double* l0 = b.lower + p.vo;
+  const double* u0 = b.upper + p.vo;
+  for (int k = threadIdx.x; k < p.nt; k += kBT) {
+    if (k < p.n) {
+      ce[k] = c0[k] * p.cs[k];
+      le[k] = l0[k] / p.cs[k];
+      ue[k] = u0[k] / p.cs[k];
+    } else {
+      const double r = p.rs[k - p.n];
+      ce[k] = c0[k] * r;
+      le[k] = l0[k] * r;
+      ue[k] = u0[k] * r;
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned char project(double z, double lo, double up, double* out) {
+  if (z <= lo) {
+    *out = lo;
+    return 1;
+  }
+  if (z >= up) {
+    *out = up;
+    return 2;
+  }
+  *out = z;
+  return 0;
+}
+
+// One fixed-step iteration on (v, vbar, y); `mask` (n+m bytes) records the projections when
+// given.
+__device__ void unroll_step(const UnrollPtrs& p, double* v, double* vbar, double* y,
+                            const double* ce, const double* le, const double* ue,
+                            unsigned char* mask) {
+  const double tau = p.eta, sigma = p.eta;
+  const int n = p.n;
+  struct G {
+    const double* x;
+    __device__ double operator()(double a, int j) const { return a * x[j]; }
+  };
+  {
+    G gx{vbar};
+    auto f = [&](int i, double s) {
+      const double yn = y[i] + sigma * (s - vbar[n + i]);
+      y[i] = yn;
+      const double r = v[n + i];
+      double rn;
+      const unsigned char c = project(r - tau * (ce[n + i] - yn), le[n + i], ue[n + i], &rn);
+      if (mask != nullptr) mask[n + i] = c;
+      v[n + i] = rn;
+      vbar[n + i] = 2.0 * rn - r;
+    };
+    block_rows<false>(p.m, p.kp, p.ki, p.kv, gx, f);
+  }
+  __syncthreads();
+  {
+    G gy{y};
+    auto f = [&](int j, double s) {
+      const double x = v[j];
+      double xn;
+      const unsigned char c = project(x - tau * (ce[j] + s), le[j], ue[j], &xn);
+      if (mask != nullptr) mask[j] = c;
+      v[j] = xn;
+      vbar[j] = 2.0 * xn - x;
+    };
+    block_rows<false>(n, p.tp, p.ti, p.tv, gy, f);
+  }
+  __syncthreads();
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kBT) unroll_forward_kernel(BatchView b, UnrollView u) {
+  for (int inst = blockIdx.x; inst < b.count; inst += gridDim.x) {
+    const UnrollPtrs p = unroll_ptrs(b, inst);
+    const int nt = p.nt, m = p.m, n = p.n;
+    double* v = p.st;
+    double* vbar = p.st + 2 * nt;
+    double* ce = p.st + 5 * nt;
+    double* le = p.st + 6 * nt;
+    double* ue = p.st + 7 * nt;
+    double* y = p.st + 8 * nt;
+    unroll_problem(b, p, ce, le, ue);
+    for (int k = threadIdx.x; k < nt; k += kBT) {
+      v[k] = 0.0;
+      vbar[k] = 0.0;
+      if (k < m) y[k] = 0.0;
+    }
+    __syncthreads();
+    double* ck = u.ck + u.ck_off[inst];
+    const int stride = 2 * nt + m;
+    for (int it = 0; it < u.iterations; ++it) {
+      if (it % u.every == 0) {
+        double* c = ck + static_cast<long long>(it / u.every) * stride;
+        for (int k = threadIdx.x; k < nt; k += kBT) {
+          c[k] = v[k];
+          c[nt + k] = vbar[k];
+          if (k < m) c[2 * nt + k] = y[k];
+        }
+      }
+      unroll_step(p, v, vbar, y, ce, le, ue, nullptr);
+    }
+    double* vo = u.v_out + p.vo;
+    for (int k = threadIdx.x; k < nt; k += kBT) {
+      vo[k] = k < n ? v[k] * p.cs[k] : v[k] / p.rs[k - n];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kBT) unroll_adjoint_kernel(BatchView b, UnrollView u) {
+  for (int inst = blockIdx.x; inst < b.count; inst += gridDim.x) {
+    const UnrollPtrs p = unroll_ptrs(b, inst);
+    const int nt = p.nt, m = p.m, n = p.n;
+    const double tau = p.eta, sigma = p.eta;
+    // Forward working state, the problem, and the adjoint state in the instance's storage.
+    double* v = p.st;
+    double* vh = p.st + nt;
+    double* vbar = p.st + 2 * nt;
+    double* bh = p.st + 3 * nt;
+    double* gh = p.st + 4 * nt;
+    double* ce = p.st + 5 * nt;
+    double* le = p.st + 6 * nt;
+    double* ue = p.st + 7 * nt;
+    double* y = p.st + 8 * nt;
+    double* yh = p.st + 8 * nt + m;
+    double* shat = p.st + 8 * nt + 2 * m;
+    double* gc = u.grad_cost + p.vo;
+    double* gl = u.grad_lower + p.vo;
+    double* gu = u.grad_upper + p.vo;
+    const double* gv = u.grad_v + p.vo;
+    unroll_problem(b, p, ce, le, ue);
+    // Adjoint of v_K in the equilibrated space: x = x_eq cs, r = r_eq / rs.
+    for (int k = threadIdx.x; k < nt; k += kBT) {
+      vh[k] = k < n ? gv[k] * p.cs[k] : gv[k] / p.rs[k - n];
+      bh[k] = 0.0;
+      gc[k] = 0.0;
+      gl[k] = 0.0;
+      gu[k] = 0.0;
+      if (k < m) yh[k] = 0.0;
+    }
+    __syncthreads();
+    const double* ck = u.ck + u.ck_off[inst];
+    unsigned char* mask = u.mask + u.mask_off[inst];
+    const int stride = 2 * nt + m;
+    struct G {
+      const double* x;
+      __device__ double operator()(double a, int j) const { return a * x[j]; }
+    };
+    for (int seg = u.nck - 1; seg >= 0; --seg) {
+      const int k0 = seg * u.every;
+      const int len = min(u.every, u.iterations - k0);
+      const double* c = ck + static_cast<long long>(seg) * stride;
+      for (int k = threadIdx.x; k < nt; k += kBT) {
+        v[k] = c[k];
+        vbar[k] = c[nt + k];
+        if (k < m) y[k] = c[2 * nt + k];
+      }
+      __syncthreads();
+      for (int t = 0; t < len; ++t) {
+        unroll_step(p, v, vbar, y, ce, le, ue, mask + static_cast<long long>(t) * nt);
+      }
+      for (int t = len - 1; t >= 0; --t) {
+        const unsigned char* mk = mask + static_cast<long long>(t) * nt;
+        for (int k = threadIdx.x; k < nt; k += kBT) {
+          const double V = vh[k] + 2.0 * bh[k];
+          const unsigned char code = mk[k];
+          const double zh = code == 0 ? V : 0.0;
+          if (code == 1) gl[k] += V;
+          if (code == 2) gu[k] += V;
+          vh[k] = zh - bh[k];
+          const double g = -tau * zh;
+          gc[k] += g;
+          gh[k] = g;
+        }
+        __syncthreads();
+        {
+          G gg{gh};
+          auto f = [&](int i, double s) {
+            const double yt = yh[i] + (s - gh[n + i]);
+            yh[i] = yt;
+            shat[i] = sigma * yt;
+          };
+          block_rows<false>(m, p.kp, p.ki, p.kv, gg, f);
+        }
+        __syncthreads();
+        {
+          G gs{shat};
+          auto f = [&](int j, double s) { bh[j] = s; };
+          block_rows<false>(n, p.tp, p.ti, p.tv, gs, f);
+          for (int i = threadIdx.x; i < m; i += kBT) bh[n + i] = -shat[i];
+        }
+        __syncthreads();
+      }
+    }
+    // Gradients in the LpProblem's space: c_eq = c s, l_eq = l / cs (columns), l rs (rows).
+    for (int k = threadIdx.x; k < nt; k += kBT) {
+      if (k < n) {
+        const double s = p.cs[k];
+        gc[k] *= s;
+        gl[k] /= s;
+        gu[k] /= s;
+      } else {
+        const double r = p.rs[k - n];
+        gc[k] *= r;
+        gl[k] *= r;
+        gu[k] *= r;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void to_fp32_kernel(const double* a, float* o, long long count) {
   for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < count;
        k += static_cast<long long>(gridDim.x) * blockDim.x) {
@@ -663,6 +931,19 @@ void launch_batch(const BatchView& b, int solve_grid, unsigned long long budget_
     batch_solve_kernel<float><<<solve_grid, kBT, 0, s>>>(b);
   } else {
     batch_solve_kernel<double><<<solve_grid, kBT, 0, s>>>(b);
+  }
+}
+
+void launch_batch_setup(const BatchView& b, cudaStream_t s) {
+  batch_setup_kernel<<<b.nmat, kBT, 0, s>>>(b);
+}
+
+void launch_unroll(const BatchView& b, const UnrollView& u, int adjoint, int grid,
+                   cudaStream_t s) {
+  if (adjoint) {
+    unroll_adjoint_kernel<<<grid, kBT, 0, s>>>(b, u);
+  } else {
+    unroll_forward_kernel<<<grid, kBT, 0, s>>>(b, u);
   }
 }
 

@@ -75,8 +75,27 @@ struct BatchView {
   int fp32;
 };
 
+// Unrolled PDHG of every instance (the differentiable layer's forward and adjoint).
+struct UnrollView {
+  int iterations;            // K
+  int every;                 // checkpoint interval
+  int nck;                   // checkpoints per instance, ceil(K / every)
+  const long long* ck_off;   // per instance: first double of its checkpoints
+  const long long* mask_off; // per instance: first byte of its segment masks
+  double* ck;                // checkpoints: nck x (v: n+m, v_bar: n+m, y: m)
+  unsigned char* mask;       // every x (n+m): 0 inside, 1 at lower, 2 at upper
+  double* v_out;             // v_K in the LpProblem's space (n+m per instance, vec_off)
+  const double* grad_v;      // adjoint of v_K (n+m per instance, vec_off)
+  double* grad_cost;         // outputs (n+m per instance, vec_off)
+  double* grad_lower;
+  double* grad_upper;
+};
+
 void launch_batch(const BatchView& b, int solve_grid, unsigned long long budget_ns,
                   cudaStream_t s);
+void launch_batch_setup(const BatchView& b, cudaStream_t s);
+void launch_unroll(const BatchView& b, const UnrollView& u, int adjoint, int grid,
+                   cudaStream_t s);
 int batch_threads();
 
 class Batch {
@@ -88,6 +107,11 @@ class Batch {
                     const double* upper, double tol, long long max_iter, double time_limit,
                     int precision, int algorithm, std::string* err);
   int solve(InstResult* results, double* x, double* y, double* device_ms, std::string* err);
+  // Differentiable layer: K fixed-step PDHG iterations of every instance (v_K out, n+m per
+  // instance) and the adjoint of v_K with respect to cost, lower and upper.
+  int unroll(int iterations, int every, double* v_out, std::string* err);
+  int unroll_adjoint(const double* grad_v, double* grad_cost, double* grad_lower,
+                     double* grad_upper, std::string* err);
   long long total_vec() const { return total_vec_; }
   long long total_rows() const { return total_rows_; }
 
@@ -99,6 +123,11 @@ class Batch {
   int grid_ = 1;
   long long total_vec_ = 0, total_rows_ = 0;
   double time_limit_ = 0.0;
+  // Unrolled PDHG: the host copies of the per-instance offsets and the device buffers.
+  UnrollView u_{};
+  std::vector<long long> vec_off_host_;
+  std::vector<int> inst_nt_host_, inst_m_host_;
+  bool unrolled_ = false;
   template <typename T>
   int alloc(T** p, size_t count);
 };

@@ -25,6 +25,11 @@ int Batch::alloc(T** p, size_t count) {
 Batch::~Batch() {
   if (stream_) cudaStreamSynchronize(stream_);
   for (void* p : allocs_) cudaFree(p);
+  for (void* p : {static_cast<void*>(u_.ck), static_cast<void*>(u_.mask),
+                  const_cast<void*>(static_cast<const void*>(u_.ck_off)),
+                  const_cast<void*>(static_cast<const void*>(u_.mask_off))}) {
+    if (p) cudaFree(p);
+  }
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -162,6 +167,13 @@ int Batch::create(Batch** out, int nmat, const int* mat_m, const int* mat_n,
   b->time_limit_ = time_limit;
   b->total_vec_ = vec_off[count];
   b->total_rows_ = yrow_off[count];
+  b->vec_off_host_ = vec_off;
+  b->inst_nt_host_.resize(count);
+  b->inst_m_host_.resize(count);
+  for (int i = 0; i < count; ++i) {
+    b->inst_nt_host_[i] = static_cast<int>(vec_off[i + 1] - vec_off[i]);
+    b->inst_m_host_[i] = mat_m[inst_mat[i]];
+  }
   SG_B_CUDA(cudaStreamCreateWithFlags(&b->stream_, cudaStreamNonBlocking));
   BatchView& v = b->v_;
   v.nmat = nmat;
@@ -303,6 +315,124 @@ int Batch::solve(InstResult* results, double* x, double* y, double* device_ms, s
   return SG_OK;
 }
 
+int Batch::unroll(int iterations, int every, double* v_out, std::string* err) {
+  if (v_.fp32) {
+    if (err) *err = "the unrolled PDHG runs in FP64: create the batch with SG_PRECISION_FP64";
+    return SG_ERR_INVALID_ARGUMENT;
+  }
+  if (iterations <= 0 || every <= 0) {
+    if (err) *err = "iterations and checkpoint interval must be positive";
+    return SG_ERR_INVALID_ARGUMENT;
+  }
+  const int count = v_.count;
+  const int nck = (iterations + every - 1) / every;
+  std::vector<long long> ck_off(count + 1, 0), mask_off(count + 1, 0);
+  for (int i = 0; i < count; ++i) {
+    const long long nt = inst_nt_host_[i];
+    ck_off[i + 1] = ck_off[i] + static_cast<long long>(nck) * (2 * nt + inst_m_host_[i]);
+    // Keep every instance's masks 16-byte aligned.
+    mask_off[i + 1] = mask_off[i] + (static_cast<long long>(every) * nt + 15) / 16 * 16;
+  }
+  auto fail = [&](cudaError_t e, const char* what) {
+    if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? SG_ERR_OUT_OF_MEMORY : SG_ERR_CUDA;
+  };
+  if (u_.iterations != iterations || u_.every != every || u_.ck == nullptr) {
+    for (void* p : {static_cast<void*>(u_.ck), static_cast<void*>(u_.mask),
+                    const_cast<void*>(static_cast<const void*>(u_.ck_off)),
+                    const_cast<void*>(static_cast<const void*>(u_.mask_off))}) {
+      if (p) cudaFree(p);
+    }
+    u_.ck = nullptr;
+    u_.mask = nullptr;
+    u_.ck_off = nullptr;
+    u_.mask_off = nullptr;
+    double* ck = nullptr;
+    unsigned char* mask = nullptr;
+    long long *cko = nullptr, *mko = nullptr;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&ck),
+                               std::max<long long>(ck_off[count], 1) * sizeof(double));
+    if (e == cudaSuccess) {
+      e = cudaMalloc(reinterpret_cast<void**>(&mask), std::max<long long>(mask_off[count], 16));
+    }
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&cko), count * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&mko), count * sizeof(long long));
+    if (e == cudaSuccess) {
+      e = cudaMemcpy(cko, ck_off.data(), count * sizeof(long long), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) {
+      e = cudaMemcpy(mko, mask_off.data(), count * sizeof(long long), cudaMemcpyHostToDevice);
+    }
+    u_.ck = ck;
+    u_.mask = mask;
+    u_.ck_off = cko;
+    u_.mask_off = mko;
+    if (e != cudaSuccess) return fail(e, "unroll buffers");
+    if (u_.v_out == nullptr) {
+      for (double** p : {&u_.v_out, &u_.grad_cost, &u_.grad_lower, &u_.grad_upper}) {
+        const int rc = alloc(p, total_vec_);
+        if (rc != SG_OK) {
+          if (err) *err = "unroll buffers: out of memory";
+          return rc;
+        }
+      }
+      double* gv = nullptr;
+      const int rc = alloc(&gv, total_vec_);
+      if (rc != SG_OK) {
+        if (err) *err = "unroll buffers: out of memory";
+        return rc;
+      }
+      u_.grad_v = gv;
+    }
+    u_.iterations = iterations;
+    u_.every = every;
+    u_.nck = nck;
+  }
+  launch_batch_setup(v_, stream_);
+  launch_unroll(v_, u_, 0, grid_, stream_);
+  cudaError_t e = cudaStreamSynchronize(stream_);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(e, "unroll");
+  if (v_out) {
+    e = cudaMemcpy(v_out, u_.v_out, sizeof(double) * total_vec_, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(e, "unroll download");
+  }
+  unrolled_ = true;
+  return SG_OK;
+}
+
+int Batch::unroll_adjoint(const double* grad_v, double* grad_cost, double* grad_lower,
+                          double* grad_upper, std::string* err) {
+  if (!unrolled_) {
+    if (err) *err = "sg_batch_unroll must run before its adjoint";
+    return SG_ERR_NOT_READY;
+  }
+  if (grad_v == nullptr) {
+    if (err) *err = "grad_v is required";
+    return SG_ERR_INVALID_ARGUMENT;
+  }
+  auto fail = [&](cudaError_t e, const char* what) {
+    if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
+    return SG_ERR_CUDA;
+  };
+  cudaError_t e = cudaMemcpy(const_cast<double*>(u_.grad_v), grad_v,
+                             sizeof(double) * total_vec_, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return fail(e, "adjoint upload");
+  launch_batch_setup(v_, stream_);
+  launch_unroll(v_, u_, 1, grid_, stream_);
+  e = cudaStreamSynchronize(stream_);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(e, "adjoint");
+  const std::pair<double*, const double*> outs[3] = {
+      {grad_cost, u_.grad_cost}, {grad_lower, u_.grad_lower}, {grad_upper, u_.grad_upper}};
+  for (const auto& o : outs) {
+    if (o.first == nullptr) continue;
+    e = cudaMemcpy(o.first, o.second, sizeof(double) * total_vec_, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(e, "adjoint download");
+  }
+  return SG_OK;
+}
+
 }  // namespace sg
 
 struct sg_batch {
@@ -366,6 +496,34 @@ void sg_batch_destroy(sg_batch* handle) {
   } catch (...) {
   }
   delete handle;
+}
+
+int sg_batch_unroll(sg_batch* handle, int iterations, int checkpoint_every, double* v_out) {
+  if (handle == nullptr || handle->batch == nullptr) return SG_ERR_INVALID_ARGUMENT;
+  try {
+    std::string why;
+    const int rc = handle->batch->unroll(iterations, checkpoint_every, v_out, &why);
+    if (rc != SG_OK) g_batch_error = why;
+    return rc;
+  } catch (...) {
+    g_batch_error = "unexpected exception";
+    return SG_ERR_INTERNAL;
+  }
+}
+
+int sg_batch_unroll_adjoint(sg_batch* handle, const double* grad_v, double* grad_cost,
+                            double* grad_lower, double* grad_upper) {
+  if (handle == nullptr || handle->batch == nullptr) return SG_ERR_INVALID_ARGUMENT;
+  try {
+    std::string why;
+    const int rc =
+        handle->batch->unroll_adjoint(grad_v, grad_cost, grad_lower, grad_upper, &why);
+    if (rc != SG_OK) g_batch_error = why;
+    return rc;
+  } catch (...) {
+    g_batch_error = "unexpected exception";
+    return SG_ERR_INTERNAL;
+  }
 }
 
 const char* sg_batch_last_error(void) { return g_batch_error.c_str(); }

@@ -143,6 +143,24 @@ def main():
     out["count"] = np.array([1])
     np.savez_compressed(os.path.join(HERE, "config0.npz"), **out)
     print("config0 written")
+    config4()
+
+
+def config4():
+    """The differentiable layer's LPs (500 x 1200 random sparse, seeds 0-7): the reference dual
+    simplex's objective, x and row duals (model space), with the model digest."""
+    out = {}
+    for k in range(8):
+        model = random_sparse_lp(m=500, n=1200, seed=k)
+        ds = ref.dual_simplex(model)
+        ok, _ = ref.verify_optimal(model, ds["x"], ds["y"])
+        out[f"k{k}_digest"] = np.frombuffer(bytes.fromhex(model_digest(model)), dtype=np.uint8)
+        out[f"k{k}_simplex"] = np.array([ds["status"], ds["objective"], ds["iterations"], int(ok)])
+        out[f"k{k}_x"] = ds["x"]
+        out[f"k{k}_y"] = ds["y"]
+    out["count"] = np.array([8])
+    np.savez_compressed(os.path.join(HERE, "config4.npz"), **out)
+    print("config4 written")
 
 
 if __name__ == "__main__":
