@@ -1,16 +1,17 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 PDLP engine: time to 1e-8 relative KKT on the transportation LP
-(1000 supplies x 2000 demands: 3000 equality rows, 2,000,000 columns, 4,000,000 nonzeros), with
-FP32 storage + FP64 iterative refinement (the headline) next to plain FP64 on the same GPU.
+(1000 supplies x 2000 demands: 3000 equality rows, 2,000,000 columns, 4,000,000 nonzeros) with
+mixed precision (FP32 PDLP to a switch tolerance, then FP64 PDLP from its answer: the headline),
+next to FP32 + FP64 iterative refinement and plain FP64 on the same GPU.
 
 One step = one full PDLP solve of the LP, inputs resident in HBM (the problem uploaded once);
 ``e2e`` = the same solve through the public C ABI from pinned host buffers (upload, solve,
-download of x and y). ``roofline`` reports the dominant kernel (the primal step: A'y SpMV fused
-with the projected primal update and the running average) against the measured HBM copy
-bandwidth; ``cpu_baseline`` times the reference's CPU PDLP (the oracle port, 1 core) on a
-bounded run of the same LP.
+download of x and y). ``roofline`` reports the dominant step kernel (both launch once per
+iteration; the slower one) against the measured HBM copy bandwidth; ``cpu_baseline`` times the
+reference's CPU PDLP (the oracle port, 1 core) on a bounded run of the same LP.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py --workload powerlaw|random|batchA|batchB|diff   (the other configurations)
 
 With N > 1 (torchrun) every rank solves its own replica (replicas only; no collective on the
 data path); the time is the max over ranks.
@@ -33,6 +34,10 @@ METRIC = "PDLP time-to-1e-8 KKT (mixed vs FP64 GPU)"
 TOL = 1e-8
 CPU_CAP_S = 20.0
 SWITCH_TOL = 3e-6
+ALGORITHM_NAMES = {
+    "enhanced": "enhanced (inf-norm Ruiz + Pock-Chambolle, primal weight |c|/|b|)",
+    "reference": "reference (samaya's L2 Ruiz, primal weight 1)",
+}
 PRECISION_NAMES = {
     "mixed": "fp32 PDLP to the switch tolerance, then fp64 PDLP from its answer",
     "refined": "fp32 storage + fp64 iterative refinement",
@@ -41,11 +46,12 @@ PRECISION_NAMES = {
 
 
 def solver_options(args, precision):
-    """PdlpOptions of a precision mode (all with the enhanced preconditioning)."""
+    """PdlpOptions of a precision mode with the chosen algorithm."""
     import samaya_gb300 as sg
     prec = {"mixed": sg.FP32_THEN_FP64, "refined": sg.FP32_REFINED, "fp64": sg.FP64}[precision]
     kw = {"inner_tol": args.switch_tol} if precision == "mixed" else {}
-    return sg.PdlpOptions(tol=TOL, algorithm=sg.ENHANCED, precision=prec,
+    alg = sg.REFERENCE if getattr(args, "algorithm", "enhanced") == "reference" else sg.ENHANCED
+    return sg.PdlpOptions(tol=TOL, algorithm=alg, precision=prec,
                           max_iterations=getattr(args, "max_iterations", -1) if args.profile
                           else -1, **kw)
 
@@ -56,7 +62,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="transport", choices=["transport", "powerlaw", "random"])
+    ap.add_argument("--workload", default="transport",
+                    choices=["transport", "powerlaw", "random", "batchA", "batchB", "diff"],
+                    help="transport (the headline), powerlaw, random (2000 x 5000): one LP to "
+                         "1e-8; batchA / batchB: LPs/s of the batched engine against sequential "
+                         "solves; diff: the differentiable layer's forward and backward")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "refined", "fp64"],
                     help="mixed: FP32 PDLP then FP64 PDLP from its answer; refined: FP32 "
                          "iterations with FP64 iterative refinement; fp64: FP64 throughout")
@@ -66,7 +76,15 @@ def parse():
                     help="one solve of the workload and nothing else (for profilers)")
     ap.add_argument("--max-iterations", type=int, default=-1,
                     help="iteration cap of the --profile solve (-1: none)")
-    return ap.parse_args()
+    ap.add_argument("--tol", type=float, default=1e-8,
+                    help="relative KKT tolerance of the single-LP workloads")
+    ap.add_argument("--algorithm", default="enhanced", choices=["enhanced", "reference"],
+                    help="enhanced: inf-norm Ruiz + Pock-Chambolle, primal weight |c|/|b|; "
+                         "reference: samaya's PDLP step for step")
+    args = ap.parse_args()
+    global TOL
+    TOL = args.tol
+    return args
 
 
 def run_profile(args):
@@ -204,9 +222,138 @@ def cpu_reference_run(lp, cap_s=CPU_CAP_S):
     return dt, r.status == o.OPTIMAL, r.iterations, worst
 
 
+def _device_clock_line(line, clk):
+    line["clocks"] = clk.summary()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_batch(args):
+    """LPs/s of one persistent batched launch against sequential single-LP GPU solves (1e-4, the
+    batch's tolerance for node relaxations and screening), FP64 and FP32 storage.
+    batchA: 512 random sparse LPs, m ~ U[100, 5000], n = ceil(m U[2, 3]);
+    batchB: 256 node relaxations of one facility-location LP (100 x 400), 5% of the facility
+    variables fixed to 0 or 1 per node."""
+    import numpy as np
+    import samaya_gb300 as sg
+    from samaya_gb300 import generators as g
+    from samaya_gb300.batch import BatchSolver
+    from samaya_gb300.problem import make_problem
+    tol = 1e-4
+    if args.workload == "batchA":
+        sizes = g.batch_a_sizes(512, seed=0)
+        probs = [make_problem(g.random_sparse_lp(mm, nn, seed=1000 + k))[0]
+                 for k, (mm, nn) in enumerate(sizes)]
+        make = lambda opts: BatchSolver.from_problems(probs, opts)  # noqa: E731
+        singles = probs
+        cfg = {"workload": "512 random sparse LPs, m ~ U[100,5000], n = ceil(m U[2,3])",
+               "instances": 512, "nnz": int(sum(p.nnz for p in probs))}
+    else:
+        model = g.facility_location_lp(100, 400, seed=0)
+        lp, sc = make_problem(model)
+        bounds = []
+        for lo, up in g.facility_node_bounds(model, 100, 256, seed=1):
+            l2 = lp.lower.copy()
+            u2 = lp.upper.copy()
+            l2[:lp.n] = lo / sc.col
+            u2[:lp.n] = up / sc.col
+            bounds.append((l2, u2))
+        make = lambda opts: BatchSolver.shared(lp, bounds, opts)  # noqa: E731
+        singles = [sg.LpProblem(m=lp.m, n=lp.n, colptr=lp.colptr, rowidx=lp.rowidx,
+                                vals=lp.vals, cost=lp.cost, lower=lo, upper=up)
+                   for lo, up in bounds]
+        cfg = {"workload": "256 facility-location node relaxations (100 x 400) sharing A",
+               "instances": 256, "nnz": int(lp.nnz)}
+    out = {}
+    with Clocks(0) as clk:
+        for name, prec in (("fp64", sg.FP64), ("fp32", sg.FP32_REFINED)):
+            for alg_name, alg in (("reference", sg.REFERENCE), ("enhanced", sg.ENHANCED)):
+                s = make(sg.PdlpOptions(tol=tol, precision=prec, algorithm=alg))
+                for _ in range(args.warmup):
+                    s.solve(download=False)
+                times = []
+                for _ in range(args.steps):
+                    r = s.solve(download=False)
+                    times.append(s.device_ms / 1e3)
+                s.close()
+                t = sum(times) / len(times)
+                out[f"{name}_{alg_name}"] = {
+                    "seconds": t, "lps_per_s": len(r) / t,
+                    "optimal": int(sum(x.status == sg.OPTIMAL for x in r)),
+                    "mean_iterations": float(np.mean([x.iterations for x in r])),
+                    "max_iterations": int(max(x.iterations for x in r))}
+        # Sequential single-LP GPU solves (FP64, each algorithm) on a sample of the instances.
+        seq = {}
+        k = 16
+        for alg_name, alg in (("reference", sg.REFERENCE), ("enhanced", sg.ENHANCED)):
+            ms = 0.0
+            for p in singles[:k]:
+                ms += sg.solve_pdlp(p, sg.PdlpOptions(tol=tol, algorithm=alg)).device_ms
+            seq[alg_name] = {"lps_per_s": k / (ms / 1e3), "sample": k}
+    best = max(out.values(), key=lambda v: v["lps_per_s"])
+    line = {"metric": "batched PDLP LPs/s at 1e-4 (one persistent launch)",
+            "value": best["lps_per_s"], "unit": "LPs/s", "higher_is_better": True,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
+            "config": dict(cfg, tol=tol), "batch": out, "sequential_fp64": seq,
+            "speedup_vs_sequential": {a: out[f"fp64_{a}"]["lps_per_s"] / seq[a]["lps_per_s"]
+                                      for a in seq}}
+    return _device_clock_line(line, clk)
+
+
+def run_diff(args):
+    """The differentiable layer on 64 random sparse LPs (m = 500, n = 1200, FP64): forward
+    (batched PDLP to 1e-8 + 2000 unrolled PDHG iterations) and backward (envelope gradients +
+    the checkpointed adjoint), seconds per step."""
+    import numpy as np
+    import samaya_gb300 as sg
+    from samaya_gb300 import generators as g
+    from samaya_gb300.diff import LpLayer, UnrolledPdhg
+    from samaya_gb300.problem import make_problem
+    B, m, n = 64, 500, 1200
+    probs = [make_problem(g.random_sparse_lp(m, n, seed=k))[0] for k in range(B)]
+    cost = np.stack([p.cost for p in probs])
+    lower = np.stack([p.lower for p in probs])
+    upper = np.stack([p.upper for p in probs])
+    layer = LpLayer(probs, tol=1e-8, iterations=2000, checkpoint_every=64)
+    fw, bw, un_f, un_b = [], [], [], []
+    with Clocks(0) as clk:
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            obj, vstar, ystar, vk, status = layer.evaluate(cost, lower, upper)
+            t1 = time.perf_counter()
+            layer.vjp(np.ones(B), np.concatenate([vk[:, :n], np.zeros((B, m))], axis=1))
+            t2 = time.perf_counter()
+            batch, unroll = layer._state[0], layer._state[1]
+            t3 = time.perf_counter()
+            unroll.forward()
+            t4 = time.perf_counter()
+            unroll.adjoint(np.ones(unroll.total))
+            t5 = time.perf_counter()
+            if i >= args.warmup:
+                fw.append(t1 - t0)
+                bw.append(t2 - t1)
+                un_f.append(t4 - t3)
+                un_b.append(t5 - t4)
+    layer.close()
+    mean = lambda a: sum(a) / len(a)  # noqa: E731
+    line = {"metric": "differentiable LP layer, seconds per forward + backward",
+            "value": mean(fw) + mean(bw), "unit": "s", "higher_is_better": False,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
+            "config": {"workload": "64 random sparse LPs m=500 n=1200 (nnz 7200 each), FP64",
+                       "unrolled_iterations": 2000, "checkpoint_every": 64, "tol": 1e-8},
+            "forward_s": mean(fw), "backward_s": mean(bw),
+            "unroll_forward_s": mean(un_f), "unroll_adjoint_s": mean(un_b),
+            "all_optimal": bool(np.all(status == sg.OPTIMAL))}
+    return _device_clock_line(line, clk)
+
+
 def run_reference(args):
     world, rank, _ = dist()
     if rank != 0:
+        return 0
+    if args.workload not in ("transport", "powerlaw", "random"):
+        print(json.dumps({"impl": "reference", "unavailable": "the reference solves one LP at "
+                          "a time and has no adjoint: no counterpart of this workload"}))
         return 0
     model, cfg = workload(args.workload)
     from samaya_gb300.problem import make_problem
@@ -239,6 +386,10 @@ def main():
         return run_reference(args)
     if args.profile:
         return run_profile(args)
+    if args.workload in ("batchA", "batchB"):
+        return run_batch(args)
+    if args.workload == "diff":
+        return run_diff(args)
     world, rank, local = dist()
     import numpy as np
     import samaya_gb300 as sg
@@ -330,8 +481,9 @@ def main():
         "data": "synthetic",
         "config": dict(cfg, tol=TOL, precision=PRECISION_NAMES[args.precision],
                        switch_tol=args.switch_tol if args.precision == "mixed" else None,
-                       algorithm="enhanced (inf-norm Ruiz + Pock-Chambolle, primal weight "
-                       "|c|/|b|)", l2="inputs larger than L2 (~260 MB)"),
+                       algorithm=ALGORITHM_NAMES[args.algorithm],
+                       l2="inputs larger than L2" if lp.nnz >= 4_000_000 else
+                       "inputs smaller than L2"),
         "status": last.status_name, "iterations": last.iterations,
         "refinement_rounds": last.refinement_rounds,
         "relative_kkt": [last.primal_residual, last.dual_residual, last.gap],
