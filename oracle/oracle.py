@@ -196,3 +196,22 @@ def eval_sums(m, n, colptr, rowidx, vals, cost, lower, upper, cs, rs, v, y):
     lib().orc_eval_sums(ctypes.c_int(m), ctypes.c_int(n), _p(arrs[0], I64), _p(arrs[1], I32),
                         *[_p(a, D) for a in arrs[2:]], _p(out, D))
     return out
+
+
+def verify_lp(model, x, y, tol_primal=1e-6, tol_dual=1e-6):
+    """The reference's verify_lp_optimality (src/verify/verify.cpp) for an LP model and its
+    column values x and row duals y (the reference's convention, d = c - A'y): (ok, dict of the
+    largest bound / row / dual violations and the objective)."""
+    out = np.zeros(4)
+    a = [np.ascontiguousarray(v, dtype=t) for v, t in (
+        (model.colptr, np.int64), (model.rowidx, np.int32), (model.vals, np.float64),
+        (model.obj, np.float64), (model.col_lower, np.float64), (model.col_upper, np.float64),
+        (model.row_lower, np.float64), (model.row_upper, np.float64), (x, np.float64),
+        (y, np.float64))]
+    f = lib().orc_verify_lp
+    f.restype = ctypes.c_int
+    ok = f(ctypes.c_int(model.m), ctypes.c_int(model.n), _p(a[0], I64), _p(a[1], I32),
+           _p(a[2], D), _p(a[3], D), D(model.obj_offset), _p(a[4], D), _p(a[5], D),
+           _p(a[6], D), _p(a[7], D), ctypes.c_int(int(model.maximize)), _p(a[8], D),
+           _p(a[9], D), D(tol_primal), D(tol_dual), _p(out, D))
+    return bool(ok), {"bound": out[0], "row": out[1], "dual": out[2], "objective": out[3]}

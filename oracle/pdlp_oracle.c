@@ -1035,3 +1035,121 @@ void orc_eval_sums(int m, int n, const int64_t* colptr, const int32_t* rowidx, c
   free(e.x_orig); free(e.r_orig); free(e.y_orig); free(e.ax); free(e.aty);
   csc_free(&A); csc_free(&At);
 }
+
+/* ------------------------------------------------------------------------------------------ */
+/* The reference's independent solution check for an LP (src/verify/verify.cpp:50-249,
+ * verify_primal + verify_kkt without Q, quadratic rows or integrality): bounds, row activities
+ * and reduced costs d = c - A'y recomputed from the model in double-double arithmetic (sums of
+ * pairs with Knuth's two-sum, products exact with fma), relative violations as there:
+ *   bound / row:  (lo - v) / (1 + max(|lo|, scale)), scale = largest |a_ij x_j| of the row
+ *   column dual:  sense d_j allowed only towards the bound x_j sits at, / (1 + |c_j| + sum |a_ij y_i|)
+ *   row dual:     sense y_i likewise for the row activity, / (1 + |y_i|)
+ * Returns 1 when every violation is within its tolerance. out[0..3] = max bound violation,
+ * max row violation, max dual violation, objective (offset + c'x). */
+
+typedef struct {
+  double hi, lo;
+} dd_t;
+
+static dd_t dd_add_d(dd_t a, double b) {
+  double s = a.hi + b;
+  double bb = s - a.hi;
+  double err = (a.hi - (s - bb)) + (b - bb);
+  err += a.lo;
+  double hi = s + err;
+  dd_t r = {hi, err - (hi - s)};
+  return r;
+}
+
+static dd_t dd_add(dd_t a, dd_t b) {
+  dd_t r = dd_add_d(a, b.hi);
+  return dd_add_d(r, b.lo);
+}
+
+static dd_t dd_prod(double a, double b) {
+  double p = a * b;
+  dd_t r = {p, fma(a, b, -p)};
+  return r;
+}
+
+static double dd_val(dd_t a) { return a.hi + a.lo; }
+
+static double bound_violation(double v, double lo, double up, double scale) {
+  double viol = 0.0;
+  if (v < lo) viol = (lo - v) / (1.0 + fmax(fabs(lo), scale));
+  if (v > up) viol = (v - up) / (1.0 + fmax(fabs(up), scale));
+  return viol;
+}
+
+static int at_bound(double v, double bound, double scale, double tol) {
+  return isfinite(bound) && fabs(v - bound) <= tol * (1.0 + fmax(fabs(bound), scale));
+}
+
+int orc_verify_lp(int m, int n, const int64_t* colptr, const int32_t* rowidx, const double* vals,
+                  const double* obj, double offset, const double* col_lower,
+                  const double* col_upper, const double* row_lower, const double* row_upper,
+                  int maximize, const double* x, const double* y, double tol_primal,
+                  double tol_dual, double* out) {
+  int ok = 1;
+  double max_bound = 0.0, max_row = 0.0, max_dual = 0.0;
+  for (int j = 0; j < n; ++j) {
+    if (!isfinite(x[j])) { ok = 0; continue; }
+    double v = bound_violation(x[j], col_lower[j], col_upper[j], 0.0);
+    max_bound = fmax(max_bound, v);
+    if (v > tol_primal) ok = 0;
+  }
+  dd_t* act = (dd_t*)xmalloc((size_t)(m > 0 ? m : 1), sizeof(dd_t));
+  double* mag = (double*)xmalloc((size_t)(m > 0 ? m : 1), sizeof(double));
+  for (int i = 0; i < m; ++i) { act[i].hi = act[i].lo = 0.0; mag[i] = 0.0; }
+  const double sense = maximize ? -1.0 : 1.0;
+  for (int j = 0; j < n; ++j) {
+    dd_t d = {obj[j], 0.0};
+    double scale = fabs(obj[j]);
+    for (int64_t p = colptr[j]; p < colptr[j + 1]; ++p) {
+      const int i = rowidx[p];
+      dd_t t = dd_prod(vals[p], y[i]);
+      t.hi = -t.hi;
+      t.lo = -t.lo;
+      d = dd_add(d, t);
+      scale += fabs(vals[p] * y[i]);
+      dd_t a = dd_prod(vals[p], x[j]);
+      act[i] = dd_add(act[i], a);
+      mag[i] = fmax(mag[i], fabs(vals[p] * x[j]));
+    }
+    const double dj = sense * dd_val(d);
+    if (!isfinite(dj) || !isfinite(scale)) { ok = 0; max_dual = ORC_INF; continue; }
+    const int lower = at_bound(x[j], col_lower[j], 0.0, tol_primal);
+    const int upper = at_bound(x[j], col_upper[j], 0.0, tol_primal);
+    double viol = 0.0;
+    if (!lower) viol = fmax(viol, dj);
+    if (!upper) viol = fmax(viol, -dj);
+    viol /= 1.0 + scale;
+    max_dual = fmax(max_dual, viol);
+    if (viol > tol_dual) ok = 0;
+  }
+  for (int i = 0; i < m; ++i) {
+    const double r = dd_val(act[i]);
+    if (!isfinite(r) || !isfinite(mag[i]) || !isfinite(y[i])) { ok = 0; max_row = ORC_INF; continue; }
+    double v = bound_violation(r, row_lower[i], row_upper[i], mag[i]);
+    max_row = fmax(max_row, v);
+    if (v > tol_primal) ok = 0;
+    const double yi = sense * y[i];
+    const int lower = at_bound(r, row_lower[i], mag[i], tol_primal);
+    const int upper = at_bound(r, row_upper[i], mag[i], tol_primal);
+    double viol = 0.0;
+    if (!lower) viol = fmax(viol, yi);
+    if (!upper) viol = fmax(viol, -yi);
+    viol /= 1.0 + fabs(yi);
+    max_dual = fmax(max_dual, viol);
+    if (viol > tol_dual) ok = 0;
+  }
+  dd_t objective = {offset, 0.0};
+  for (int j = 0; j < n; ++j) objective = dd_add(objective, dd_prod(obj[j], x[j]));
+  out[0] = max_bound;
+  out[1] = max_row;
+  out[2] = max_dual;
+  out[3] = dd_val(objective);
+  free(act);
+  free(mag);
+  return ok;
+}

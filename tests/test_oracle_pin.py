@@ -3,6 +3,8 @@ reference's own code, through the golden fixtures made from the reference
 (tests/golden/make_golden.py), and with the reference library itself where it is built."""
 from __future__ import annotations
 
+import os
+
 import numpy as np
 import pytest
 
@@ -109,3 +111,26 @@ def test_engine_host_scaling_matches_reference_fixtures(group):
         assert np.array_equal(sc.col, c.col_scale) and np.array_equal(sc.row, c.row_scale)
         for k in ("colptr", "rowidx", "vals", "cost", "lower", "upper"):
             assert np.array_equal(getattr(lp, k), getattr(c.lp, k)), (group, c.k, k)
+
+
+def test_verifier_restatement_on_the_dual_simplex_solutions(oracle):
+    """The oracle's restatement of the reference's verify_lp_optimality passes the reference
+    dual simplex's solutions of the 500 x 1200 LPs (their objectives to the bit) and rejects
+    perturbed ones; where the reference is built, it agrees with the reference's verifier on
+    every case."""
+    import numpy as np
+    from oracle import ref
+    from samaya_gb300.generators import random_sparse_lp
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "config4.npz"))
+    live = ref.available()
+    for k in range(int(d["count"][0])):
+        model = random_sparse_lp(500, 1200, seed=k)
+        x, y = d[f"k{k}_x"], d[f"k{k}_y"]
+        for xx, yy, expect in ((x, y, True), (x * 1.0001, y, False), (x, y * 1.01, False)):
+            ok, rep = oracle.verify_lp(model, xx, yy)
+            assert ok == expect, (k, rep)
+            if expect:
+                assert rep["objective"] == float(d[f"k{k}_simplex"][1])
+            if live:
+                ok_ref, obj_ref = ref.verify_optimal(model, xx, yy)
+                assert ok_ref == ok and obj_ref == rep["objective"]
