@@ -135,6 +135,29 @@ struct PrimalEpi {
 template <typename T>
 using Acc = T;  // FP64 storage accumulates in FP64, FP32 storage in FP32.
 
+// The scalars of one step launch, computed once per CTA by thread 0 and shared: a division and
+// four conversions in every thread of thousands of CTAs kept GB300's small FP64 pipe busy
+// (half its peak in the FP32 dual step).
+template <typename ACC>
+struct StepScalars {
+  ACC sigma, tau, alpha, beta;
+};
+
+template <typename ACC>
+__device__ __forceinline__ StepScalars<ACC> step_scalars(const Ctl* __restrict__ ctl,
+                                                         long long k) {
+  __shared__ StepScalars<ACC> sh;
+  if (threadIdx.x == 0) {
+    const double alpha = 1.0 / static_cast<double>(k + 1);
+    sh.sigma = static_cast<ACC>(ctl->sigma);
+    sh.tau = static_cast<ACC>(ctl->tau);
+    sh.alpha = static_cast<ACC>(alpha);
+    sh.beta = static_cast<ACC>(1.0 - alpha);
+  }
+  __syncthreads();
+  return sh;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kBlock, 6) dual_step_kernel(const Ctl* __restrict__ ctl,
                                                            OpView<T> K, IterView<T> it, int j) {
@@ -144,7 +167,7 @@ __global__ void __launch_bounds__(kBlock, 6) dual_step_kernel(const Ctl* __restr
   using ACC = Acc<T>;
   const int p = static_cast<int>(t & 1);
   const long long k = ctl->k + j;
-  const double alpha = 1.0 / static_cast<double>(k + 1);
+  const StepScalars<ACC> sc = step_scalars<ACC>(ctl, k);
   DualEpi<T, ACC> epi;
   const int n = it.n;
   epi.y = it.Y[p];
@@ -158,10 +181,10 @@ __global__ void __launch_bounds__(kBlock, 6) dual_step_kernel(const Ctl* __restr
   epi.q = it.rhs;
   epi.yerg = it.Yerg;
   epi.verg_r = it.Verg + n;
-  epi.sigma = static_cast<ACC>(ctl->sigma);
-  epi.tau = static_cast<ACC>(ctl->tau);
-  epi.alpha = static_cast<ACC>(alpha);
-  epi.beta = static_cast<ACC>(1.0 - alpha);
+  epi.sigma = sc.sigma;
+  epi.tau = sc.tau;
+  epi.alpha = sc.alpha;
+  epi.beta = sc.beta;
   Gather1<T, ACC> g{it.Vbar};
   run_tiles<T, ACC, 1>(K.ts, K.ptr, K.idx, K.val, g, epi);
 }
@@ -175,7 +198,7 @@ __global__ void __launch_bounds__(kBlock, 6) primal_step_kernel(const Ctl* __res
   using ACC = Acc<T>;
   const int p = static_cast<int>(t & 1);
   const long long k = ctl->k + j;
-  const double alpha = 1.0 / static_cast<double>(k + 1);
+  const StepScalars<ACC> sc = step_scalars<ACC>(ctl, k);
   PrimalEpi<T, ACC> epi;
   epi.x = it.V[p];
   epi.x_new = it.V[p ^ 1];
@@ -184,9 +207,9 @@ __global__ void __launch_bounds__(kBlock, 6) primal_step_kernel(const Ctl* __res
   epi.l = it.lower;
   epi.u = it.upper;
   epi.xerg = it.Verg;
-  epi.tau = static_cast<ACC>(ctl->tau);
-  epi.alpha = static_cast<ACC>(alpha);
-  epi.beta = static_cast<ACC>(1.0 - alpha);
+  epi.tau = sc.tau;
+  epi.alpha = sc.alpha;
+  epi.beta = sc.beta;
   Gather1<T, ACC> g{it.Y[p ^ 1]};
   run_tiles<T, ACC, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
 }

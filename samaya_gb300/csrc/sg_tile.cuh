@@ -75,6 +75,32 @@ struct Vec4<double> {
   }
 };
 
+// Deterministic block reduction of K values in the accumulation type (fixed shuffle tree, then
+// the warps in order by thread 0, which receives the totals).
+template <typename ACC, int K, bool MAXRED>
+__device__ __forceinline__ void block_reduce_acc(ACC (&v)[K], ACC* scratch, ACC (&out)[K]) {
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  constexpr int kWarps = kBlock / 32;
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    ACC s = v[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s = combine<MAXRED>(s, __shfl_down_sync(0xffffffffu, s, o));
+    if (lane == 0) scratch[q * kWarps + warp] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      ACC s = scratch[q * kWarps];
+      for (int w = 1; w < kWarps; ++w) s = combine<MAXRED>(s, scratch[q * kWarps + w]);
+      out[q] = s;
+    }
+  }
+  __syncthreads();
+}
+
 // Prod: ACC operator()(int v, T val, int col) const — the v-th product of a nonzero.
 // Epi: void row(int r, const ACC (&s)[NV]) for rows of kind-0 tiles (lane 0 of the row's team),
 //      void long_row(int lrow, int r, const ACC (&s)[NV]) for a split row (thread 0 of the CTA
@@ -211,12 +237,12 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
         if (lane == 0) epi.row(r, s);
       }
     } else {
-      // A segment of a long row: strided sums, then the fixed block tree.
-      double part[NV];
-      {
-        ACC s[NV];
+      // A segment of a long row: strided sums, then the fixed block tree (in the accumulation
+      // type: FP32 kernels keep off GB300's small FP64 pipe).
+      ACC s[NV];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) s[v] = ACC(0);
+      for (int v = 0; v < NV; ++v) s[v] = ACC(0);
+      {
         // Head up to a 4-aligned position, then 16-byte loads of four nonzeros per thread,
         // then the tail (scalar).
         const int k0 = tile.k0;
@@ -249,24 +275,17 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
 #pragma unroll
           for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
         }
-#pragma unroll
-        for (int v = 0; v < NV; ++v) part[v] = static_cast<double>(s[v]);
       }
-      double tot[NV];
-      block_reduce<NV, MAXRED ? 0xFFu : 0u>(part, red, tot);
+      ACC tot[NV];
+      block_reduce_acc<ACC, NV, MAXRED>(s, reinterpret_cast<ACC*>(red), tot);
       if (tile.nseg == 1) {
         // The whole row in one tile: no partials to combine.
-        if (tid == 0) {
-          ACC s[NV];
-#pragma unroll
-          for (int v = 0; v < NV; ++v) s[v] = static_cast<ACC>(tot[v]);
-          epi.long_row(tile.lrow, tile.r0, s);
-        }
+        if (tid == 0) epi.long_row(tile.lrow, tile.r0, tot);
         continue;
       }
       if (tid == 0) {
 #pragma unroll
-        for (int v = 0; v < NV; ++v) ts.seg_part[ti * kMaxVec + v] = tot[v];
+        for (int v = 0; v < NV; ++v) ts.seg_part[ti * kMaxVec + v] = static_cast<double>(tot[v]);
         __threadfence();
         const unsigned prev = atomicAdd(ts.lcount + tile.lrow, 1u);
         last_seg = (prev == static_cast<unsigned>(tile.nseg - 1));
