@@ -265,9 +265,11 @@ def run_batch(args):
         cfg = {"workload": "256 facility-location node relaxations (100 x 400) sharing A",
                "instances": 256, "nnz": int(lp.nnz)}
     out = {}
+    algs = (("reference", sg.REFERENCE),) if args.algorithm == "reference" else (
+        ("enhanced", sg.ENHANCED),)
     with Clocks(0) as clk:
         for name, prec in (("fp64", sg.FP64), ("fp32", sg.FP32_REFINED)):
-            for alg_name, alg in (("reference", sg.REFERENCE), ("enhanced", sg.ENHANCED)):
+            for alg_name, alg in algs:
                 s = make(sg.PdlpOptions(tol=tol, precision=prec, algorithm=alg))
                 for _ in range(args.warmup):
                     s.solve(download=False)
@@ -285,7 +287,7 @@ def run_batch(args):
         # Sequential single-LP GPU solves (FP64, each algorithm) on a sample of the instances.
         seq = {}
         k = 16
-        for alg_name, alg in (("reference", sg.REFERENCE), ("enhanced", sg.ENHANCED)):
+        for alg_name, alg in algs:
             ms = 0.0
             for p in singles[:k]:
                 ms += sg.solve_pdlp(p, sg.PdlpOptions(tol=tol, algorithm=alg)).device_ms
