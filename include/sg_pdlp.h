@@ -64,6 +64,9 @@ typedef struct sg_pdlp_opts {
   double inner_tol;          /* tolerance of each FP32 solve or FP32 phase (default 1e-4) */
   int verbose;               /* 0 silent */
   int algorithm;             /* SG_ALGORITHM_* (default SG_ALGORITHM_REFERENCE) */
+  int autotune;              /* 1 (default): time candidate tile shapes of each large operator
+                                on the device at create, keyed by its row-length statistics
+                                (cached per process); 0: the built-in rule */
 } sg_pdlp_opts;
 
 /* Algorithm variants. REFERENCE follows samaya's PDLP step for step (L2 Ruiz, fixed step
@@ -163,6 +166,11 @@ int sg_pdhg_download(sg_pdlp* handle, double* v, double* v_new, double* y, doubl
  * roofline report; the iterate is left unusable (the next solve starts afresh). */
 int sg_pdlp_time_kernels(sg_pdlp* handle, int reps, double* ms_dual, double* ms_primal,
                          double* ms_eval);
+
+/* The tile shape in use for A (transpose 0) or A' (transpose 1): nonzeros per tile, rows per
+ * short-row tile, number of tiles (diagnostics; set by the autotuner or the built-in rule). */
+int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_rows,
+                       int* ntiles);
 
 /* Model -> LpProblem: samaya's power-of-two scaling and computational form, as
  * compute_scaling + make_problem compute them (reference src/linalg/scaling.cpp:130-200,

@@ -22,7 +22,8 @@ class Opts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("max_iterations", ctypes.c_longlong),
                 ("time_limit", ctypes.c_double), ("precision", ctypes.c_int),
                 ("refine_max_rounds", ctypes.c_int), ("inner_tol", ctypes.c_double),
-                ("verbose", ctypes.c_int), ("algorithm", ctypes.c_int)]
+                ("verbose", ctypes.c_int), ("algorithm", ctypes.c_int),
+                ("autotune", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -104,6 +105,8 @@ def _declare(lib):
                                  c_double_p]),
         "sg_spmv": (I, [P, I, c_double_p, c_double_p]),
         "sg_pdlp_time_kernels": (I, [P, I, c_double_p, c_double_p, c_double_p]),
+        "sg_pdlp_tile_shape": (I, [P, I, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                   ctypes.POINTER(ctypes.c_int)]),
         "sg_scale_model": (I, [I, I, c_int64_p, c_int32_p, c_double_p, c_double_p, c_double_p,
                                c_double_p, c_double_p, c_double_p, I, c_int64_p, c_int32_p,
                                c_double_p, c_double_p, c_double_p, c_double_p, c_double_p,

@@ -36,6 +36,7 @@ sg::Options to_options(const sg_pdlp_opts* o) {
   opt.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
   opt.verbose = o->verbose;
   opt.algorithm = o->algorithm == SG_ALGORITHM_ENHANCED ? 1 : 0;
+  opt.autotune = o->autotune != 0;
   return opt;
 }
 
@@ -53,6 +54,7 @@ void sg_pdlp_default_opts(sg_pdlp_opts* opts) {
   opts->refine_max_rounds = 6;
   opts->inner_tol = 1e-4;
   opts->verbose = 0;
+  opts->autotune = 1;
 }
 
 int sg_pdlp_available(int* cc_major, int* cc_minor, char* name, size_t name_len) {
@@ -224,6 +226,14 @@ int sg_pdlp_time_kernels(sg_pdlp* handle, int reps, double* ms_dual, double* ms_
     return fail(SG_ERR_INVALID_ARGUMENT, "bad arguments");
   }
   SG_SEAM(handle->engine->time_kernels(reps, ms_dual, ms_primal, ms_eval));
+}
+
+int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_rows,
+                       int* ntiles) {
+  if (cap_nnz == nullptr || cap_rows == nullptr || ntiles == nullptr) {
+    return fail(SG_ERR_INVALID_ARGUMENT, "NULL output");
+  }
+  SG_SEAM(handle->engine->tile_shape(transpose, cap_nnz, cap_rows, ntiles));
 }
 
 int sg_spmv(sg_pdlp* handle, int transpose, const double* x, double* y) {

@@ -5,7 +5,10 @@
 #include <algorithm>
 #include <chrono>
 #include <limits>
+#include <map>
+#include <mutex>
 #include <random>
+#include <tuple>
 #include <type_traits>
 
 #include "sg_engine.cuh"
@@ -44,27 +47,27 @@ std::vector<double> power_start(int m) {
 
 }  // namespace
 
-// Tiles: a row longer than tile_nnz / 8 is reduced by a whole CTA, as ceil(len / tile_nnz)
-// segment tiles of its own; the other rows go consecutively into tiles of at most tile_nnz
-// nonzeros and tile_rows rows, with team = the power of two nearest below half the tile's mean
-// row length (1..32 lanes per row).
-void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, std::vector<Tile>* out,
-                 int* nlong) {
+// Tiles: a row longer than tile_nnz is reduced by whole CTAs, as ceil(len / tile_nnz) segment
+// tiles of its own (kind 1); rows of more than warp_min nonzeros go by up to 8 into warp-per-row
+// tiles (kind 2); the other rows go consecutively into tiles of at most tile_nnz nonzeros and
+// tile_rows rows, a thread per row (kind 0).
+void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, int warp_min,
+                 std::vector<Tile>* out, int* nlong) {
   out->clear();
   *nlong = 0;
   const int rows = static_cast<int>(ptr.size()) - 1;
   // Rows longer than a tile are split into CTA segments (kind 1); rows of more than
-  // kWarpRowMin nonzeros get a warp each, kWarpsPerTile rows per tile (kind 2).
-  const int long_len = std::max(tile_nnz, kWarpRowMin);
+  // warp_min nonzeros get a warp each, kWarpsPerTile rows per tile (kind 2).
+  const int long_len = std::max(tile_nnz, warp_min);
   int r = 0;
   while (r < rows) {
     const int len = ptr[r + 1] - ptr[r];
-    if (len > kWarpRowMin && len <= long_len) {
+    if (len > warp_min && len <= long_len) {
       Tile t{};
       t.r0 = r;
       while (r < rows && r - t.r0 < kWarpsPerTile) {
         const int l = ptr[r + 1] - ptr[r];
-        if (l <= kWarpRowMin || l > long_len) break;
+        if (l <= warp_min || l > long_len) break;
         ++r;
       }
       t.r1 = r;
@@ -100,7 +103,7 @@ void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, std::
     const int r0 = r;
     while (r < rows && r - r0 < tile_rows) {
       const int l = ptr[r + 1] - ptr[r];
-      if (l > kWarpRowMin) break;
+      if (l > warp_min) break;
       if (ptr[r + 1] - ptr[r0] > tile_nnz) break;
       ++r;
     }
@@ -313,34 +316,10 @@ int Engine::create(Engine** out, int m, int n, const int64_t* colptr, const int3
   if (ce == cudaSuccess) ce = up(e->upper_orig_, upper, nt * sizeof(double));
   std::vector<double> u0 = power_start(m);
   if (ce == cudaSuccess) ce = up(e->u0_, u0.data(), u0.size() * sizeof(double));
-  // Tiles: the capacity is a power of two between 256 and kTileNnz nonzeros chosen so each
-  // operator has about 8 tiles per SM (small problems spread over every SM; large ones stream
-  // long tiles); rows per tile at most half the nonzero capacity (at least 256).
   {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&e->sm_count_, cudaDevAttrMultiProcessorCount, dev);
-  }
-  for (DevOp* op : {&e->K_, &e->Kt_}) {
-    const long long target = std::max<long long>(1, op->nnz / (8LL * e->sm_count_));
-    int cap = 256;
-    while (cap < kTileNnz && cap < target) cap *= 2;
-    op->cap_nnz = cap;
-    op->cap_rows = std::min(kTileRows, std::max(256, cap / 2));
-    std::vector<Tile> tiles;
-    int nlong = 0;
-    build_tiles(op->host_ptr, op->cap_nnz, op->cap_rows, &tiles, &nlong);
-    op->ntiles = static_cast<int>(tiles.size());
-    op->nlong = nlong;
-    if (ce == cudaSuccess) ce = dalloc(&op->tiles, tiles.size());
-    if (ce == cudaSuccess) ce = up(op->tiles, tiles.data(), tiles.size() * sizeof(Tile));
-    if (ce == cudaSuccess) ce = dalloc(&op->seg_part, tiles.size() * kMaxVec);
-    if (ce == cudaSuccess) ce = dalloc(&op->lcount, std::max(nlong, 1));
-    if (ce == cudaSuccess) ce = cudaMemsetAsync(op->lcount, 0, std::max(nlong, 1) * sizeof(unsigned), s);
-  }
-  if (ce == cudaSuccess) {
-    const int maxlong = std::max(std::max(e->K_.nlong, e->Kt_.nlong), 1);
-    ce = dalloc(&e->long_terms_, static_cast<size_t>(maxlong) * kMaxSums);
   }
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
   if (ce != cudaSuccess) {
@@ -349,17 +328,204 @@ int Engine::create(Engine** out, int m, int n, const int64_t* colptr, const int3
     delete e;
     return code;
   }
-  // Grids: persistent CTAs for the evaluation kernels (2 per SM with 82 KB of shared memory);
-  // one CTA per tile for the step kernels.
-  int dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&e->sm_count_, cudaDevAttrMultiProcessorCount, dev);
-  const int eval_cap = e->sm_count_ * 2;
-  e->grid_k_ = std::max(1, std::min(e->K_.ntiles, eval_cap));
-  e->grid_t_ = std::max(1, std::min(e->Kt_.ntiles, eval_cap));
-  e->grid_step_k_ = std::max(1, std::min(e->K_.ntiles, 65535));
-  e->grid_step_t_ = std::max(1, std::min(e->Kt_.ntiles, 65535));
+  // Tiles of both operators (tuned or by the built-in rule), then the grids.
+  rc = e->tune_tiles(&why);
+  if (rc != kOk) {
+    if (err) *err = why;
+    delete e;
+    return rc;
+  }
   *out = e;
+  return kOk;
+}
+
+namespace {
+
+// Row-length statistics of an operator: the autotuner's cache key.
+struct ShapeKey {
+  int rows;
+  long long nnz;
+  int max_len;
+  long long over32, over128, over4096;
+  int fp32;
+  bool operator<(const ShapeKey& o) const {
+    return std::tie(rows, nnz, max_len, over32, over128, over4096, fp32) <
+           std::tie(o.rows, o.nnz, o.max_len, o.over32, o.over128, o.over4096, o.fp32);
+  }
+};
+
+std::mutex g_shape_mu;
+std::map<ShapeKey, TileShape> g_shape_cache;
+
+ShapeKey shape_key(const DevOp& op, bool fp32) {
+  ShapeKey k{op.rows, op.nnz, 0, 0, 0, 0, fp32 ? 1 : 0};
+  for (int r = 0; r < op.rows; ++r) {
+    const int len = op.host_ptr[r + 1] - op.host_ptr[r];
+    k.max_len = std::max(k.max_len, len);
+    k.over32 += len > 32;
+    k.over128 += len > 128;
+    k.over4096 += len > 4096;
+  }
+  return k;
+}
+
+}  // namespace
+
+// The built-in rule: a power of two between 256 and kTileNnz nonzeros per tile giving each
+// operator about 8 tiles per SM (small problems spread over every SM; large ones stream long
+// tiles); short-row tiles of at most half that many rows (256 to kTileRows).
+TileShape Engine::default_shape(const DevOp& op) const {
+  const long long target = std::max<long long>(1, op.nnz / (8LL * sm_count_));
+  TileShape sh;
+  int cap = 256;
+  while (cap < kTileNnz && cap < target) cap *= 2;
+  sh.cap_nnz = cap;
+  sh.cap_rows = std::min(kTileRows, std::max(256, cap / 2));
+  sh.warp_min = kWarpRowMin;
+  return sh;
+}
+
+// Builds an operator's tiles for a shape and uploads them (replacing earlier ones).
+int Engine::set_tiles(DevOp* op, const TileShape& shape) {
+  std::string* err = nullptr;
+  std::vector<Tile> tiles;
+  int nlong = 0;
+  build_tiles(op->host_ptr, shape.cap_nnz, shape.cap_rows, shape.warp_min, &tiles, &nlong);
+  SG_TRY(cudaStreamSynchronize(stream_));
+  dfree(op->tiles);
+  dfree(op->seg_part);
+  dfree(op->lcount);
+  op->cap_nnz = shape.cap_nnz;
+  op->cap_rows = shape.cap_rows;
+  op->warp_min = shape.warp_min;
+  op->ntiles = static_cast<int>(tiles.size());
+  op->nlong = nlong;
+  SG_TRY(dalloc(&op->tiles, tiles.size()));
+  if (!tiles.empty()) {
+    SG_TRY(cudaMemcpyAsync(op->tiles, tiles.data(), tiles.size() * sizeof(Tile),
+                           cudaMemcpyHostToDevice, stream_));
+  }
+  SG_TRY(dalloc(&op->seg_part, tiles.size() * kMaxVec));
+  SG_TRY(dalloc(&op->lcount, std::max(nlong, 1)));
+  SG_TRY(cudaMemsetAsync(op->lcount, 0, std::max(nlong, 1) * sizeof(unsigned), stream_));
+  SG_TRY(cudaStreamSynchronize(stream_));
+  return kOk;
+}
+
+// Average device milliseconds of one step kernel (the dual step on K, or the primal step on
+// K'), in the precision of the solve, over `reps` launches after two warm-up launches. The
+// control block is set to run (it is re-initialised by every solve's setup).
+double Engine::time_step_kernel(bool dual, int reps) {
+  Ctl* c = fp32_ ? ctl32_ : ctl_;
+  Ctl h;
+  memset(&h, 0, sizeof(h));
+  h.m = m_;
+  h.n = n_;
+  h.max_iter = std::numeric_limits<long long>::max();
+  h.status = kRunning;
+  h.tau = h.sigma = h.eta = 0.5;
+  h.omega = 1.0;
+  if (cudaMemcpy(c, &h, sizeof(Ctl), cudaMemcpyHostToDevice) != cudaSuccess) return -1.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto launch = [&](int j) {
+    if (fp32_) {
+      IterView<float> it = iter_view(it32_);
+      if (dual) {
+        launch_dual_step(c, K_.view32(), it, j, std::max(1, std::min(K_.ntiles, 65535)), stream_);
+      } else {
+        launch_primal_step(c, Kt_.view32(), it, j, std::max(1, std::min(Kt_.ntiles, 65535)),
+                           stream_);
+      }
+    } else {
+      IterView<double> it = iter_view(it64_);
+      if (dual) {
+        launch_dual_step(c, K_.view64(), it, j, std::max(1, std::min(K_.ntiles, 65535)), stream_);
+      } else {
+        launch_primal_step(c, Kt_.view64(), it, j, std::max(1, std::min(Kt_.ntiles, 65535)),
+                           stream_);
+      }
+    }
+  };
+  launch(0);
+  launch(1);
+  cudaEventRecord(e0, stream_);
+  for (int r = 0; r < reps; ++r) launch(r & 1);
+  cudaEventRecord(e1, stream_);
+  float ms = -1.0f;
+  if (cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (cudaGetLastError() != cudaSuccess) return -1.0;
+  return ms / reps;
+}
+
+// Tile shapes of both operators. With autotuning, an operator of at least 2^18 nonzeros whose
+// row-length statistics were not seen before in this process gets its step kernel timed for
+// four shapes around the built-in rule (half, same, twice and four times the nonzeros per tile;
+// short-row tiles of half as many rows); the fastest is kept and cached under the statistics.
+int Engine::tune_tiles(std::string* err) {
+  for (int which = 0; which < 2; ++which) {
+    DevOp* op = which == 0 ? &K_ : &Kt_;
+    const TileShape base = default_shape(*op);
+    TileShape best = base;
+    const bool tune = opt_.autotune && op->nnz >= (1LL << 18);
+    ShapeKey key{};
+    bool cached = false;
+    if (tune) {
+      key = shape_key(*op, fp32_);
+      std::lock_guard<std::mutex> lock(g_shape_mu);
+      auto it = g_shape_cache.find(key);
+      if (it != g_shape_cache.end()) {
+        best = it->second;
+        cached = true;
+      }
+    }
+    if (tune && !cached) {
+      double best_ms = -1.0;
+      for (const int cap : {base.cap_nnz / 2, base.cap_nnz, base.cap_nnz * 2, base.cap_nnz * 4}) {
+        if (cap < 256 || cap > 4 * kTileNnz) continue;
+        TileShape sh = base;
+        sh.cap_nnz = cap;
+        sh.cap_rows = std::min(kTileRows, std::max(256, cap / 2));
+        const int rc = set_tiles(op, sh);
+        if (rc != kOk) {
+          if (err) *err = "autotune: tile upload failed";
+          return rc;
+        }
+        const double ms = time_step_kernel(which == 0, 10);
+        if (ms < 0) {
+          if (err) *err = std::string("autotune: ") + cudaGetErrorString(cudaGetLastError());
+          return kErrCuda;
+        }
+        if (best_ms < 0 || ms < best_ms) {
+          best_ms = ms;
+          best = sh;
+        }
+      }
+      std::lock_guard<std::mutex> lock(g_shape_mu);
+      g_shape_cache[key] = best;
+    }
+    const int rc = set_tiles(op, best);
+    if (rc != kOk) {
+      if (err) *err = "tile upload failed";
+      return rc;
+    }
+  }
+  dfree(long_terms_);
+  const int maxlong = std::max(std::max(K_.nlong, Kt_.nlong), 1);
+  if (dalloc(&long_terms_, static_cast<size_t>(maxlong) * kMaxSums) != cudaSuccess) {
+    if (err) *err = "out of device memory";
+    return kErrOutOfMemory;
+  }
+  // Grids: persistent CTAs for the evaluation kernels (2 per SM); one CTA per tile for the
+  // step kernels.
+  const int eval_cap = sm_count_ * 2;
+  grid_k_ = std::max(1, std::min(K_.ntiles, eval_cap));
+  grid_t_ = std::max(1, std::min(Kt_.ntiles, eval_cap));
+  grid_step_k_ = std::max(1, std::min(K_.ntiles, 65535));
+  grid_step_t_ = std::max(1, std::min(Kt_.ntiles, 65535));
   return kOk;
 }
 

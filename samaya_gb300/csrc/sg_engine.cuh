@@ -35,6 +35,15 @@ struct Options {
   double inner_tol = 1e-4;
   int verbose = 0;
   int algorithm = 0;        // 0 the reference's PDLP, 1 enhanced preconditioning + weight
+  bool autotune = true;     // time candidate tile shapes of large operators at create
+};
+
+// Tile shape of an operator: nonzeros per tile (and per long-row segment), rows per short-row
+// tile, and the row length above which a row gets a warp.
+struct TileShape {
+  int cap_nnz = kTileNnz;
+  int cap_rows = kTileRows;
+  int warp_min = kWarpRowMin;
 };
 
 struct SolveInfo {
@@ -69,6 +78,7 @@ struct DevOp {
   unsigned* lcount = nullptr;
   int cap_nnz = kTileNnz;
   int cap_rows = kTileRows;
+  int warp_min = kWarpRowMin;
   std::vector<int> host_ptr;
 
   TileSet tileset() const {
@@ -132,6 +142,13 @@ class Engine {
   // Average device milliseconds of the step kernels and the evaluation (CUDA events).
   int time_kernels(int reps, double* ms_dual, double* ms_primal, double* ms_eval);
   int tile_capacity(int transpose) const { return transpose ? Kt_.cap_nnz : K_.cap_nnz; }
+  int tile_shape(int transpose, int* cap_nnz, int* cap_rows, int* ntiles) const {
+    const DevOp& op = transpose ? Kt_ : K_;
+    *cap_nnz = op.cap_nnz;
+    *cap_rows = op.cap_rows;
+    *ntiles = op.ntiles;
+    return 0;
+  }
   bool fp32() const { return fp32_; }
 
   int m() const { return m_; }
@@ -162,6 +179,10 @@ class Engine {
                   double* dual_ray, double* primal_ray);
   void enqueue_chunk_body();
   int check(cudaError_t e, const char* what);
+  TileShape default_shape(const DevOp& op) const;
+  int set_tiles(DevOp* op, const TileShape& shape);
+  int tune_tiles(std::string* err);
+  double time_step_kernel(bool dual, int reps);
 
   int m_ = 0, n_ = 0;
   long long nnz_ = 0;
@@ -221,7 +242,8 @@ class Engine {
 };
 
 // Builds the tile partition of a CSR operator (host). Exposed for the CPU tests.
-void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, std::vector<Tile>* out,
+void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, int warp_min,
+                 std::vector<Tile>* out,
                  int* nlong);
 
 // Device facts for sg_pdlp_available.

@@ -41,6 +41,7 @@ class PdlpOptions:
     inner_tol: float = 1e-4
     algorithm: int = REFERENCE
     verbose: int = 0
+    autotune: bool = True
 
     def to_c(self) -> _native.Opts:
         o = _native.Opts()
@@ -53,6 +54,7 @@ class PdlpOptions:
         o.inner_tol = float(self.inner_tol)
         o.algorithm = int(self.algorithm)
         o.verbose = int(self.verbose)
+        o.autotune = 1 if self.autotune else 0
         return o
 
 
@@ -120,6 +122,17 @@ class PdlpSolver:
                                                      ctypes.byref(b), ctypes.byref(c)),
                       "sg_pdlp_time_kernels")
         return a.value, b.value, c.value
+
+    def tile_shapes(self):
+        """{"A": (nonzeros per tile, rows per short-row tile, tiles), "At": ...} in use."""
+        out = {}
+        for name, t in (("A", 0), ("At", 1)):
+            a, b, c = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+            _native.check(self._lib.sg_pdlp_tile_shape(self._h, t, ctypes.byref(a),
+                                                       ctypes.byref(b), ctypes.byref(c)),
+                          "sg_pdlp_tile_shape")
+            out[name] = (a.value, b.value, c.value)
+        return out
 
     def solve(self, x_out: np.ndarray | None = None, y_out: np.ndarray | None = None,
               download: bool = True) -> PdlpResult:

@@ -222,3 +222,29 @@ def test_solutions_pass_the_reference_verifier(engine):
     assert not failures["fp64-reference"], failures["fp64-reference"]
     for mode, bad in failures.items():
         assert len(bad) <= 0.2 * len(cases), (mode, bad)
+
+
+def test_autotuned_tiles_agree_with_the_built_in_rule(engine):
+    """A 20000 x 50000 random sparse LP (300,000 nonzeros: large enough to be tuned): the tile
+    shape the autotuner picks is one of its candidates, a second engine on the same structure
+    gets the same shape from the cache, and the solve agrees with the built-in rule's (status;
+    objective to 1e-3 relative at 1e-4, where the summation order may differ)."""
+    from samaya_gb300.generators import random_sparse_lp
+    from samaya_gb300.problem import make_problem
+    lp, _ = make_problem(random_sparse_lp(20000, 50000, seed=4))
+    base = dict(tol=1e-4, algorithm=engine.REFERENCE)
+    with engine.PdlpSolver(lp, engine.PdlpOptions(autotune=False, **base)) as s0:
+        r0 = s0.solve()
+        rule = s0.tile_shapes()
+    with engine.PdlpSolver(lp, engine.PdlpOptions(autotune=True, **base)) as s1:
+        r1 = s1.solve()
+        tuned = s1.tile_shapes()
+    with engine.PdlpSolver(lp, engine.PdlpOptions(autotune=True, **base)) as s2:
+        assert s2.tile_shapes() == tuned
+    for name in ("A", "At"):
+        assert tuned[name][0] in (rule[name][0] // 2, rule[name][0], 2 * rule[name][0],
+                                  4 * rule[name][0]), (tuned, rule)
+    assert r0.status == r1.status == engine.OPTIMAL
+    o0 = float(np.dot(lp.cost, r0.x))
+    o1 = float(np.dot(lp.cost, r1.x))
+    assert abs(o0 - o1) <= 1e-3 * (1 + abs(o0)), (o0, o1)
