@@ -135,9 +135,9 @@ struct PrimalEpi {
 template <typename T>
 using Acc = T;  // FP64 storage accumulates in FP64, FP32 storage in FP32.
 
-// The scalars of one step launch, computed once per CTA by thread 0 and shared: a division and
-// four conversions in every thread of thousands of CTAs kept GB300's small FP64 pipe busy
-// (half its peak in the FP32 dual step).
+// The scalars of one step launch. FP64 kernels compute them once per CTA (thread 0) and share
+// them: an FP64 division in every thread of thousands of CTAs kept GB300's small FP64 pipe
+// busy. FP32 kernels compute the average weight in FP32 per thread.
 template <typename ACC>
 struct StepScalars {
   ACC sigma, tau, alpha, beta;
@@ -146,16 +146,27 @@ struct StepScalars {
 template <typename ACC>
 __device__ __forceinline__ StepScalars<ACC> step_scalars(const Ctl* __restrict__ ctl,
                                                          long long k) {
-  __shared__ StepScalars<ACC> sh;
-  if (threadIdx.x == 0) {
-    const double alpha = 1.0 / static_cast<double>(k + 1);
-    sh.sigma = static_cast<ACC>(ctl->sigma);
-    sh.tau = static_cast<ACC>(ctl->tau);
-    sh.alpha = static_cast<ACC>(alpha);
-    sh.beta = static_cast<ACC>(1.0 - alpha);
+  if constexpr (std::is_same<ACC, double>::value) {
+    __shared__ StepScalars<double> sh;
+    if (threadIdx.x == 0) {
+      const double alpha = 1.0 / static_cast<double>(k + 1);
+      sh.sigma = ctl->sigma;
+      sh.tau = ctl->tau;
+      sh.alpha = alpha;
+      sh.beta = 1.0 - alpha;
+    }
+    __syncthreads();
+    return sh;
+  } else {
+    // FP32: per thread, the average weight by an FP32 division (the shared-memory broadcast
+    // above put a dependent load and a barrier in front of every CTA's first load: slower).
+    StepScalars<ACC> s;
+    s.sigma = static_cast<ACC>(ctl->sigma);
+    s.tau = static_cast<ACC>(ctl->tau);
+    s.alpha = ACC(1) / static_cast<ACC>(k + 1);
+    s.beta = ACC(1) - s.alpha;
+    return s;
   }
-  __syncthreads();
-  return sh;
 }
 
 template <typename T>
