@@ -168,9 +168,10 @@ int sg_pdlp_time_kernels(sg_pdlp* handle, int reps, double* ms_dual, double* ms_
                          double* ms_eval);
 
 /* The tile shape in use for A (transpose 0) or A' (transpose 1): nonzeros per tile, rows per
- * short-row tile, number of tiles (diagnostics; set by the autotuner or the built-in rule). */
+ * short-row tile, number of tiles, and whether the step kernel runs its deep-unroll variant
+ * (diagnostics; set by the autotuner or the built-in rule). */
 int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_rows,
-                       int* ntiles);
+                       int* ntiles, int* wide);
 
 /* Model -> LpProblem: samaya's power-of-two scaling and computational form, as
  * compute_scaling + make_problem compute them (reference src/linalg/scaling.cpp:130-200,

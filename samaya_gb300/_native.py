@@ -105,8 +105,7 @@ def _declare(lib):
                                  c_double_p]),
         "sg_spmv": (I, [P, I, c_double_p, c_double_p]),
         "sg_pdlp_time_kernels": (I, [P, I, c_double_p, c_double_p, c_double_p]),
-        "sg_pdlp_tile_shape": (I, [P, I, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
-                                   ctypes.POINTER(ctypes.c_int)]),
+        "sg_pdlp_tile_shape": (I, [P, I] + [ctypes.POINTER(ctypes.c_int)] * 4),
         "sg_scale_model": (I, [I, I, c_int64_p, c_int32_p, c_double_p, c_double_p, c_double_p,
                                c_double_p, c_double_p, c_double_p, I, c_int64_p, c_int32_p,
                                c_double_p, c_double_p, c_double_p, c_double_p, c_double_p,

@@ -229,11 +229,11 @@ int sg_pdlp_time_kernels(sg_pdlp* handle, int reps, double* ms_dual, double* ms_
 }
 
 int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_rows,
-                       int* ntiles) {
-  if (cap_nnz == nullptr || cap_rows == nullptr || ntiles == nullptr) {
+                       int* ntiles, int* wide) {
+  if (cap_nnz == nullptr || cap_rows == nullptr || ntiles == nullptr || wide == nullptr) {
     return fail(SG_ERR_INVALID_ARGUMENT, "NULL output");
   }
-  SG_SEAM(handle->engine->tile_shape(transpose, cap_nnz, cap_rows, ntiles));
+  SG_SEAM(handle->engine->tile_shape(transpose, cap_nnz, cap_rows, ntiles, wide));
 }
 
 int sg_spmv(sg_pdlp* handle, int transpose, const double* x, double* y) {

@@ -45,6 +45,8 @@ struct TileSet {
   unsigned* lcount; // [nlong] arrival counters (reset by the last arrival)
   int cap_nnz;      // nonzeros per tile at most (shared-memory staging capacity)
   int cap_rows;     // rows per tile at most
+  int wide;         // step kernels: the deep-unroll variant (long rows) instead of the
+                    // high-occupancy one
 };
 
 constexpr int kMaxVec = 2;

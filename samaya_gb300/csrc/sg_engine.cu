@@ -382,6 +382,13 @@ TileShape Engine::default_shape(const DevOp& op) const {
   sh.cap_nnz = cap;
   sh.cap_rows = std::min(kTileRows, std::max(256, cap / 2));
   sh.warp_min = kWarpRowMin;
+  // The deep-unroll kernel variant when most nonzeros sit in rows a warp or CTAs take.
+  long long in_long = 0;
+  for (int r = 0; r < op.rows; ++r) {
+    const int len = op.host_ptr[r + 1] - op.host_ptr[r];
+    if (len > sh.warp_min) in_long += len;
+  }
+  sh.wide = 2 * in_long >= op.nnz && op.nnz > 0;
   return sh;
 }
 
@@ -398,6 +405,7 @@ int Engine::set_tiles(DevOp* op, const TileShape& shape) {
   op->cap_nnz = shape.cap_nnz;
   op->cap_rows = shape.cap_rows;
   op->warp_min = shape.warp_min;
+  op->wide = shape.wide;
   op->ntiles = static_cast<int>(tiles.size());
   op->nlong = nlong;
   SG_TRY(dalloc(&op->tiles, tiles.size()));
@@ -463,8 +471,9 @@ double Engine::time_step_kernel(bool dual, int reps) {
 
 // Tile shapes of both operators. With autotuning, an operator of at least 2^18 nonzeros whose
 // row-length statistics were not seen before in this process gets its step kernel timed for
-// four shapes around the built-in rule (half, same, twice and four times the nonzeros per tile;
-// short-row tiles of half as many rows); the fastest is kept and cached under the statistics.
+// eight shapes around the built-in rule (half, same, twice and four times the nonzeros per
+// tile, short-row tiles of half as many rows; each with both kernel variants); the fastest is
+// kept and cached under the statistics.
 int Engine::tune_tiles(std::string* err) {
   for (int which = 0; which < 2; ++which) {
     DevOp* op = which == 0 ? &K_ : &Kt_;
@@ -484,11 +493,13 @@ int Engine::tune_tiles(std::string* err) {
     }
     if (tune && !cached) {
       double best_ms = -1.0;
-      for (const int cap : {base.cap_nnz / 2, base.cap_nnz, base.cap_nnz * 2, base.cap_nnz * 4}) {
+      for (int c = 0; c < 8; ++c) {
+        const int cap = (base.cap_nnz / 2) << (c >> 1);
         if (cap < 256 || cap > 4 * kTileNnz) continue;
         TileShape sh = base;
         sh.cap_nnz = cap;
         sh.cap_rows = std::min(kTileRows, std::max(256, cap / 2));
+        sh.wide = (c & 1) != 0;
         const int rc = set_tiles(op, sh);
         if (rc != kOk) {
           if (err) *err = "autotune: tile upload failed";

@@ -44,6 +44,7 @@ struct TileShape {
   int cap_nnz = kTileNnz;
   int cap_rows = kTileRows;
   int warp_min = kWarpRowMin;
+  bool wide = false;        // step kernel variant (see sg_kernels.cu)
 };
 
 struct SolveInfo {
@@ -79,6 +80,7 @@ struct DevOp {
   int cap_nnz = kTileNnz;
   int cap_rows = kTileRows;
   int warp_min = kWarpRowMin;
+  bool wide = false;
   std::vector<int> host_ptr;
 
   TileSet tileset() const {
@@ -90,6 +92,7 @@ struct DevOp {
     t.lcount = lcount;
     t.cap_nnz = cap_nnz;
     t.cap_rows = cap_rows;
+    t.wide = wide ? 1 : 0;
     return t;
   }
   OpView<double> view64() const { return OpView<double>{ptr, idx, val, rows, tileset()}; }
@@ -142,11 +145,12 @@ class Engine {
   // Average device milliseconds of the step kernels and the evaluation (CUDA events).
   int time_kernels(int reps, double* ms_dual, double* ms_primal, double* ms_eval);
   int tile_capacity(int transpose) const { return transpose ? Kt_.cap_nnz : K_.cap_nnz; }
-  int tile_shape(int transpose, int* cap_nnz, int* cap_rows, int* ntiles) const {
+  int tile_shape(int transpose, int* cap_nnz, int* cap_rows, int* ntiles, int* wide) const {
     const DevOp& op = transpose ? Kt_ : K_;
     *cap_nnz = op.cap_nnz;
     *cap_rows = op.cap_rows;
     *ntiles = op.ntiles;
+    *wide = op.wide ? 1 : 0;
     return 0;
   }
   bool fp32() const { return fp32_; }

@@ -169,9 +169,13 @@ __device__ __forceinline__ StepScalars<ACC> step_scalars(const Ctl* __restrict__
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kBlock, 6) dual_step_kernel(const Ctl* __restrict__ ctl,
-                                                           OpView<T> K, IterView<T> it, int j) {
+// Two variants of each step kernel: WIDE = false keeps 6 CTAs per SM resident (40 registers;
+// operators of short rows, where occupancy hides the latency); WIDE = true allows 128
+// registers and unrolls the warp-per-row and segment loops twice as deep (operators of long
+// rows, whose few CTAs need more loads in flight each). TileSet::wide selects one per operator.
+template <typename T, bool WIDE>
+__global__ void __launch_bounds__(kBlock, WIDE ? 2 : 6) dual_step_kernel(
+    const Ctl* __restrict__ ctl, OpView<T> K, IterView<T> it, int j) {
   if (ctl->done) return;
   const long long t = ctl->t + j;
   if (t >= ctl->max_iter) return;
@@ -197,12 +201,13 @@ __global__ void __launch_bounds__(kBlock, 6) dual_step_kernel(const Ctl* __restr
   epi.alpha = sc.alpha;
   epi.beta = sc.beta;
   Gather1<T, ACC> g{it.Vbar};
-  run_tiles<T, ACC, 1>(K.ts, K.ptr, K.idx, K.val, g, epi);
+  run_tiles<T, ACC, 1, Gather1<T, ACC>, DualEpi<T, ACC>, false, WIDE>(K.ts, K.ptr, K.idx, K.val,
+                                                                      g, epi);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kBlock, 6) primal_step_kernel(const Ctl* __restrict__ ctl,
-                                                             OpView<T> Kt, IterView<T> it, int j) {
+template <typename T, bool WIDE>
+__global__ void __launch_bounds__(kBlock, WIDE ? 2 : 6) primal_step_kernel(
+    const Ctl* __restrict__ ctl, OpView<T> Kt, IterView<T> it, int j) {
   if (ctl->done) return;
   const long long t = ctl->t + j;
   if (t >= ctl->max_iter) return;
@@ -222,7 +227,8 @@ __global__ void __launch_bounds__(kBlock, 6) primal_step_kernel(const Ctl* __res
   epi.alpha = sc.alpha;
   epi.beta = sc.beta;
   Gather1<T, ACC> g{it.Y[p ^ 1]};
-  run_tiles<T, ACC, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
+  run_tiles<T, ACC, 1, Gather1<T, ACC>, PrimalEpi<T, ACC>, false, WIDE>(Kt.ts, Kt.ptr, Kt.idx,
+                                                                        Kt.val, g, epi);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1335,10 +1341,14 @@ void configure_kernels() {
   cudaFuncSetAttribute(eval_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_ray_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_ray_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(dual_step_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(primal_step_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(dual_step_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(primal_step_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(dual_step_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(primal_step_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(dual_step_kernel<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(primal_step_kernel<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(dual_step_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(primal_step_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(dual_step_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(primal_step_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_farkas_cols_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_farkas_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(max_norm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
@@ -1354,7 +1364,11 @@ void launch_dual_step(const Ctl* ctl, const OpView<T>& K, const IterView<T>& it,
                       cudaStream_t s) {
   if (K.ts.ntiles == 0) return;
   const size_t sm = tile_smem_bytes(K.ts, 1, sizeof(T));
-  dual_step_kernel<T><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
+  if (K.ts.wide) {
+    dual_step_kernel<T, true><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
+  } else {
+    dual_step_kernel<T, false><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
+  }
 }
 
 template <typename T>
@@ -1362,7 +1376,11 @@ void launch_primal_step(const Ctl* ctl, const OpView<T>& Kt, const IterView<T>& 
                         int grid, cudaStream_t s) {
   if (Kt.ts.ntiles == 0) return;
   const size_t sm = tile_smem_bytes(Kt.ts, 1, sizeof(T));
-  primal_step_kernel<T><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
+  if (Kt.ts.wide) {
+    primal_step_kernel<T, true><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
+  } else {
+    primal_step_kernel<T, false><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
+  }
 }
 
 template <typename T>

@@ -106,7 +106,9 @@ __device__ __forceinline__ void block_reduce_acc(ACC (&v)[K], ACC* scratch, ACC 
 //      void long_row(int lrow, int r, const ACC (&s)[NV]) for a split row (thread 0 of the CTA
 //      that completes it).
 // MAXRED: each row's products are combined by max instead of + (norm statistics).
-template <typename T, typename ACC, int NV, typename Prod, typename Epi, bool MAXRED = false>
+// WIDE: unroll the warp-per-row loop 8 deep (4 otherwise) and the segment loop 4 deep (2).
+template <typename T, typename ACC, int NV, typename Prod, typename Epi, bool MAXRED = false,
+          bool WIDE = false>
 __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restrict__ ptr,
                                           const int* __restrict__ idx,
                                           const T* __restrict__ val, const Prod& prod, Epi& epi) {
@@ -207,8 +209,7 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
 #pragma unroll
           for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
         }
-#pragma unroll 4
-        for (int q = a0 + 4 * lane; q < a1; q += 128) {
+        auto quad = [&](int q) {
           T a[4];
           Vec4<T>::load(val, q, a);
           const int4 j = __ldg(reinterpret_cast<const int4*>(idx + q));
@@ -219,6 +220,13 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
             s[v] = combine<MAXRED>(s[v], prod(v, a[2], j.z));
             s[v] = combine<MAXRED>(s[v], prod(v, a[3], j.w));
           }
+        };
+        if constexpr (WIDE) {
+#pragma unroll 8
+          for (int q = a0 + 4 * lane; q < a1; q += 128) quad(q);
+        } else {
+#pragma unroll 4
+          for (int q = a0 + 4 * lane; q < a1; q += 128) quad(q);
         }
         if (a1 + lane < e) {
           const int q = a1 + lane;
@@ -256,8 +264,7 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
 #pragma unroll
           for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
         }
-#pragma unroll 2
-        for (int q = a0 + 4 * tid; q < a1; q += 4 * kBlock) {
+        auto quad = [&](int q) {
           T a[4];
           Vec4<T>::load(val, q, a);
           const int4 j = __ldg(reinterpret_cast<const int4*>(idx + q));
@@ -268,6 +275,13 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
             s[v] = combine<MAXRED>(s[v], prod(v, a[2], j.z));
             s[v] = combine<MAXRED>(s[v], prod(v, a[3], j.w));
           }
+        };
+        if constexpr (WIDE) {
+#pragma unroll 4
+          for (int q = a0 + 4 * tid; q < a1; q += 4 * kBlock) quad(q);
+        } else {
+#pragma unroll 2
+          for (int q = a0 + 4 * tid; q < a1; q += 4 * kBlock) quad(q);
         }
         for (int q = a1 + tid; q < k1; q += kBlock) {
           const T a = ldg(val + q);

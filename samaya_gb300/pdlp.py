@@ -124,14 +124,14 @@ class PdlpSolver:
         return a.value, b.value, c.value
 
     def tile_shapes(self):
-        """{"A": (nonzeros per tile, rows per short-row tile, tiles), "At": ...} in use."""
+        """{"A": (nonzeros per tile, rows per short-row tile, tiles, deep-unroll variant),
+        "At": ...} in use."""
         out = {}
         for name, t in (("A", 0), ("At", 1)):
-            a, b, c = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
-            _native.check(self._lib.sg_pdlp_tile_shape(self._h, t, ctypes.byref(a),
-                                                       ctypes.byref(b), ctypes.byref(c)),
+            v = [ctypes.c_int(0) for _ in range(4)]
+            _native.check(self._lib.sg_pdlp_tile_shape(self._h, t, *[ctypes.byref(x) for x in v]),
                           "sg_pdlp_tile_shape")
-            out[name] = (a.value, b.value, c.value)
+            out[name] = (v[0].value, v[1].value, v[2].value, bool(v[3].value))
         return out
 
     def solve(self, x_out: np.ndarray | None = None, y_out: np.ndarray | None = None,
