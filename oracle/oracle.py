@@ -2,8 +2,9 @@
 
 ctypes binding of ``oracle/pdlp_oracle.c``, the plain-C restatement of the reference solver's
 CPU PDLP path (``src/lp/pdlp.cpp`` of the reference).  Only ``tests/``,
-``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import this module, as the checker
-or as the timed CPU baseline; the product package ``samaya_gb300`` never does.
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import this module, as the
+result the GPU engine is compared with or as the timed CPU baseline; the product package
+``samaya_gb300`` never does.
 
 Pinned bit-for-bit against the reference's own compiled code through the fixtures in
 ``tests/golden/`` (``tests/test_oracle_pin.py``).

@@ -1,7 +1,7 @@
 /*
  * ORACLE — test infrastructure only. A plain-C restatement of the reference solver's CPU PDLP
- * path, used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker and
- * as the timed CPU baseline. The product path (samaya_gb300/) never links, loads or calls it.
+ * path, used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the result the
+ * GPU engine is compared with and as the timed CPU baseline. The product path (samaya_gb300/) never links, loads or calls it.
  *
  * Pinned: tests/test_oracle_pin.py checks this restatement bit-for-bit (iteration counts, x, y,
  * residuals, rays) against golden fixtures produced by the reference's own compiled code

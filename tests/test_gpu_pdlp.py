@@ -140,7 +140,7 @@ def test_infeasible_and_unbounded_detection(engine):
 
 def test_random_sparse_lp_objective_vs_dual_simplex(engine):
     """The 200 x 500 random sparse LPs at 1e-4: objective within 1e-4 relative of the reference
-    dual simplex (the benchmark spec's bar for the plain path)."""
+    dual simplex (the bar for the plain FP64 path at 1e-4)."""
     for case in load_group("config0_small"):
         r = solve(engine, case)
         assert r.status == engine.OPTIMAL
