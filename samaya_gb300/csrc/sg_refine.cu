@@ -230,28 +230,46 @@ __global__ void ir_reset_kernel(Ctl* c, double tol, long long max_iter, int stal
   c->no_detect = 1;
 }
 
-__global__ void switch_vectors_kernel(const Ctl* __restrict__ c32, IterView<float> it32,
-                                      IterView<double> it64) {
-  const int cur = static_cast<int>(c32->t & 1);
-  const bool avg = c32->result_average != 0;
-  const float* w = avg ? it32.Verg : it32.V[cur];
-  const float* z = avg ? it32.Yerg : it32.Y[cur];
-  const int nt = it64.n + it64.m;
+// Precision switch: the whole FP32 state as doubles (both ping-pong iterates, the
+// extrapolated point, the averages and the restart point), so the FP64 PDLP continues the same
+// run rather than restarting at its answer.
+__global__ void continue_vectors_kernel(IterView<float> a, IterView<double> b) {
+  const int nt = b.n + b.m;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
-    const double v = static_cast<double>(w[k]);
-    it64.V[0][k] = v;
-    it64.V[1][k] = v;
-    it64.Vbar[k] = v;
-    it64.Verg[k] = v;
-    it64.Vrst[k] = v;
-    if (k < it64.m) {
-      const double yv = static_cast<double>(z[k]);
-      it64.Y[0][k] = yv;
-      it64.Y[1][k] = yv;
-      it64.Yerg[k] = yv;
-      it64.Yrst[k] = yv;
+    b.V[0][k] = static_cast<double>(a.V[0][k]);
+    b.V[1][k] = static_cast<double>(a.V[1][k]);
+    b.Vbar[k] = static_cast<double>(a.Vbar[k]);
+    b.Verg[k] = static_cast<double>(a.Verg[k]);
+    b.Vrst[k] = static_cast<double>(a.Vrst[k]);
+    if (k < b.m) {
+      b.Y[0][k] = static_cast<double>(a.Y[0][k]);
+      b.Y[1][k] = static_cast<double>(a.Y[1][k]);
+      b.Yerg[k] = static_cast<double>(a.Yerg[k]);
+      b.Yrst[k] = static_cast<double>(a.Yrst[k]);
     }
   }
+}
+
+// The FP64 control block continues the FP32 one: iteration counters (parity and the averages'
+// weights), primal weight and steps; the restart references start afresh because the FP64
+// evaluation measures the original problem and the FP32 one the equilibrated problem.
+__global__ void continue_ctl_kernel(Ctl* c, const Ctl* __restrict__ c32) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  c->t = c32->t;
+  c->k = c32->k;
+  c->kkt_at_restart = INFINITY;
+  c->kkt_previous = INFINITY;
+  c->status = kRunning;
+  c->done = 0;
+  c->result_average = 0;
+  c->restart_pending = 0;
+  c->detect_pending = 0;
+  c->iterations = 0;
+  c->restarts = 0;
+  c->evaluations = 0;
+  c->omega = c32->omega;
+  c->tau = c->eta / c->omega;
+  c->sigma = c->eta * c->omega;
 }
 
 // The FP64 iterates, average and restart point = the FP64 point V[0], Y[0].
@@ -344,11 +362,11 @@ void launch_ir_reset(Ctl* c32, double tol, long long max_iter, int stall_limit,
   ir_reset_kernel<<<1, 32, 0, s>>>(c32, tol, max_iter, stall_limit);
 }
 
-void launch_switch(Ctl* c64, const Ctl* c32, const IterView<float>& it32,
-                   const IterView<double>& it64, long long max_iter, cudaStream_t s) {
-  switch_vectors_kernel<<<grid_for(static_cast<long long>(it64.n) + it64.m, 4096), kBlock, 0,
-                          s>>>(c32, it32, it64);
-  switch_ctl_kernel<<<1, 32, 0, s>>>(c64, c32, 1.0, max_iter);
+void launch_continue(Ctl* c64, const Ctl* c32, const IterView<float>& it32,
+                     const IterView<double>& it64, cudaStream_t s) {
+  continue_vectors_kernel<<<grid_for(static_cast<long long>(it64.n) + it64.m, 4096), kBlock, 0,
+                            s>>>(it32, it64);
+  continue_ctl_kernel<<<1, 32, 0, s>>>(c64, c32);
 }
 
 void launch_restart_at_point(Ctl* c64, double omega, const IterView<double>& it64,

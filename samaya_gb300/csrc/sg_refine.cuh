@@ -40,10 +40,10 @@ void launch_ir_reset(Ctl* c32, double tol, long long max_iter, int stall_limit,
 constexpr int kStallEvaluations = 64;
 void launch_norm_into(const double* x, long long len, const RedView& red, double* out,
                       cudaStream_t s);
-// Precision switch: the FP64 iterates, average and restart point = the FP32 answer; the FP64
-// control block restarted (t = k = 0, no restart history) with the FP32 solve's primal weight.
-void launch_switch(Ctl* c64, const Ctl* c32, const IterView<float>& it32,
-                   const IterView<double>& it64, long long max_iter, cudaStream_t s);
+// Precision switch: the FP64 state = the FP32 state (iterates, extrapolated point, averages,
+// restart point; iteration counters and primal weight), so the FP64 PDLP continues the run.
+void launch_continue(Ctl* c64, const Ctl* c32, const IterView<float>& it32,
+                     const IterView<double>& it64, cudaStream_t s);
 // The same from the FP64 point V[0], Y[0] of it64 with primal weight `omega`.
 void launch_restart_at_point(Ctl* c64, double omega, const IterView<double>& it64,
                              long long max_iter, cudaStream_t s);
