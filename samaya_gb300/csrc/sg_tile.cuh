@@ -101,6 +101,48 @@ __device__ __forceinline__ void block_reduce_acc(ACC (&v)[K], ACC* scratch, ACC 
   __syncthreads();
 }
 
+// Two consecutive nonzeros (values and indices) at an even position, in one load each.
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<float> {
+  __device__ __forceinline__ static float2 load(const float* v, int q) {
+    return __ldg(reinterpret_cast<const float2*>(v + q));
+  }
+};
+template <>
+struct Vec2<double> {
+  __device__ __forceinline__ static double2 load(const double* v, int q) {
+    return __ldg(reinterpret_cast<const double2*>(v + q));
+  }
+};
+
+// s += the products of a short row's nonzeros [b, e), in order. A row of two nonzeros at an
+// even position (every column of a transportation LP) is read with one load for its indices and
+// one for its values.
+template <typename T, int NV, bool MAXRED, typename Prod, typename ACC>
+__device__ __forceinline__ void short_row_sum(int b, int e, const int* __restrict__ idx,
+                                              const T* __restrict__ val, const Prod& prod,
+                                              ACC (&s)[NV]) {
+  if (e - b == 2 && (b & 1) == 0) {
+    const int2 j = __ldg(reinterpret_cast<const int2*>(idx + b));
+    const auto a = Vec2<T>::load(val, b);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      s[v] = combine<MAXRED>(s[v], prod(v, a.x, j.x));
+      s[v] = combine<MAXRED>(s[v], prod(v, a.y, j.y));
+    }
+    return;
+  }
+#pragma unroll 4
+  for (int q = b; q < e; ++q) {
+    const T a = ldg(val + q);
+    const int j = ldg(idx + q);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
+  }
+}
+
 // Prod: ACC operator()(int v, T val, int col) const — the v-th product of a nonzero.
 // Epi: void row(int r, const ACC (&s)[NV]) for rows of kind-0 tiles (lane 0 of the row's team),
 //      void long_row(int lrow, int r, const ACC (&s)[NV]) for a split row (thread 0 of the CTA
@@ -139,13 +181,7 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
             ACC s[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) s[v] = ACC(0);
-#pragma unroll 4
-            for (int q = b; q < e; ++q) {
-              const T a = ldg(val + q);
-              const int j = ldg(idx + q);
-#pragma unroll
-              for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
-            }
+            short_row_sum<T, NV, MAXRED>(b, e, idx, val, prod, s);
             epi.row(tile.r0 + lr, s, pre);
           }
         } else {
@@ -153,13 +189,7 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
             ACC s[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) s[v] = ACC(0);
-#pragma unroll 4
-            for (int q = b; q < e; ++q) {
-              const T a = ldg(val + q);
-              const int j = ldg(idx + q);
-#pragma unroll
-              for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
-            }
+            short_row_sum<T, NV, MAXRED>(b, e, idx, val, prod, s);
             epi.row(tile.r0 + lr, s);
           }
         }
