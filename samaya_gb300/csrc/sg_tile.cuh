@@ -117,25 +117,32 @@ struct Vec2<double> {
   }
 };
 
-// s += the products of a short row's nonzeros [b, e), in order. A row of two nonzeros at an
-// even position (every column of a transportation LP) is read with one load for its indices and
-// one for its values.
+// s += the products of a short row's nonzeros [b, e), in order: an odd first position alone,
+// then pairs at even positions read with one load for two indices and one for two values (a
+// column of a transportation LP is one pair), then a last single nonzero.
 template <typename T, int NV, bool MAXRED, typename Prod, typename ACC>
 __device__ __forceinline__ void short_row_sum(int b, int e, const int* __restrict__ idx,
                                               const T* __restrict__ val, const Prod& prod,
                                               ACC (&s)[NV]) {
-  if (e - b == 2 && (b & 1) == 0) {
-    const int2 j = __ldg(reinterpret_cast<const int2*>(idx + b));
-    const auto a = Vec2<T>::load(val, b);
+  int q = b;
+  if ((q & 1) != 0 && q < e) {
+    const T a = ldg(val + q);
+    const int j = ldg(idx + q);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
+    ++q;
+  }
+#pragma unroll 2
+  for (; q + 1 < e; q += 2) {
+    const int2 j = __ldg(reinterpret_cast<const int2*>(idx + q));
+    const auto a = Vec2<T>::load(val, q);
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       s[v] = combine<MAXRED>(s[v], prod(v, a.x, j.x));
       s[v] = combine<MAXRED>(s[v], prod(v, a.y, j.y));
     }
-    return;
   }
-#pragma unroll 4
-  for (int q = b; q < e; ++q) {
+  if (q < e) {
     const T a = ldg(val + q);
     const int j = ldg(idx + q);
 #pragma unroll
