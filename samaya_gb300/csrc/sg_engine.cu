@@ -172,7 +172,8 @@ Engine::~Engine() {
     dfree(*p);
   }
   for (double** p : {&cost_orig_, &lower_orig_, &upper_orig_, &cost_ev_, &lower_ev_, &upper_ev_,
-                     &rhs_ev_, &cs_, &rs_, &cn_, &rn_, &pu_, &pv_, &u0_, &scratch_n_, &x_out_,
+                     &rhs_ev_, &cs_, &rs_, &inv_cs_, &inv_rs_, &cn_, &rn_, &pu_, &pv_, &u0_,
+                     &scratch_n_, &x_out_,
                      &y_out_, &ray_out_, &partial_, &long_terms_}) {
     dfree(*p);
   }
@@ -586,7 +587,8 @@ int Engine::alloc_all(std::string* err) {
     SG_TRY(dalloc(p, nt));
   }
   for (double** p : {&rhs_ev_, &rs_, &rn_, &pu_, &u0_, &y_out_, &ray_out_}) SG_TRY(dalloc(p, m));
-  for (double** p : {&cs_, &cn_, &pv_}) SG_TRY(dalloc(p, static_cast<size_t>(n_)));
+  for (double** p : {&cs_, &cn_, &pv_, &inv_cs_}) SG_TRY(dalloc(p, static_cast<size_t>(n_)));
+  SG_TRY(dalloc(&inv_rs_, m));
   SG_TRY(dalloc(&partial_, static_cast<size_t>(4096) * kMaxSums));
   SG_TRY(dalloc(&counter_, 8));
   SG_TRY(cudaMemsetAsync(counter_, 0, 8 * sizeof(unsigned), stream_));
@@ -623,6 +625,8 @@ EvalView Engine::eval_view() const {
   EvalView ev;
   ev.cs = cs_;
   ev.rs = rs_;
+  ev.inv_cs = inv_cs_;
+  ev.inv_rs = inv_rs_;
   ev.cost = cost_ev_;
   ev.lower = lower_ev_;
   ev.upper = upper_ev_;
@@ -697,6 +701,8 @@ int Engine::setup_device(const double* rhs_orig) {
     }
   }
   launch_apply_scaling(K, Kt, rs_, cs_, nnz_, s);
+  launch_reciprocals(cs_, inv_cs_, n_, s);
+  launch_reciprocals(rs_, inv_rs_, m_, s);
   launch_scale_vectors(n_, m_, cs_, rs_, cost_orig_, lower_orig_, upper_orig_, nullptr,
                        it64_.cost, it64_.lower, it64_.upper, nullptr, s);
   if (m_ > 0) {
@@ -780,6 +786,8 @@ EvalView Engine::inner_eval_view() const {
   EvalView ev;
   ev.cs = ones_n_;
   ev.rs = ones_m_;
+  ev.inv_cs = ones_n_;
+  ev.inv_rs = ones_m_;
   ev.cost = cost_in_;
   ev.lower = lower_in_;
   ev.upper = upper_in_;
@@ -1243,6 +1251,8 @@ int Engine::seam_set_original(const double* cs, const double* rs, const double* 
   }
   SG_TRY(cudaMemcpyAsync(cs_, cs, static_cast<size_t>(n_) * sizeof(double), cudaMemcpyHostToDevice, s));
   SG_TRY(cudaMemcpyAsync(rs_, rs, static_cast<size_t>(m_) * sizeof(double), cudaMemcpyHostToDevice, s));
+  launch_reciprocals(cs_, inv_cs_, n_, s);
+  launch_reciprocals(rs_, inv_rs_, m_, s);
   SG_TRY(cudaMemcpyAsync(cost_ev_, cost, nt * sizeof(double), cudaMemcpyHostToDevice, s));
   SG_TRY(cudaMemcpyAsync(lower_ev_, lower, nt * sizeof(double), cudaMemcpyHostToDevice, s));
   SG_TRY(cudaMemcpyAsync(upper_ev_, upper, nt * sizeof(double), cudaMemcpyHostToDevice, s));

@@ -208,6 +208,8 @@ class Engine {
   double* rhs_ev_ = nullptr;      // m, null when zero
   double* cs_ = nullptr;
   double* rs_ = nullptr;
+  double* inv_cs_ = nullptr;      // 1 / cs_, 1 / rs_ (the evaluation's multipliers)
+  double* inv_rs_ = nullptr;
   double* cn_ = nullptr;
   double* rn_ = nullptr;
   double* pu_ = nullptr;          // power iteration vectors

@@ -21,6 +21,31 @@ __device__ __forceinline__ T clampv(T v, T lo, T hi) {
   return fmin(fmax(v, lo), hi);
 }
 
+// Doubles compared through their bit patterns mapped to a signed integer order, on the integer
+// pipe (GB300's FP64 pipe is small): the same as fmin(fmax(v, lo), hi) for numbers (with
+// -0 ordered below +0).
+__device__ __forceinline__ long long order_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+
+template <>
+__device__ __forceinline__ double clampv<double>(double v, double lo, double hi) {
+  const double r = order_key(v) < order_key(lo) ? lo : v;
+  return order_key(r) > order_key(hi) ? hi : r;
+}
+
+// The extrapolated point 2 v+ - v (one fused operation in FP64).
+template <typename T>
+__device__ __forceinline__ T extrapolate(T vn, T v) {
+  return vn + (vn - v);
+}
+
+template <>
+__device__ __forceinline__ double extrapolate<double>(double vn, double v) {
+  return fma(2.0, vn, -v);
+}
+
 // lambda of the reduced cost g for a variable with bounds [lo, up] (pdlp.cpp:455-465).
 __device__ __forceinline__ double bound_part(double g, double lo, double up) {
   const bool hl = lo > -INFINITY;
@@ -91,7 +116,7 @@ struct DualEpi {
     ACC rn = p.r - tau * (p.c - yn);
     rn = clampv<ACC>(rn, p.l, p.u);
     vr_new[i] = static_cast<T>(rn);
-    vbar_r[i] = static_cast<T>(rn + (rn - p.r));
+    vbar_r[i] = static_cast<T>(extrapolate<ACC>(rn, p.r));
     yerg[i] = static_cast<T>(beta * p.yerg + alpha * yn);
     verg_r[i] = static_cast<T>(beta * p.rerg + alpha * rn);
   }
@@ -125,7 +150,7 @@ struct PrimalEpi {
     ACC xn = p.x - tau * (p.c + s[0]);
     xn = clampv<ACC>(xn, p.l, p.u);
     x_new[j] = static_cast<T>(xn);
-    xbar[j] = static_cast<T>(xn + (xn - p.x));
+    xbar[j] = static_cast<T>(extrapolate<ACC>(xn, p.x));
     xerg[j] = static_cast<T>(beta * p.xerg + alpha * xn);
   }
   __device__ __forceinline__ void row(int j, const ACC (&s)[1]) { row(j, s, load(j)); }
@@ -249,6 +274,7 @@ struct EvalRowEpi {
   double* long_terms;
   __device__ __forceinline__ void terms(int i, const double (&s)[2], double (&a)[kEvalSums]) {
     const double rs = ev.rs[i];
+    const double irs = ev.inv_rs[i];
     const double c = ev.cost[n + i];
     const double lo = ev.lower[n + i];
     const double up = ev.upper[n + i];
@@ -257,10 +283,10 @@ struct EvalRowEpi {
     for (int w = 0; w < 2; ++w) {
       const double vrv = static_cast<double>(vr[w][i]);
       const double yv = static_cast<double>(y[w][i]);
-      const double value = vrv / rs;
+      const double value = vrv * irs;
       const double yo = yv * rs;
       const double g = c - yo;
-      const double e = s[w] / rs - value - q;
+      const double e = s[w] * irs - value - q;
       a[w * 7 + 0] += e * e;
       a[w * 7 + 5] += value * value;
       a[w * 7 + 6] += yo * yo;
@@ -299,6 +325,7 @@ struct EvalColEpi {
   double* long_terms;
   __device__ __forceinline__ void terms(int j, const double (&s)[2], double (&a)[kEvalSums]) {
     const double cs = ev.cs[j];
+    const double ics = ev.inv_cs[j];
     const double c = ev.cost[j];
     const double lo = ev.lower[j];
     const double up = ev.upper[j];
@@ -306,7 +333,7 @@ struct EvalColEpi {
     for (int w = 0; w < 2; ++w) {
       const double xv = static_cast<double>(x[w][j]);
       const double value = xv * cs;
-      const double g = c + (m > 0 ? s[w] / cs : 0.0);
+      const double g = c + (m > 0 ? s[w] * ics : 0.0);
       a[w * 7 + 4] += value * value;
       a[w * 7 + 2] += c * value;
       const double lam = bound_part(g, lo, up);
@@ -1451,6 +1478,18 @@ void launch_setup_norms(Ctl* ctl, const OpView<double>& K, const OpView<double>&
   const int nt = K.rows + Kt.rows;
   sum_sq_kernel<<<vec_grid(nt) < 1024 ? vec_grid(nt) : 1024, kBlock, 0, s>>>(cost, nt, red,
                                                                           &ctl->c_norm);
+}
+
+__global__ void reciprocal_kernel(const double* a, double* out, int count) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+    out[k] = 1.0 / a[k];
+  }
+}
+
+void launch_reciprocals(const double* a, double* out, int count, cudaStream_t s) {
+  if (count <= 0) return;
+  reciprocal_kernel<<<vec_grid(count) < 1024 ? vec_grid(count) : 1024, kBlock, 0, s>>>(a, out,
+                                                                                     count);
 }
 
 void launch_ruiz_pass(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt, double* rs,

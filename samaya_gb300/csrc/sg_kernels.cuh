@@ -41,6 +41,8 @@ struct EvalView {
   const double* lower;   // n + m
   const double* upper;   // n + m
   const double* rhs;     // m (null: zero)
+  const double* inv_cs;  // 1 / cs and 1 / rs (the evaluation multiplies: divisions would load
+  const double* inv_rs;  // GB300's small FP64 pipe)
 };
 
 // Scratch of the grid reductions.
@@ -78,6 +80,8 @@ void launch_extract(const Ctl* ctl, const IterView<T>& it, const EvalView& ev, d
 void launch_setup_norms(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt,
                         const double* cost, const RedView& red, int grid_k, int grid_t,
                         cudaStream_t s);
+// out[k] = 1 / a[k] for k < count.
+void launch_reciprocals(const double* a, double* out, int count, cudaStream_t s);
 void launch_ruiz_pass(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt, double* rs,
                       double* cs, double* rn, double* cn, const RedView& red, int grid_k,
                       int grid_t, cudaStream_t s);
