@@ -78,10 +78,13 @@ def parse():
                     help="iteration cap of the --profile solve (-1: none)")
     ap.add_argument("--tol", type=float, default=1e-8,
                     help="relative KKT tolerance of the single-LP workloads")
-    ap.add_argument("--algorithm", default="enhanced", choices=["enhanced", "reference"],
+    ap.add_argument("--algorithm", default="auto", choices=["auto", "enhanced", "reference"],
                     help="enhanced: inf-norm Ruiz + Pock-Chambolle, primal weight |c|/|b|; "
-                         "reference: samaya's PDLP step for step")
+                         "reference: samaya's PDLP step for step; auto: the faster one for "
+                         "the workload (reference on the random sparse LPs, enhanced otherwise)")
     args = ap.parse_args()
+    if args.algorithm == "auto":
+        args.algorithm = "reference" if args.workload in ("random", "batchA") else "enhanced"
     global TOL
     TOL = args.tol
     return args

@@ -365,14 +365,20 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
   T* st = reinterpret_cast<T*>(b.state) + b.state_off[inst];
   // Per-instance state (storage type T): V0 V1 Vbar Verg Vrst c l u (nt each), Y0 Y1 Yerg Yrst
   // (m each).
-  T* V[2] = {st, st + nt};
+  // Ping-pong pairs picked by selects (a runtime index into a local array puts it in local
+  // memory).
+  T* const V0 = st;
+  T* const V1 = st + nt;
   T* Vbar = st + 2 * nt;
   T* Verg = st + 3 * nt;
   T* Vrst = st + 4 * nt;
   T* ce = st + 5 * nt;
   T* le = st + 6 * nt;
   T* ue = st + 7 * nt;
-  T* Y[2] = {st + 8 * nt, st + 8 * nt + m};
+  T* const Y0 = st + 8 * nt;
+  T* const Y1 = st + 8 * nt + m;
+  auto V = [&](int q) { return q ? V1 : V0; };
+  auto Y = [&](int q) { return q ? Y1 : Y0; };
   T* Yerg = st + 8 * nt + 2 * m;
   T* Yrst = st + 8 * nt + 3 * m;
   // Scaled problem, zero iterates, ||c||.
@@ -396,8 +402,8 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
     le[k] = static_cast<T>(l);
     ue[k] = static_cast<T>(u);
     cc += cost0[k] * cost0[k];
-    V[0][k] = V[1][k] = Vbar[k] = Verg[k] = Vrst[k] = T(0);
-    if (k < m) Y[0][k] = Y[1][k] = Yerg[k] = Yrst[k] = T(0);
+    V0[k] = V1[k] = Vbar[k] = Verg[k] = Vrst[k] = T(0);
+    if (k < m) Y0[k] = Y1[k] = Yerg[k] = Yrst[k] = T(0);
   }
   double nrm[3] = {cc, c2, b2};
   bsums<3>(nrm, sh);
@@ -434,10 +440,10 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
           return static_cast<double>(a) * static_cast<double>(x[j]);
         }
       } gx{Vbar};
-      const T* yv = Y[p];
-      T* yn = Y[p ^ 1];
-      const T* vr = V[p] + n;
-      T* vrn = V[p ^ 1] + n;
+      const T* yv = Y(p);
+      T* yn = Y(p ^ 1);
+      const T* vr = V(p) + n;
+      T* vrn = V(p ^ 1) + n;
       T* vbr = Vbar + n;
       auto f = [&](int i, double s) {
         const T res = static_cast<T>(s) - vbr[i];
@@ -461,9 +467,9 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
         __device__ double operator()(T a, int i) const {
           return static_cast<double>(a) * static_cast<double>(y[i]);
         }
-      } gy{Y[p ^ 1]};
-      const T* x = V[p];
-      T* xn = V[p ^ 1];
+      } gy{Y(p ^ 1)};
+      const T* x = V(p);
+      T* xn = V(p ^ 1);
       auto f = [&](int j, double s) {
         const T xo = x[j];
         T v = xo - ttau * (ce[j] + static_cast<T>(s));
@@ -480,59 +486,71 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
     if (t % 64 != 0 && t != max_iter) continue;
     // Evaluation of the current and the average iterate (pdlp.cpp:411-488), original space.
     const int cur = static_cast<int>(t & 1);
+    // One iterate's sums (7 evaluation sums, restart distances of v and y) into e with
+    // constant indices, so they stay in registers; called for the current and the average
+    // iterate.
+    struct G2 {
+      const T* x;
+      __device__ double operator()(T v, int j) const {
+        return static_cast<double>(v) * static_cast<double>(x[j]);
+      }
+    };
+    auto eval_one = [&](const T* vv, const T* yy, double (&e)[9]) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) e[q] = 0.0;
+      G2 gx{vv};
+      auto fr = [&](int i, double s) {
+        const double r_s = rs[i];
+        const double value = static_cast<double>(vv[n + i]) / r_s;
+        const double yo2 = static_cast<double>(yy[i]) * r_s;
+        const double c = cost0[n + i];
+        const double g2 = c - yo2;
+        const double ep = s / r_s - value;
+        e[0] += ep * ep;
+        e[5] += value * value;
+        e[6] += yo2 * yo2;
+        e[2] += c * value;
+        const double lam = lam_of(g2, lo0[n + i], up0[n + i]);
+        e[1] += (g2 - lam) * (g2 - lam);
+        if (lam > 0.0) e[3] += lam * lo0[n + i];
+        if (lam < 0.0) e[3] += lam * up0[n + i];
+        const double dv = static_cast<double>(vv[n + i]) - static_cast<double>(Vrst[n + i]);
+        const double dy = static_cast<double>(yy[i]) - static_cast<double>(Yrst[i]);
+        e[7] += dv * dv;
+        e[8] += dy * dy;
+      };
+      block_rows<false>(m, kp, ki, kv, gx, fr);
+      G2 gy{yy};
+      auto fc = [&](int j, double s) {
+        const double c_s = cs[j];
+        const double value = static_cast<double>(vv[j]) * c_s;
+        const double c = cost0[j];
+        const double g2 = c + (m > 0 ? s / c_s : 0.0);
+        e[4] += value * value;
+        e[2] += c * value;
+        const double lam = lam_of(g2, lo0[j], up0[j]);
+        e[1] += (g2 - lam) * (g2 - lam);
+        if (lam > 0.0) e[3] += lam * lo0[j];
+        if (lam < 0.0) e[3] += lam * up0[j];
+        const double dv = static_cast<double>(vv[j]) - static_cast<double>(Vrst[j]);
+        e[7] += dv * dv;
+      };
+      block_rows<false>(n, tp, ti, tv, gy, fc);
+    };
+    double ec[9], ea[9];
+    eval_one(V(cur), Y(cur), ec);
+    eval_one(Verg, Yerg, ea);
+    // a: the current iterate's 7 sums, the average's 7, then the distances (v, y) of each.
     double a[18];
 #pragma unroll
-    for (int q = 0; q < 18; ++q) a[q] = 0.0;
-    {
-      struct G2 {
-        const T* x;
-        __device__ double operator()(T v, int j) const {
-          return static_cast<double>(v) * static_cast<double>(x[j]);
-        }
-      };
-      for (int w = 0; w < 2; ++w) {
-        const T* vv = w == 0 ? V[cur] : Verg;
-        const T* yy = w == 0 ? Y[cur] : Yerg;
-        G2 gx{vv};
-        auto fr = [&](int i, double s) {
-          const double r_s = rs[i];
-          const double value = static_cast<double>(vv[n + i]) / r_s;
-          const double yo2 = static_cast<double>(yy[i]) * r_s;
-          const double c = cost0[n + i];
-          const double g2 = c - yo2;
-          const double e = s / r_s - value;
-          a[w * 7 + 0] += e * e;
-          a[w * 7 + 5] += value * value;
-          a[w * 7 + 6] += yo2 * yo2;
-          a[w * 7 + 2] += c * value;
-          const double lam = lam_of(g2, lo0[n + i], up0[n + i]);
-          a[w * 7 + 1] += (g2 - lam) * (g2 - lam);
-          if (lam > 0.0) a[w * 7 + 3] += lam * lo0[n + i];
-          if (lam < 0.0) a[w * 7 + 3] += lam * up0[n + i];
-          const double dv = static_cast<double>(vv[n + i]) - static_cast<double>(Vrst[n + i]);
-          const double dy = static_cast<double>(yy[i]) - static_cast<double>(Yrst[i]);
-          a[14 + 2 * w] += dv * dv;
-          a[15 + 2 * w] += dy * dy;
-        };
-        block_rows<false>(m, kp, ki, kv, gx, fr);
-        G2 gy{yy};
-        auto fc = [&](int j, double s) {
-          const double c_s = cs[j];
-          const double value = static_cast<double>(vv[j]) * c_s;
-          const double c = cost0[j];
-          const double g2 = c + (m > 0 ? s / c_s : 0.0);
-          a[w * 7 + 4] += value * value;
-          a[w * 7 + 2] += c * value;
-          const double lam = lam_of(g2, lo0[j], up0[j]);
-          a[w * 7 + 1] += (g2 - lam) * (g2 - lam);
-          if (lam > 0.0) a[w * 7 + 3] += lam * lo0[j];
-          if (lam < 0.0) a[w * 7 + 3] += lam * up0[j];
-          const double dv = static_cast<double>(vv[j]) - static_cast<double>(Vrst[j]);
-          a[14 + 2 * w] += dv * dv;
-        };
-        block_rows<false>(n, tp, ti, tv, gy, fc);
-      }
+    for (int q = 0; q < 7; ++q) {
+      a[q] = ec[q];
+      a[7 + q] = ea[q];
     }
+    a[14] = ec[7];
+    a[15] = ec[8];
+    a[16] = ea[7];
+    a[17] = ea[8];
     bsums<18>(a, sh);
     const Meas mc = finish7(a, mi.a_norm_max_col, mi.at_norm_max_row, c_norm, m);
     const Meas ma = finish7(a + 7, mi.a_norm_max_col, mi.at_norm_max_row, c_norm, m);
@@ -565,19 +583,19 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
         tau = eta / omega;
         sigma = eta * omega;
       }
-      const T* vc = to_avg ? Verg : V[cur];
-      const T* yc = to_avg ? Yerg : Y[cur];
+      const T* vc = to_avg ? Verg : V(cur);
+      const T* yc = to_avg ? Yerg : Y(cur);
       for (int k = threadIdx.x; k < nt; k += kBT) {
         const T v = vc[k];
         Vrst[k] = v;
-        V[0][k] = v;
-        V[1][k] = v;
+        V0[k] = v;
+        V1[k] = v;
         Vbar[k] = v;
         if (k < m) {
           const T y = yc[k];
           Yrst[k] = y;
-          Y[0][k] = y;
-          Y[1][k] = y;
+          Y0[k] = y;
+          Y1[k] = y;
         }
       }
       __syncthreads();
@@ -598,8 +616,8 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
   }
   // Answer in the LpProblem's space.
   const int cur = static_cast<int>(t & 1);
-  const T* vv = result_avg ? Verg : V[cur];
-  const T* yy = result_avg ? Yerg : Y[cur];
+  const T* vv = result_avg ? Verg : V(cur);
+  const T* yy = result_avg ? Yerg : Y(cur);
   double* xo = b.x_out + vo;
   double* yo2 = b.y_out + yo;
   for (int k = threadIdx.x; k < nt; k += kBT) {

@@ -194,12 +194,19 @@ __device__ __forceinline__ StepScalars<ACC> step_scalars(const Ctl* __restrict__
   }
 }
 
-// Two variants of each step kernel: WIDE = false keeps 6 CTAs per SM resident (40 registers;
-// operators of short rows, where occupancy hides the latency); WIDE = true allows 128
-// registers and unrolls the warp-per-row and segment loops twice as deep (operators of long
-// rows, whose few CTAs need more loads in flight each). TileSet::wide selects one per operator.
+// Two variants of each step kernel: WIDE = false keeps many CTAs per SM resident (operators of
+// short rows, where occupancy hides the latency): 6 (40 registers) in FP32; in FP64, whose
+// epilogues spilled at 40 registers, 5 (48) for the primal step and 4 (64) for the dual step
+// (nine FP64 row values preloaded). WIDE = true allows 128 registers and unrolls the
+// warp-per-row and segment loops twice as deep (operators of long rows, whose few CTAs need
+// more loads in flight each). TileSet::wide selects one per operator.
+template <typename T>
+constexpr int step_min_blocks(bool wide, bool dual) {
+  return wide ? 2 : (sizeof(T) == 8 ? (dual ? 4 : 5) : 6);
+}
+
 template <typename T, bool WIDE>
-__global__ void __launch_bounds__(kBlock, WIDE ? 2 : 6) dual_step_kernel(
+__global__ void __launch_bounds__(kBlock, step_min_blocks<T>(WIDE, true)) dual_step_kernel(
     const Ctl* __restrict__ ctl, OpView<T> K, IterView<T> it, int j) {
   if (ctl->done) return;
   const long long t = ctl->t + j;
@@ -210,10 +217,10 @@ __global__ void __launch_bounds__(kBlock, WIDE ? 2 : 6) dual_step_kernel(
   const StepScalars<ACC> sc = step_scalars<ACC>(ctl, k);
   DualEpi<T, ACC> epi;
   const int n = it.n;
-  epi.y = it.Y[p];
-  epi.y_new = it.Y[p ^ 1];
-  epi.vr = it.V[p] + n;
-  epi.vr_new = it.V[p ^ 1] + n;
+  epi.y = it.y(p);
+  epi.y_new = it.y(p ^ 1);
+  epi.vr = it.v(p) + n;
+  epi.vr_new = it.v(p ^ 1) + n;
   epi.vbar_r = it.Vbar + n;
   epi.c = it.cost + n;
   epi.l = it.lower + n;
@@ -231,7 +238,7 @@ __global__ void __launch_bounds__(kBlock, WIDE ? 2 : 6) dual_step_kernel(
 }
 
 template <typename T, bool WIDE>
-__global__ void __launch_bounds__(kBlock, WIDE ? 2 : 6) primal_step_kernel(
+__global__ void __launch_bounds__(kBlock, step_min_blocks<T>(WIDE, false)) primal_step_kernel(
     const Ctl* __restrict__ ctl, OpView<T> Kt, IterView<T> it, int j) {
   if (ctl->done) return;
   const long long t = ctl->t + j;
@@ -241,8 +248,8 @@ __global__ void __launch_bounds__(kBlock, WIDE ? 2 : 6) primal_step_kernel(
   const long long k = ctl->k + j;
   const StepScalars<ACC> sc = step_scalars<ACC>(ctl, k);
   PrimalEpi<T, ACC> epi;
-  epi.x = it.V[p];
-  epi.x_new = it.V[p ^ 1];
+  epi.x = it.v(p);
+  epi.x_new = it.v(p ^ 1);
   epi.xbar = it.Vbar;
   epi.c = it.cost;
   epi.l = it.lower;
@@ -251,7 +258,7 @@ __global__ void __launch_bounds__(kBlock, WIDE ? 2 : 6) primal_step_kernel(
   epi.tau = sc.tau;
   epi.alpha = sc.alpha;
   epi.beta = sc.beta;
-  Gather1<T, ACC> g{it.Y[p ^ 1]};
+  Gather1<T, ACC> g{it.y(p ^ 1)};
   run_tiles<T, ACC, 1, Gather1<T, ACC>, PrimalEpi<T, ACC>, false, WIDE>(Kt.ts, Kt.ptr, Kt.idx,
                                                                         Kt.val, g, epi);
 }
@@ -378,9 +385,9 @@ __global__ void __launch_bounds__(kBlock) eval_rows_kernel(Ctl* ctl, OpView<T> K
   const int cur = eval_parity(ctl, fixed_parity);
   EvalRowEpi<T> epi;
   const int n = it.n;
-  epi.vr[0] = it.V[cur] + n;
+  epi.vr[0] = it.v(cur) + n;
   epi.vr[1] = it.Verg + n;
-  epi.y[0] = it.Y[cur];
+  epi.y[0] = it.y(cur);
   epi.y[1] = it.Yerg;
   epi.vr_rst = it.Vrst + n;
   epi.y_rst = it.Yrst;
@@ -389,7 +396,7 @@ __global__ void __launch_bounds__(kBlock) eval_rows_kernel(Ctl* ctl, OpView<T> K
   epi.long_terms = red.long_terms;
 #pragma unroll
   for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0;
-  Gather2<T> g{it.V[cur], it.Verg};
+  Gather2<T> g{it.v(cur), it.Verg};
   run_tiles<T, double, 2>(K.ts, K.ptr, K.idx, K.val, g, epi);
   EvalFin fin{ctl->eval_r};
   grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, smem_red(), fin, red.long_terms,
@@ -403,7 +410,7 @@ __global__ void __launch_bounds__(kBlock) eval_cols_kernel(Ctl* ctl, OpView<T> K
   if (fixed_parity < 0 && ctl->done) return;
   const int cur = eval_parity(ctl, fixed_parity);
   EvalColEpi<T> epi;
-  epi.x[0] = it.V[cur];
+  epi.x[0] = it.v(cur);
   epi.x[1] = it.Verg;
   epi.x_rst = it.Vrst;
   epi.ev = ev;
@@ -411,7 +418,7 @@ __global__ void __launch_bounds__(kBlock) eval_cols_kernel(Ctl* ctl, OpView<T> K
   epi.long_terms = red.long_terms;
 #pragma unroll
   for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0;
-  Gather2<T> g{it.Y[cur], it.Yerg};
+  Gather2<T> g{it.y(cur), it.Yerg};
   run_tiles<T, double, 2>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
   EvalFin fin{ctl->eval_c};
   grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, smem_red(), fin, red.long_terms,
@@ -531,9 +538,9 @@ __global__ void __launch_bounds__(kBlock) eval_rows32_kernel(Ctl* ctl, OpView<fl
   const int cur = eval_parity(ctl, fixed_parity);
   const int n = it.n;
   EvalRowEpi32 epi;
-  epi.vr[0] = it.V[cur] + n;
+  epi.vr[0] = it.v(cur) + n;
   epi.vr[1] = it.Verg + n;
-  epi.y[0] = it.Y[cur];
+  epi.y[0] = it.y(cur);
   epi.y[1] = it.Yerg;
   epi.vr_rst = it.Vrst + n;
   epi.y_rst = it.Yrst;
@@ -544,7 +551,7 @@ __global__ void __launch_bounds__(kBlock) eval_rows32_kernel(Ctl* ctl, OpView<fl
   epi.long_terms = red.long_terms;
 #pragma unroll
   for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0f;
-  Gather2f g{it.V[cur], it.Verg};
+  Gather2f g{it.v(cur), it.Verg};
   run_tiles<float, float, 2>(K.ts, K.ptr, K.idx, K.val, g, epi);
   double acc[kEvalSums];
 #pragma unroll
@@ -560,7 +567,7 @@ __global__ void __launch_bounds__(kBlock) eval_cols32_kernel(Ctl* ctl, OpView<fl
   if (fixed_parity < 0 && ctl->done) return;
   const int cur = eval_parity(ctl, fixed_parity);
   EvalColEpi32 epi;
-  epi.x[0] = it.V[cur];
+  epi.x[0] = it.v(cur);
   epi.x[1] = it.Verg;
   epi.x_rst = it.Vrst;
   epi.c = it.cost;
@@ -570,7 +577,7 @@ __global__ void __launch_bounds__(kBlock) eval_cols32_kernel(Ctl* ctl, OpView<fl
   epi.long_terms = red.long_terms;
 #pragma unroll
   for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0f;
-  Gather2f g{it.Y[cur], it.Yerg};
+  Gather2f g{it.y(cur), it.Yerg};
   run_tiles<float, float, 2>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
   double acc[kEvalSums];
 #pragma unroll
@@ -748,8 +755,8 @@ __global__ void restart_kernel(const Ctl* __restrict__ ctl, IterView<T> it) {
   const int cur = static_cast<int>(ctl->t & 1);
   const bool avg = ctl->restart_to_avg != 0;
   const int nt = it.n + it.m;
-  const T* vc = avg ? it.Verg : it.V[cur];
-  const T* yc = avg ? it.Yerg : it.Y[cur];
+  const T* vc = avg ? it.Verg : it.v(cur);
+  const T* yc = avg ? it.Yerg : it.y(cur);
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
     const T val = vc[k];
     it.Vrst[k] = val;
@@ -775,8 +782,8 @@ __global__ void extract_kernel(const Ctl* __restrict__ ctl, IterView<T> it, Eval
                                double* x_out, double* y_out, double* dual_ray) {
   const int cur = static_cast<int>(ctl->t & 1);
   const bool avg = ctl->result_average != 0;
-  const T* v = avg ? it.Verg : it.V[cur];
-  const T* y = avg ? it.Yerg : it.Y[cur];
+  const T* v = avg ? it.Verg : it.v(cur);
+  const T* y = avg ? it.Yerg : it.y(cur);
   const int n = it.n;
   const int nt = n + it.m;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
@@ -909,8 +916,8 @@ __global__ void __launch_bounds__(kBlock) det_ray_max_kernel(Ctl* c, IterView<T>
   const int cur = static_cast<int>(((c->t + (c->max_iter - c->t < kCheckFrequency
                                                   ? c->max_iter - c->t
                                                   : kCheckFrequency))) & 1);
-  const T* vn = it.V[cur];
-  const T* vo = it.V[cur ^ 1];
+  const T* vn = it.v(cur);
+  const T* vo = it.v(cur ^ 1);
   const int nt = it.n + it.m;
   double a[1] = {0.0};
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
@@ -930,8 +937,8 @@ __global__ void __launch_bounds__(kBlock) det_ray_cols_kernel(Ctl* c, IterView<T
   const int cur = static_cast<int>(((c->t + (c->max_iter - c->t < kCheckFrequency
                                                   ? c->max_iter - c->t
                                                   : kCheckFrequency))) & 1);
-  const T* vn = it.V[cur];
-  const T* vo = it.V[cur ^ 1];
+  const T* vn = it.v(cur);
+  const T* vo = it.v(cur ^ 1);
   const double v_max = c->det[5];
   double a[2] = {0.0, 0.0};  // cost_dir (cols), bound failure
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < it.n; j += gridDim.x * blockDim.x) {
@@ -1009,8 +1016,8 @@ __global__ void __launch_bounds__(kBlock) det_ray_rows_kernel(Ctl* c, OpView<T> 
                                                   ? c->max_iter - c->t
                                                   : kCheckFrequency))) & 1);
   RayRowEpi<T> epi;
-  epi.vn = it.V[cur];
-  epi.vo = it.V[cur ^ 1];
+  epi.vn = it.v(cur);
+  epi.vo = it.v(cur ^ 1);
   epi.inv_vmax = 1.0;
   const double v_max = c->det[5];
   epi.ev = ev;

@@ -30,6 +30,10 @@ struct IterView {
   const T* upper;  // n + m
   const T* rhs;    // m right-hand side q of [A -I] v = q (null: zero)
   int n, m;
+  // V[p], Y[p] by a select: indexing a kernel parameter's array with a runtime index makes
+  // the compiler copy the whole view to local memory first.
+  __host__ __device__ __forceinline__ T* v(int p) const { return p ? V[1] : V[0]; }
+  __host__ __device__ __forceinline__ T* y(int p) const { return p ? Y[1] : Y[0]; }
 };
 
 // The data the evaluation maps iterates back with (FP64): equilibration factors and the

@@ -192,8 +192,8 @@ __global__ void ir_update_kernel(const Ctl* __restrict__ c32, IterView<float> it
                                  int round) {
   const int cur = static_cast<int>(c32->t & 1);
   const bool avg = c32->result_average != 0;
-  const float* w = avg ? it.Verg : it.V[cur];
-  const float* z = avg ? it.Yerg : it.Y[cur];
+  const float* w = avg ? it.Verg : it.v(cur);
+  const float* z = avg ? it.Yerg : it.y(cur);
   const double dp = c32->ir_dp;
   const double dd = c32->ir_dd;
   const int nt = v.n + v.m;
