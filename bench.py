@@ -420,7 +420,7 @@ def main():
     opts = solver_options(args, args.precision)
     solver = sg.PdlpSolver(lp, opts)
     cfg["tiles"] = {k: {"nnz_per_tile": v[0], "rows_per_tile": v[1], "tiles": v[2],
-                        "deep_unroll_kernel": v[3]}
+                        "kernel_variant": v[3], "team_split": v[4]}
                     for k, v in solver.tile_shapes().items()}
     for _ in range(args.warmup):
         warm = solver.solve(download=False)

@@ -67,6 +67,9 @@ typedef struct sg_pdlp_opts {
   int autotune;              /* 1 (default): time candidate tile shapes of each large operator
                                 on the device at create, keyed by its row-length statistics
                                 (cached per process); 0: the built-in rule */
+  int tile_split;            /* built-in rule: medium rows (more than 128 nonzeros) longer than
+                                this many nonzeros are summed by a team of 2-8 warps; 0
+                                (default): one warp per row */
 } sg_pdlp_opts;
 
 /* Algorithm variants. REFERENCE follows samaya's PDLP step for step (L2 Ruiz, fixed step
@@ -168,10 +171,12 @@ int sg_pdlp_time_kernels(sg_pdlp* handle, int reps, double* ms_dual, double* ms_
                          double* ms_eval);
 
 /* The tile shape in use for A (transpose 0) or A' (transpose 1): nonzeros per tile, rows per
- * short-row tile, number of tiles, and whether the step kernel runs its deep-unroll variant
- * (diagnostics; set by the autotuner or the built-in rule). */
+ * short-row tile, number of tiles, the step kernel variant (0 high occupancy, 1 deep unroll
+ * of medium and long rows), and the nonzeros per warp above
+ * which a medium row is summed by a team of warps (0: one warp per row). Diagnostics; set by
+ * the autotuner or the built-in rule. */
 int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_rows,
-                       int* ntiles, int* wide);
+                       int* ntiles, int* variant, int* split);
 
 /* Model -> LpProblem: samaya's power-of-two scaling and computational form, as
  * compute_scaling + make_problem compute them (reference src/linalg/scaling.cpp:130-200,

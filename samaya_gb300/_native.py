@@ -23,7 +23,8 @@ class Opts(ctypes.Structure):
                 ("time_limit", ctypes.c_double), ("precision", ctypes.c_int),
                 ("refine_max_rounds", ctypes.c_int), ("inner_tol", ctypes.c_double),
                 ("verbose", ctypes.c_int), ("algorithm", ctypes.c_int),
-                ("autotune", ctypes.c_int)]
+                ("autotune", ctypes.c_int),
+                ("tile_split", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -105,7 +106,7 @@ def _declare(lib):
                                  c_double_p]),
         "sg_spmv": (I, [P, I, c_double_p, c_double_p]),
         "sg_pdlp_time_kernels": (I, [P, I, c_double_p, c_double_p, c_double_p]),
-        "sg_pdlp_tile_shape": (I, [P, I] + [ctypes.POINTER(ctypes.c_int)] * 4),
+        "sg_pdlp_tile_shape": (I, [P, I] + [ctypes.POINTER(ctypes.c_int)] * 5),
         "sg_scale_model": (I, [I, I, c_int64_p, c_int32_p, c_double_p, c_double_p, c_double_p,
                                c_double_p, c_double_p, c_double_p, I, c_int64_p, c_int32_p,
                                c_double_p, c_double_p, c_double_p, c_double_p, c_double_p,

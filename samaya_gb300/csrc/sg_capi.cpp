@@ -37,6 +37,7 @@ sg::Options to_options(const sg_pdlp_opts* o) {
   opt.verbose = o->verbose;
   opt.algorithm = o->algorithm == SG_ALGORITHM_ENHANCED ? 1 : 0;
   opt.autotune = o->autotune != 0;
+  opt.tile_split = o->tile_split > 0 ? o->tile_split : 0;
   return opt;
 }
 
@@ -55,6 +56,7 @@ void sg_pdlp_default_opts(sg_pdlp_opts* opts) {
   opts->inner_tol = 1e-4;
   opts->verbose = 0;
   opts->autotune = 1;
+  opts->tile_split = 0;
 }
 
 int sg_pdlp_available(int* cc_major, int* cc_minor, char* name, size_t name_len) {
@@ -229,11 +231,12 @@ int sg_pdlp_time_kernels(sg_pdlp* handle, int reps, double* ms_dual, double* ms_
 }
 
 int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_rows,
-                       int* ntiles, int* wide) {
-  if (cap_nnz == nullptr || cap_rows == nullptr || ntiles == nullptr || wide == nullptr) {
+                       int* ntiles, int* variant, int* split) {
+  if (cap_nnz == nullptr || cap_rows == nullptr || ntiles == nullptr || variant == nullptr ||
+      split == nullptr) {
     return fail(SG_ERR_INVALID_ARGUMENT, "NULL output");
   }
-  SG_SEAM(handle->engine->tile_shape(transpose, cap_nnz, cap_rows, ntiles, wide));
+  SG_SEAM(handle->engine->tile_shape(transpose, cap_nnz, cap_rows, ntiles, variant, split));
 }
 
 int sg_spmv(sg_pdlp* handle, int transpose, const double* x, double* y) {

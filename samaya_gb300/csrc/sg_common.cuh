@@ -26,12 +26,13 @@ constexpr int kCheckFrequency = 64;  // iterations between evaluations (pdlp.cpp
 
 // One CTA's share of an operator. kind 0: rows [r0, r1) whole, nonzeros [k0, k1);
 // kind 1: one segment [k0, k1) of long row r0 (r1 = r0 + 1), segment `seg` of `nseg`, long
-// row id `lrow` (its partials are combined by the last segment to finish).
+// row id `lrow` (its partials are combined by the last segment to finish); kind 2: rows
+// [r0, r1) of medium length, `team` warps each.
 struct Tile {
   int r0, r1;
   int k0, k1;
   int kind;
-  int team;  // lanes per row in kind 0 (1..32)
+  int team;  // kind 2: warps per row (1, 2, 4 or 8); 1 otherwise
   int seg, nseg;
   int lrow;
   int pad[3];
@@ -45,8 +46,7 @@ struct TileSet {
   unsigned* lcount; // [nlong] arrival counters (reset by the last arrival)
   int cap_nnz;      // nonzeros per tile at most (shared-memory staging capacity)
   int cap_rows;     // rows per tile at most
-  int wide;         // step kernels: the deep-unroll variant (long rows) instead of the
-                    // high-occupancy one
+  int variant;      // step kernels: 0 high occupancy, 1 deep unroll of medium and long rows
 };
 
 constexpr int kMaxVec = 2;

@@ -52,29 +52,38 @@ std::vector<double> power_start(int m) {
 // tiles (kind 2); the other rows go consecutively into tiles of at most tile_nnz nonzeros and
 // tile_rows rows, a thread per row (kind 0).
 void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, int warp_min,
-                 std::vector<Tile>* out, int* nlong) {
+                 int split, std::vector<Tile>* out, int* nlong) {
   out->clear();
   *nlong = 0;
   const int rows = static_cast<int>(ptr.size()) - 1;
   // Rows longer than a tile are split into CTA segments (kind 1); rows of more than
-  // warp_min nonzeros get a warp each, kWarpsPerTile rows per tile (kind 2).
+  // warp_min nonzeros get a warp each, kWarpsPerTile rows per tile (kind 2) — or, with
+  // split > 0, a team of the fewest warps (a power of two up to kWarpsPerTile) giving each at
+  // most `split` nonzeros, kWarpsPerTile / team rows of equal team per tile.
   const int long_len = std::max(tile_nnz, warp_min);
+  auto team_of = [split](int len) {
+    int t = 1;
+    if (split > 0) {
+      while (t < kWarpsPerTile && len > static_cast<long long>(t) * split) t *= 2;
+    }
+    return t;
+  };
   int r = 0;
   while (r < rows) {
     const int len = ptr[r + 1] - ptr[r];
     if (len > warp_min && len <= long_len) {
       Tile t{};
       t.r0 = r;
-      while (r < rows && r - t.r0 < kWarpsPerTile) {
+      t.team = team_of(len);
+      while (r < rows && r - t.r0 < kWarpsPerTile / t.team) {
         const int l = ptr[r + 1] - ptr[r];
-        if (l <= warp_min || l > long_len) break;
+        if (l <= warp_min || l > long_len || team_of(l) != t.team) break;
         ++r;
       }
       t.r1 = r;
       t.k0 = ptr[t.r0];
       t.k1 = ptr[r];
       t.kind = 2;
-      t.team = 32;
       t.seg = 0;
       t.nseg = 1;
       t.lrow = -1;
@@ -90,7 +99,7 @@ void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, int w
         t.k0 = ptr[r] + s * tile_nnz;
         t.k1 = std::min(ptr[r + 1], t.k0 + tile_nnz);
         t.kind = 1;
-        t.team = 32;
+        t.team = 1;
         t.seg = s;
         t.nseg = nseg;
         t.lrow = *nlong;
@@ -113,10 +122,7 @@ void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, int w
     t.k0 = ptr[r0];
     t.k1 = ptr[r];
     t.kind = 0;
-    const double mean = static_cast<double>(t.k1 - t.k0) / std::max(1, r - r0);
-    int team = 1;
-    while (team < 32 && 2 * team * 2 <= mean) team *= 2;
-    t.team = team;
+    t.team = 1;
     t.seg = 0;
     t.nseg = 1;
     t.lrow = -1;
@@ -389,7 +395,8 @@ TileShape Engine::default_shape(const DevOp& op) const {
     const int len = op.host_ptr[r + 1] - op.host_ptr[r];
     if (len > sh.warp_min) in_long += len;
   }
-  sh.wide = 2 * in_long >= op.nnz && op.nnz > 0;
+  sh.variant = 2 * in_long >= op.nnz && op.nnz > 0 ? 1 : 0;
+  sh.split = opt_.tile_split;
   return sh;
 }
 
@@ -398,7 +405,8 @@ int Engine::set_tiles(DevOp* op, const TileShape& shape) {
   std::string* err = nullptr;
   std::vector<Tile> tiles;
   int nlong = 0;
-  build_tiles(op->host_ptr, shape.cap_nnz, shape.cap_rows, shape.warp_min, &tiles, &nlong);
+  build_tiles(op->host_ptr, shape.cap_nnz, shape.cap_rows, shape.warp_min, shape.split, &tiles,
+              &nlong);
   SG_TRY(cudaStreamSynchronize(stream_));
   dfree(op->tiles);
   dfree(op->seg_part);
@@ -406,7 +414,8 @@ int Engine::set_tiles(DevOp* op, const TileShape& shape) {
   op->cap_nnz = shape.cap_nnz;
   op->cap_rows = shape.cap_rows;
   op->warp_min = shape.warp_min;
-  op->wide = shape.wide;
+  op->variant = shape.variant;
+  op->split = shape.split;
   op->ntiles = static_cast<int>(tiles.size());
   op->nlong = nlong;
   SG_TRY(dalloc(&op->tiles, tiles.size()));
@@ -472,9 +481,10 @@ double Engine::time_step_kernel(bool dual, int reps) {
 
 // Tile shapes of both operators. With autotuning, an operator of at least 2^18 nonzeros whose
 // row-length statistics were not seen before in this process gets its step kernel timed for
-// eight shapes around the built-in rule (half, same, twice and four times the nonzeros per
-// tile, short-row tiles of half as many rows; each with both kernel variants); the fastest is
-// kept and cached under the statistics.
+// shapes around the built-in rule (half, same, twice and four times the nonzeros per tile,
+// short-row tiles of half as many rows; each with both step kernel variants and each team
+// split of the medium rows); the fastest (by a margin over the built-in shape) is kept and
+// cached under the statistics.
 int Engine::tune_tiles(std::string* err) {
   for (int which = 0; which < 2; ++which) {
     DevOp* op = which == 0 ? &K_ : &Kt_;
@@ -493,25 +503,56 @@ int Engine::tune_tiles(std::string* err) {
       }
     }
     if (tune && !cached) {
+      // Team splits of the medium rows: none, the median medium row's length and half of it
+      // (rows longer than the split get 2-8 warps; only when medium rows exist).
+      std::vector<int> medium;
+      for (int r = 0; r < op->rows; ++r) {
+        const int len = op->host_ptr[r + 1] - op->host_ptr[r];
+        if (len > base.warp_min) medium.push_back(len);
+      }
+      std::vector<int> splits{0};
+      if (!medium.empty()) {
+        std::nth_element(medium.begin(), medium.begin() + medium.size() / 2, medium.end());
+        const int med = medium[medium.size() / 2];
+        splits.push_back(med);
+        if (med / 2 > base.warp_min) splits.push_back(med / 2);
+      }
+      // Candidates: the built-in shape first, then (split, capacity, variant). A candidate
+      // replaces the best so far only when it is at least kTuneMargin faster (the best of
+      // three timed rounds each), so launch-to-launch noise keeps the built-in shape.
+      std::vector<TileShape> cands{base};
+      for (int split : splits) {
+        for (int ci = 0; ci < 4; ++ci) {
+          const int cap = (base.cap_nnz / 2) << ci;
+          if (cap < 256 || cap > 4 * kTileNnz) continue;
+          for (int variant = 0; variant < 2; ++variant) {
+            TileShape sh = base;
+            sh.cap_nnz = cap;
+            sh.cap_rows = std::min(kTileRows, std::max(256, cap / 2));
+            sh.variant = variant;
+            sh.split = split;
+            cands.push_back(sh);
+          }
+        }
+      }
+      constexpr double kTuneMargin = 0.97;
       double best_ms = -1.0;
-      for (int c = 0; c < 8; ++c) {
-        const int cap = (base.cap_nnz / 2) << (c >> 1);
-        if (cap < 256 || cap > 4 * kTileNnz) continue;
-        TileShape sh = base;
-        sh.cap_nnz = cap;
-        sh.cap_rows = std::min(kTileRows, std::max(256, cap / 2));
-        sh.wide = (c & 1) != 0;
+      for (const TileShape& sh : cands) {
         const int rc = set_tiles(op, sh);
         if (rc != kOk) {
           if (err) *err = "autotune: tile upload failed";
           return rc;
         }
-        const double ms = time_step_kernel(which == 0, 10);
-        if (ms < 0) {
-          if (err) *err = std::string("autotune: ") + cudaGetErrorString(cudaGetLastError());
-          return kErrCuda;
+        double ms = -1.0;
+        for (int round = 0; round < 3; ++round) {
+          const double t = time_step_kernel(which == 0, 8);
+          if (t < 0) {
+            if (err) *err = std::string("autotune: ") + cudaGetErrorString(cudaGetLastError());
+            return kErrCuda;
+          }
+          ms = ms < 0 ? t : std::min(ms, t);
         }
-        if (best_ms < 0 || ms < best_ms) {
+        if (best_ms < 0 || ms < kTuneMargin * best_ms) {
           best_ms = ms;
           best = sh;
         }

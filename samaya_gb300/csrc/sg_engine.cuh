@@ -36,6 +36,7 @@ struct Options {
   int verbose = 0;
   int algorithm = 0;        // 0 the reference's PDLP, 1 enhanced preconditioning + weight
   bool autotune = true;     // time candidate tile shapes of large operators at create
+  int tile_split = 0;       // built-in rule's team split of medium rows (0: a warp per row)
 };
 
 // Tile shape of an operator: nonzeros per tile (and per long-row segment), rows per short-row
@@ -44,7 +45,8 @@ struct TileShape {
   int cap_nnz = kTileNnz;
   int cap_rows = kTileRows;
   int warp_min = kWarpRowMin;
-  bool wide = false;        // step kernel variant (see sg_kernels.cu)
+  int variant = 0;          // step kernel variant (see sg_kernels.cu)
+  int split = 0;            // kind-2 rows: nonzeros per warp of a team (0: a warp per row)
 };
 
 struct SolveInfo {
@@ -80,7 +82,8 @@ struct DevOp {
   int cap_nnz = kTileNnz;
   int cap_rows = kTileRows;
   int warp_min = kWarpRowMin;
-  bool wide = false;
+  int variant = 0;
+  int split = 0;
   std::vector<int> host_ptr;
 
   TileSet tileset() const {
@@ -92,7 +95,7 @@ struct DevOp {
     t.lcount = lcount;
     t.cap_nnz = cap_nnz;
     t.cap_rows = cap_rows;
-    t.wide = wide ? 1 : 0;
+    t.variant = variant;
     return t;
   }
   OpView<double> view64() const { return OpView<double>{ptr, idx, val, rows, tileset()}; }
@@ -145,12 +148,14 @@ class Engine {
   // Average device milliseconds of the step kernels and the evaluation (CUDA events).
   int time_kernels(int reps, double* ms_dual, double* ms_primal, double* ms_eval);
   int tile_capacity(int transpose) const { return transpose ? Kt_.cap_nnz : K_.cap_nnz; }
-  int tile_shape(int transpose, int* cap_nnz, int* cap_rows, int* ntiles, int* wide) const {
+  int tile_shape(int transpose, int* cap_nnz, int* cap_rows, int* ntiles, int* variant,
+                 int* split) const {
     const DevOp& op = transpose ? Kt_ : K_;
     *cap_nnz = op.cap_nnz;
     *cap_rows = op.cap_rows;
     *ntiles = op.ntiles;
-    *wide = op.wide ? 1 : 0;
+    *variant = op.variant;
+    *split = op.split;
     return 0;
   }
   bool fp32() const { return fp32_; }
@@ -249,8 +254,7 @@ class Engine {
 
 // Builds the tile partition of a CSR operator (host). Exposed for the CPU tests.
 void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, int warp_min,
-                 std::vector<Tile>* out,
-                 int* nlong);
+                 int split, std::vector<Tile>* out, int* nlong);
 
 // Device facts for sg_pdlp_available.
 int device_info(int* major, int* minor, char* name, size_t len);

@@ -194,19 +194,25 @@ __device__ __forceinline__ StepScalars<ACC> step_scalars(const Ctl* __restrict__
   }
 }
 
-// Two variants of each step kernel: WIDE = false keeps many CTAs per SM resident (operators of
-// short rows, where occupancy hides the latency): 6 (40 registers) in FP32; in FP64, whose
-// epilogues spilled at 40 registers, 5 (48) for the primal step and 4 (64) for the dual step
-// (nine FP64 row values preloaded). WIDE = true allows 128 registers and unrolls the
-// warp-per-row and segment loops twice as deep (operators of long rows, whose few CTAs need
-// more loads in flight each). TileSet::wide selects one per operator.
+// Two variants of each step kernel (TileSet::variant, one per operator, picked by the tile
+// tuner or the built-in rule):
+//   0: many CTAs per SM resident (operators of short rows, where occupancy hides the latency),
+//      as many as fit without spills: the primal step 6 (40 registers) in FP32 and 5 (48) in
+//      FP64; the dual step, whose epilogue preloads nine row values, 5 in FP32 and 4 (64) in
+//      FP64;
+//   1: 128 registers, the warp-per-row and segment loops unrolled twice as deep (operators of
+//      long rows, whose few CTAs need more loads in flight each).
+// (Measured and not kept: a third variant loading a short row's first three pairs of
+// nonzeros together at 4 CTAs per SM; no faster on the transportation or power-law LPs.)
 template <typename T>
-constexpr int step_min_blocks(bool wide, bool dual) {
-  return wide ? 2 : (sizeof(T) == 8 ? (dual ? 4 : 5) : 6);
+constexpr int step_min_blocks(int variant, bool dual) {
+  if (variant == 1) return 2;
+  if (sizeof(T) == 8) return dual ? 4 : 5;
+  return dual ? 5 : 6;
 }
 
-template <typename T, bool WIDE>
-__global__ void __launch_bounds__(kBlock, step_min_blocks<T>(WIDE, true)) dual_step_kernel(
+template <typename T, int VAR>
+__global__ void __launch_bounds__(kBlock, step_min_blocks<T>(VAR, true)) dual_step_kernel(
     const Ctl* __restrict__ ctl, OpView<T> K, IterView<T> it, int j) {
   if (ctl->done) return;
   const long long t = ctl->t + j;
@@ -233,12 +239,12 @@ __global__ void __launch_bounds__(kBlock, step_min_blocks<T>(WIDE, true)) dual_s
   epi.alpha = sc.alpha;
   epi.beta = sc.beta;
   Gather1<T, ACC> g{it.Vbar};
-  run_tiles<T, ACC, 1, Gather1<T, ACC>, DualEpi<T, ACC>, false, WIDE>(K.ts, K.ptr, K.idx, K.val,
-                                                                      g, epi);
+  run_tiles<T, ACC, 1, Gather1<T, ACC>, DualEpi<T, ACC>, false, VAR == 1>(
+      K.ts, K.ptr, K.idx, K.val, g, epi);
 }
 
-template <typename T, bool WIDE>
-__global__ void __launch_bounds__(kBlock, step_min_blocks<T>(WIDE, false)) primal_step_kernel(
+template <typename T, int VAR>
+__global__ void __launch_bounds__(kBlock, step_min_blocks<T>(VAR, false)) primal_step_kernel(
     const Ctl* __restrict__ ctl, OpView<T> Kt, IterView<T> it, int j) {
   if (ctl->done) return;
   const long long t = ctl->t + j;
@@ -259,8 +265,8 @@ __global__ void __launch_bounds__(kBlock, step_min_blocks<T>(WIDE, false)) prima
   epi.alpha = sc.alpha;
   epi.beta = sc.beta;
   Gather1<T, ACC> g{it.y(p ^ 1)};
-  run_tiles<T, ACC, 1, Gather1<T, ACC>, PrimalEpi<T, ACC>, false, WIDE>(Kt.ts, Kt.ptr, Kt.idx,
-                                                                        Kt.val, g, epi);
+  run_tiles<T, ACC, 1, Gather1<T, ACC>, PrimalEpi<T, ACC>, false, VAR == 1>(
+      Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1375,14 +1381,14 @@ void configure_kernels() {
   cudaFuncSetAttribute(eval_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_ray_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_ray_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(dual_step_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(primal_step_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(dual_step_kernel<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(primal_step_kernel<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(dual_step_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(primal_step_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(dual_step_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(primal_step_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(dual_step_kernel<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(primal_step_kernel<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(dual_step_kernel<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(primal_step_kernel<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(dual_step_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(primal_step_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(dual_step_kernel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(primal_step_kernel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_farkas_cols_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_farkas_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(max_norm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
@@ -1398,10 +1404,10 @@ void launch_dual_step(const Ctl* ctl, const OpView<T>& K, const IterView<T>& it,
                       cudaStream_t s) {
   if (K.ts.ntiles == 0) return;
   const size_t sm = tile_smem_bytes(K.ts, 1, sizeof(T));
-  if (K.ts.wide) {
-    dual_step_kernel<T, true><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
+  if (K.ts.variant == 1) {
+    dual_step_kernel<T, 1><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
   } else {
-    dual_step_kernel<T, false><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
+    dual_step_kernel<T, 0><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
   }
 }
 
@@ -1410,10 +1416,10 @@ void launch_primal_step(const Ctl* ctl, const OpView<T>& Kt, const IterView<T>& 
                         int grid, cudaStream_t s) {
   if (Kt.ts.ntiles == 0) return;
   const size_t sm = tile_smem_bytes(Kt.ts, 1, sizeof(T));
-  if (Kt.ts.wide) {
-    primal_step_kernel<T, true><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
+  if (Kt.ts.variant == 1) {
+    primal_step_kernel<T, 1><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
   } else {
-    primal_step_kernel<T, false><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
+    primal_step_kernel<T, 0><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
   }
 }
 

@@ -6,8 +6,9 @@
 //     epi.row(row, sums) — the fused update of the row's entries; a row longer than 32
 //     nonzeros is taken over by its whole warp (ballot queue, fixed shuffle tree).
 //   kind 2 (up to 8 rows of medium length, 128 < nonzeros <= the tile capacity): one warp per
-//     row, 16-byte loads of four nonzeros per lane, a fixed shuffle tree, lane 0 runs
-//     epi.row(row, sums). A CTA per row would spend most of its time on the block tree.
+//     row, or a team of 2-8 warps for the longer rows of a skewed operator, 16-byte loads of
+//     four nonzeros per lane, a fixed shuffle tree (then the team's partials in warp order),
+//     and epi.row(row, sums). A CTA per row would spend most of its time on the block tree.
 //   kind 1 (a segment of a row longer than the tile capacity): the CTA sums the segment
 //     (strided, then the fixed block tree) into TileSet::seg_part; the last segment to arrive
 //     (counter) adds the row's segments in tile order and runs epi.long_row.
@@ -227,19 +228,25 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
         }
       }
     } else if (tile.kind == 2) {
-      // Rows of medium length, one warp each: head up to a 4-aligned position, 16-byte loads
-      // of four nonzeros per lane, tail, then the fixed shuffle tree; lane 0 updates the row.
+      // Rows of medium length, `team` warps each (1, 2, 4 or 8; the CTA holds 8 / team rows):
+      // head up to a 4-aligned position, 16-byte loads of four nonzeros per lane (the team's
+      // warps take every team-th block of 128 nonzeros), tail, then the fixed shuffle tree;
+      // the team's partial sums are added in warp order and lane 0 of its first warp updates
+      // the row.
       const int lane = tid & 31;
-      const int r = tile.r0 + (tid >> 5);
+      const int warp = tid >> 5;
+      const int team = tile.team;
+      const int part = warp & (team - 1);
+      const int r = tile.r0 + warp / team;
+      ACC s[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) s[v] = ACC(0);
       if (r < tile.r1) {
         const int b = ldg(ptr + r);
         const int e = ldg(ptr + r + 1);
-        ACC s[NV];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) s[v] = ACC(0);
         const int a0 = min(e, (b + 3) & ~3);
         const int a1 = max(a0, e & ~3);
-        if (b + lane < a0) {
+        if (part == 0 && b + lane < a0) {
           const int q = b + lane;
           const T a = ldg(val + q);
           const int j = ldg(idx + q);
@@ -258,14 +265,26 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
             s[v] = combine<MAXRED>(s[v], prod(v, a[3], j.w));
           }
         };
+        // A warp per row keeps its own loop (a compile-time stride unrolls deeper).
+        const int step = 128 * team;
         if constexpr (WIDE) {
+          if (team == 1) {
 #pragma unroll 8
-          for (int q = a0 + 4 * lane; q < a1; q += 128) quad(q);
+            for (int q = a0 + 4 * lane; q < a1; q += 128) quad(q);
+          } else {
+#pragma unroll 8
+            for (int q = a0 + 4 * lane + 128 * part; q < a1; q += step) quad(q);
+          }
         } else {
+          if (team == 1) {
 #pragma unroll 4
-          for (int q = a0 + 4 * lane; q < a1; q += 128) quad(q);
+            for (int q = a0 + 4 * lane; q < a1; q += 128) quad(q);
+          } else {
+#pragma unroll 4
+            for (int q = a0 + 4 * lane + 128 * part; q < a1; q += step) quad(q);
+          }
         }
-        if (a1 + lane < e) {
+        if (part == 0 && a1 + lane < e) {
           const int q = a1 + lane;
           const T a = ldg(val + q);
           const int j = ldg(idx + q);
@@ -279,7 +298,27 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
             s[v] = combine<MAXRED>(s[v], __shfl_down_sync(0xffffffffu, s[v], o));
           }
         }
-        if (lane == 0) epi.row(r, s);
+        if (team == 1 && lane == 0) epi.row(r, s);
+      }
+      if (team > 1) {
+        // team is uniform over the tile, so every thread of the CTA reaches both barriers.
+        ACC* partial = reinterpret_cast<ACC*>(red);
+        if (lane == 0) {
+#pragma unroll
+          for (int v = 0; v < NV; ++v) partial[warp * NV + v] = s[v];
+        }
+        __syncthreads();
+        if (part == 0 && lane == 0 && r < tile.r1) {
+          ACC tot[NV];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            ACC a = partial[warp * NV + v];
+            for (int w = 1; w < team; ++w) a = combine<MAXRED>(a, partial[(warp + w) * NV + v]);
+            tot[v] = a;
+          }
+          epi.row(r, tot);
+        }
+        __syncthreads();
       }
     } else {
       // A segment of a long row: strided sums, then the fixed block tree (in the accumulation

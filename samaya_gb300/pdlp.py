@@ -42,6 +42,7 @@ class PdlpOptions:
     algorithm: int = REFERENCE
     verbose: int = 0
     autotune: bool = True
+    tile_split: int = 0
 
     def to_c(self) -> _native.Opts:
         o = _native.Opts()
@@ -55,6 +56,7 @@ class PdlpOptions:
         o.algorithm = int(self.algorithm)
         o.verbose = int(self.verbose)
         o.autotune = 1 if self.autotune else 0
+        o.tile_split = int(self.tile_split)
         return o
 
 
@@ -124,14 +126,14 @@ class PdlpSolver:
         return a.value, b.value, c.value
 
     def tile_shapes(self):
-        """{"A": (nonzeros per tile, rows per short-row tile, tiles, deep-unroll variant),
-        "At": ...} in use."""
+        """{"A": (nonzeros per tile, rows per short-row tile, tiles, step kernel variant,
+        nonzeros per warp of a medium row's team or 0), "At": ...} in use."""
         out = {}
         for name, t in (("A", 0), ("At", 1)):
-            v = [ctypes.c_int(0) for _ in range(4)]
+            v = [ctypes.c_int(0) for _ in range(5)]
             _native.check(self._lib.sg_pdlp_tile_shape(self._h, t, *[ctypes.byref(x) for x in v]),
                           "sg_pdlp_tile_shape")
-            out[name] = (v[0].value, v[1].value, v[2].value, bool(v[3].value))
+            out[name] = (v[0].value, v[1].value, v[2].value, v[3].value, v[4].value)
         return out
 
     def solve(self, x_out: np.ndarray | None = None, y_out: np.ndarray | None = None,
@@ -213,7 +215,10 @@ class PdhgDevice:
     CURRENT = 0
     AVERAGE = 1
 
-    def __init__(self, m, n, colptr, rowidx, vals, cost, lower, upper):
+    def __init__(self, m, n, colptr, rowidx, vals, cost, lower, upper,
+                 options: PdlpOptions | None = None):
+        """``options`` (the engine's own knobs, e.g. the tile shape): None keeps the defaults
+        ``sg_pdhg_create`` uses."""
         self._lib = _native.load()
         self.m, self.n = int(m), int(n)
         self._keep = [np.ascontiguousarray(colptr, dtype=np.int64),
@@ -224,10 +229,15 @@ class PdhgDevice:
                       np.ascontiguousarray(upper, dtype=np.float64)]
         k = self._keep
         self._h = ctypes.c_void_p()
-        _native.check(self._lib.sg_pdhg_create(
-            ctypes.byref(self._h), self.m, self.n, _ptr(k[0], ctypes.c_int64),
-            _ptr(k[1], ctypes.c_int32), _ptr(k[2], ctypes.c_double), _ptr(k[3], ctypes.c_double),
-            _ptr(k[4], ctypes.c_double), _ptr(k[5], ctypes.c_double)), "sg_pdhg_create")
+        args = (ctypes.byref(self._h), self.m, self.n, _ptr(k[0], ctypes.c_int64),
+                _ptr(k[1], ctypes.c_int32), _ptr(k[2], ctypes.c_double),
+                _ptr(k[3], ctypes.c_double), _ptr(k[4], ctypes.c_double),
+                _ptr(k[5], ctypes.c_double))
+        if options is None:
+            _native.check(self._lib.sg_pdhg_create(*args), "sg_pdhg_create")
+        else:
+            o = options.to_c()
+            _native.check(self._lib.sg_pdlp_create(*args, ctypes.byref(o)), "sg_pdlp_create")
 
     def set_original(self, col_scale, row_scale, cost, lower, upper):
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in

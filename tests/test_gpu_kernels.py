@@ -69,10 +69,12 @@ def test_spmv_rows_of_every_length_match_the_cpu(engine):
     assert np.array_equal(t, dev.spmv(yt, transpose=True))
 
 
-def test_spmv_medium_rows_on_several_warps_match_the_cpu(engine):
+@pytest.mark.parametrize("split", [0, 300, 1000])
+def test_spmv_medium_rows_on_several_warps_match_the_cpu(engine, split):
     """A 2000 x 60000 operator with 2.6M nonzeros (4096-nonzero tiles): rows of 129 to 4096
-    nonzeros (a warp per row, unaligned starts), rows one past a tile, short and empty rows;
-    both products against scipy to 1e-12 and bit-identical on repeat."""
+    nonzeros (a warp per row, or with a team split of `split` nonzeros per warp teams of 2, 4
+    and 8 warps; unaligned starts), rows one past a tile, short and empty rows; both products
+    against scipy to 1e-12 and bit-identical on repeat."""
     sp = pytest.importorskip("scipy.sparse")
     rng = np.random.default_rng(615)
     m, n = 2000, 60000
@@ -86,7 +88,8 @@ def test_spmv_medium_rows_on_several_warps_match_the_cpu(engine):
     colptr = A.indptr.astype(np.int64)
     rowidx = A.indices.astype(np.int32)
     dev = engine.PdhgDevice(m, n, colptr, rowidx, A.data.copy(), np.zeros(n + m),
-                            np.zeros(n + m), np.zeros(n + m))
+                            np.zeros(n + m), np.zeros(n + m),
+                            options=engine.PdlpOptions(autotune=False, tile_split=split))
     x = rng.uniform(-1, 1, size=n)
     y_cpu = A @ x
     a = dev.spmv(x)
