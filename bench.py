@@ -287,21 +287,24 @@ def run_batch(args):
                     "optimal": int(sum(x.status == sg.OPTIMAL for x in r)),
                     "mean_iterations": float(np.mean([x.iterations for x in r])),
                     "max_iterations": int(max(x.iterations for x in r))}
-        # Sequential single-LP GPU solves (FP64, each algorithm) on a sample of the instances.
+        # Sequential single-LP GPU solves (each precision and algorithm) on a sample of the
+        # instances.
         seq = {}
         k = 16
-        for alg_name, alg in algs:
-            ms = 0.0
-            for p in singles[:k]:
-                ms += sg.solve_pdlp(p, sg.PdlpOptions(tol=tol, algorithm=alg)).device_ms
-            seq[alg_name] = {"lps_per_s": k / (ms / 1e3), "sample": k}
+        for name, prec in (("fp64", sg.FP64), ("fp32", sg.FP32_REFINED)):
+            for alg_name, alg in algs:
+                ms = 0.0
+                for p in singles[:k]:
+                    ms += sg.solve_pdlp(p, sg.PdlpOptions(tol=tol, precision=prec,
+                                                          algorithm=alg)).device_ms
+                seq[f"{name}_{alg_name}"] = {"lps_per_s": k / (ms / 1e3), "sample": k}
     best = max(out.values(), key=lambda v: v["lps_per_s"])
     line = {"metric": "batched PDLP LPs/s at 1e-4 (one persistent launch)",
             "value": best["lps_per_s"], "unit": "LPs/s", "higher_is_better": True,
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
-            "config": dict(cfg, tol=tol), "batch": out, "sequential_fp64": seq,
-            "speedup_vs_sequential": {a: out[f"fp64_{a}"]["lps_per_s"] / seq[a]["lps_per_s"]
-                                      for a in seq}}
+            "config": dict(cfg, tol=tol), "batch": out, "sequential": seq,
+            "speedup_vs_sequential": {key: out[key]["lps_per_s"] / seq[key]["lps_per_s"]
+                                      for key in seq}}
     return _device_clock_line(line, clk)
 
 

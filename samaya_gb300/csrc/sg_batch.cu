@@ -89,11 +89,13 @@ __device__ __forceinline__ double bmax(double v, double* sh) {
 }
 
 // For every row r < rows of a CSR (ptr, idx, val): s = sum_k prod(val_k, idx_k) (or max), then
-// f(r, s). Thread per row; rows longer than 32 nonzeros by their warp.
+// f(r, s). Thread per row; rows longer than 32 nonzeros by their warp. The sums are taken in
+// prod's result type (FP32 for the FP32 steps: GB300's FP64 pipe is small).
 template <bool MAXRED, typename T, typename Prod, typename F>
 __device__ __forceinline__ void block_rows(int rows, const int* __restrict__ ptr,
                                            const int* __restrict__ idx, const T* __restrict__ val,
                                            const Prod& prod, F& f) {
+  using ACC = decltype(prod(val[0], 0));
   const int lane = threadIdx.x & 31;
   for (int base = 0; base < rows; base += kBT) {
     const int r = base + threadIdx.x;
@@ -105,9 +107,9 @@ __device__ __forceinline__ void block_rows(int rows, const int* __restrict__ ptr
     }
     const bool shortrow = valid && e - b <= 32;
     if (shortrow) {
-      double s = 0.0;
+      ACC s = ACC(0);
       for (int q = b; q < e; ++q) {
-        const double p = prod(val[q], idx[q]);
+        const ACC p = prod(val[q], idx[q]);
         s = MAXRED ? fmax(s, p) : s + p;
       }
       f(r, s);
@@ -118,14 +120,14 @@ __device__ __forceinline__ void block_rows(int rows, const int* __restrict__ ptr
       pending &= pending - 1u;
       const int rb = __shfl_sync(0xffffffffu, b, src);
       const int re = __shfl_sync(0xffffffffu, e, src);
-      double s = 0.0;
+      ACC s = ACC(0);
       for (int q = rb + lane; q < re; q += 32) {
-        const double p = prod(val[q], idx[q]);
+        const ACC p = prod(val[q], idx[q]);
         s = MAXRED ? fmax(s, p) : s + p;
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const double t = __shfl_down_sync(0xffffffffu, s, o);
+        const ACC t = __shfl_down_sync(0xffffffffu, s, o);
         s = MAXRED ? fmax(s, t) : s + t;
       }
       if (lane == 0) f(base + (threadIdx.x & ~31) + src, s);
@@ -434,19 +436,18 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
     const T tsig = static_cast<T>(sigma), ttau = static_cast<T>(tau);
     // Dual step (rows of A_eq) with the logicals' primal update.
     {
+      // Products and sums in the storage type.
       struct G {
         const T* x;
-        __device__ double operator()(T a, int j) const {
-          return static_cast<double>(a) * static_cast<double>(x[j]);
-        }
+        __device__ T operator()(T a, int j) const { return a * x[j]; }
       } gx{Vbar};
       const T* yv = Y(p);
       T* yn = Y(p ^ 1);
       const T* vr = V(p) + n;
       T* vrn = V(p ^ 1) + n;
       T* vbr = Vbar + n;
-      auto f = [&](int i, double s) {
-        const T res = static_cast<T>(s) - vbr[i];
+      auto f = [&](int i, T s) {
+        const T res = s - vbr[i];
         const T ynew = yv[i] + tsig * res;
         yn[i] = ynew;
         const T r = vr[i];
@@ -464,15 +465,13 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
     {
       struct G {
         const T* y;
-        __device__ double operator()(T a, int i) const {
-          return static_cast<double>(a) * static_cast<double>(y[i]);
-        }
+        __device__ T operator()(T a, int i) const { return a * y[i]; }
       } gy{Y(p ^ 1)};
       const T* x = V(p);
       T* xn = V(p ^ 1);
-      auto f = [&](int j, double s) {
+      auto f = [&](int j, T s) {
         const T xo = x[j];
-        T v = xo - ttau * (ce[j] + static_cast<T>(s));
+        T v = xo - ttau * (ce[j] + s);
         v = fmin(fmax(v, le[j]), ue[j]);
         xn[j] = v;
         Vbar[j] = v + (v - xo);

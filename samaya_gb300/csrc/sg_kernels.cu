@@ -183,13 +183,21 @@ __device__ __forceinline__ StepScalars<ACC> step_scalars(const Ctl* __restrict__
     __syncthreads();
     return sh;
   } else {
-    // FP32: per thread, the average weight by an FP32 division (the shared-memory broadcast
-    // above put a dependent load and a barrier in front of every CTA's first load: slower).
-    StepScalars<ACC> s;
-    s.sigma = static_cast<ACC>(ctl->sigma);
-    s.tau = static_cast<ACC>(ctl->tau);
-    s.alpha = ACC(1) / static_cast<ACC>(k + 1);
-    s.beta = ACC(1) - s.alpha;
+    // FP32: lane 0 of each warp converts and divides, the warp shuffles the results (the
+    // shared-memory broadcast above put a dependent load and a barrier in front of every CTA's
+    // first load: slower; per thread, the FP64 -> FP32 and 64-bit integer conversions ran on
+    // the FP64 pipe in every thread). Every lane is active at kernel entry.
+    StepScalars<ACC> s{};
+    if ((threadIdx.x & 31) == 0) {
+      s.sigma = static_cast<ACC>(ctl->sigma);
+      s.tau = static_cast<ACC>(ctl->tau);
+      s.alpha = ACC(1) / static_cast<ACC>(k + 1);
+      s.beta = ACC(1) - s.alpha;
+    }
+    s.sigma = __shfl_sync(0xffffffffu, s.sigma, 0);
+    s.tau = __shfl_sync(0xffffffffu, s.tau, 0);
+    s.alpha = __shfl_sync(0xffffffffu, s.alpha, 0);
+    s.beta = __shfl_sync(0xffffffffu, s.beta, 0);
     return s;
   }
 }
