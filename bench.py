@@ -36,8 +36,10 @@ CPU_CAP_S = 20.0
 SWITCH_TOL = 3e-6
 ALGORITHM_NAMES = {
     "enhanced": "enhanced (inf-norm Ruiz + Pock-Chambolle, primal weight |c|/|b|)",
+    "halpern": "halpern (enhanced scaling, reflected Halpern PDHG)",
     "reference": "reference (samaya's L2 Ruiz, primal weight 1)",
 }
+ALGORITHM_IDS = {"reference": 0, "enhanced": 1, "halpern": 2}
 PRECISION_NAMES = {
     "mixed": "fp32 PDLP to the switch tolerance, then fp64 PDLP from its answer",
     "refined": "fp32 storage + fp64 iterative refinement",
@@ -50,7 +52,7 @@ def solver_options(args, precision):
     import samaya_gb300 as sg
     prec = {"mixed": sg.FP32_THEN_FP64, "refined": sg.FP32_REFINED, "fp64": sg.FP64}[precision]
     kw = {"inner_tol": args.switch_tol} if precision == "mixed" else {}
-    alg = sg.REFERENCE if getattr(args, "algorithm", "enhanced") == "reference" else sg.ENHANCED
+    alg = ALGORITHM_IDS[getattr(args, "algorithm", "enhanced")]
     return sg.PdlpOptions(tol=TOL, algorithm=alg, precision=prec,
                           max_iterations=getattr(args, "max_iterations", -1) if args.profile
                           else -1, **kw)
@@ -78,13 +80,17 @@ def parse():
                     help="iteration cap of the --profile solve (-1: none)")
     ap.add_argument("--tol", type=float, default=1e-8,
                     help="relative KKT tolerance of the single-LP workloads")
-    ap.add_argument("--algorithm", default="auto", choices=["auto", "enhanced", "reference"],
+    ap.add_argument("--algorithm", default="auto",
+                    choices=["auto", "enhanced", "halpern", "reference"],
                     help="enhanced: inf-norm Ruiz + Pock-Chambolle, primal weight |c|/|b|; "
+                         "halpern: enhanced with the reflected Halpern iteration; "
                          "reference: samaya's PDLP step for step; auto: the faster one for "
-                         "the workload (reference on the random sparse LPs, enhanced otherwise)")
+                         "the workload (halpern on the transportation LP, reference on the "
+                         "random sparse LPs, enhanced otherwise)")
     args = ap.parse_args()
     if args.algorithm == "auto":
-        args.algorithm = "reference" if args.workload in ("random", "batchA") else "enhanced"
+        args.algorithm = {"transport": "halpern", "random": "reference",
+                          "batchA": "reference"}.get(args.workload, "enhanced")
     global TOL
     TOL = args.tol
     return args

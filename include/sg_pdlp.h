@@ -75,10 +75,15 @@ typedef struct sg_pdlp_opts {
 /* Algorithm variants. REFERENCE follows samaya's PDLP step for step (L2 Ruiz, fixed step
  * 0.99 / ||[A -I]||, primal weight 1 updated at restarts, the 0.2 / 0.8 / 0.36 restarts);
  * ENHANCED replaces the preconditioning by infinity-norm Ruiz + Pock-Chambolle (alpha = 1)
- * and starts the primal weight at |c| / |b|; everything else is the same. */
+ * and starts the primal weight at |c| / |b|; everything else is the same. HALPERN is ENHANCED
+ * with the reflected Halpern iteration z+ = lambda (2 T(z) - z) + (1 - lambda) z0 in place
+ * of the running average (T the PDHG map, z0 the restart point, lambda = (k+1)/(k+2));
+ * termination, restarts and the answer use T(z); no infeasibility / unboundedness checks.
+ * The batched engine runs HALPERN requests as ENHANCED. */
 enum {
   SG_ALGORITHM_REFERENCE = 0,
-  SG_ALGORITHM_ENHANCED = 1
+  SG_ALGORITHM_ENHANCED = 1,
+  SG_ALGORITHM_HALPERN = 2
 };
 
 /* Result: the scalars of samaya::PdlpResult (reference src/lp/pdlp.hpp:19-30) plus counters. */

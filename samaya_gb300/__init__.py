@@ -4,7 +4,8 @@ The engine (CUDA for sm_103a behind the C ABI in include/sg_pdlp.h) replaces the
 PDLP path: ``samaya::solve_pdlp`` (src/lp/pdlp.cpp) and its GPU back end (src/gpu/).
 """
 from .model import LpProblem, Model  # noqa: F401
-from .pdlp import (ENHANCED, FP32_REFINED, FP32_THEN_FP64, FP64, REFERENCE, INFEASIBLE,  # noqa: F401
+from .pdlp import (ENHANCED, FP32_REFINED, FP32_THEN_FP64, FP64, HALPERN, REFERENCE,  # noqa: F401
+                   INFEASIBLE,
                    ITERATION_LIMIT, NUMERICAL_ERROR,
                    OPTIMAL, STATUS_NAMES, TIME_LIMIT, UNBOUNDED, PdhgDevice, PdlpOptions,
                    PdlpResult, PdlpSolver, gpu_info, solve_pdlp)

@@ -270,7 +270,7 @@ int Batch::create(Batch** out, int nmat, const int* mat_m, const int* mat_n,
   v.total_nnz = total_nnz;
   v.max_iter = max_iter;
   v.tol = tol;
-  v.algorithm = algorithm;
+  v.algorithm = algorithm != 0 ? 1 : 0;  // Halpern requests run as ENHANCED here
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -35,7 +35,9 @@ sg::Options to_options(const sg_pdlp_opts* o) {
   opt.refine_max_rounds = o->refine_max_rounds > 0 ? o->refine_max_rounds : 6;
   opt.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
   opt.verbose = o->verbose;
-  opt.algorithm = o->algorithm == SG_ALGORITHM_ENHANCED ? 1 : 0;
+  opt.algorithm = o->algorithm == SG_ALGORITHM_ENHANCED  ? 1
+                  : o->algorithm == SG_ALGORITHM_HALPERN ? 2
+                                                         : 0;
   opt.autotune = o->autotune != 0;
   opt.tile_split = o->tile_split > 0 ? o->tile_split : 0;
   return opt;

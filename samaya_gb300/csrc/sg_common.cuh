@@ -116,7 +116,8 @@ struct Ctl {
   double ir_dp, ir_dd, ir_dp_prev, ir_dd_prev;
   double ir_omega0;
   int no_detect;  // 1: no infeasibility/unboundedness checks (the refinement's inner solves)
-  int pad1;
+  int halpern;    // 1: reflected Halpern PDHG (the answer and restarts use T(z), the second
+                  // evaluated iterate; the Halpern iterate itself may leave the bounds)
   // Stall test of the FP32 solves: stop when the better iterate's largest relative residual has
   // not fallen below 0.8 x its best for stall_limit evaluations (0: off).
   double stall_best;

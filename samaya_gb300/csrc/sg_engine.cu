@@ -717,6 +717,10 @@ int Engine::setup_device(const double* rhs_orig) {
   h.kkt_previous = INFINITY;
   h.status = kRunning;
   h.omega = 1.0;
+  // Halpern: no infeasibility / unboundedness checks (they read differences of consecutive
+  // PDHG iterates, which the Halpern iterates are not).
+  h.halpern = opt_.algorithm == 2 ? 1 : 0;
+  h.no_detect = h.halpern;
   SG_TRY(cudaMemcpyAsync(ctl_, &h, sizeof(Ctl), cudaMemcpyHostToDevice, s));
   SG_TRY(cudaStreamSynchronize(s));  // h lives on this stack frame
   const OpView<double> K = K_.view64();
@@ -733,7 +737,7 @@ int Engine::setup_device(const double* rhs_orig) {
   }
   launch_setup_norms(ctl_, K, Kt, cost_orig_, red, grid_k_, grid_t_, s);
   if (m_ > 0 && n_ > 0) {
-    if (opt_.algorithm == 1) {
+    if (opt_.algorithm >= 1) {
       launch_enhanced_scaling(K, Kt, rs_, cs_, rn_, cn_, grid_k_, grid_t_, s);
     } else {
       for (int pass = 0; pass < 10; ++pass) {
@@ -751,7 +755,7 @@ int Engine::setup_device(const double* rhs_orig) {
                            cudaMemcpyDeviceToDevice, s));
   }
   launch_power_iteration(ctl_, K, Kt, pu_, pv_, red, 20, grid_k_, grid_t_, s);
-  if (opt_.algorithm == 1) {
+  if (opt_.algorithm >= 1) {
     launch_primal_weight_init(ctl_, n_, m_, it64_.cost, it64_.lower, it64_.upper, red, s);
   }
   // Iterates start at zero (pdlp.cpp:323-329).
@@ -773,13 +777,18 @@ namespace {
 template <typename T>
 int enqueue_chunk(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
                   const EvalView& ev, const RedView& red, double* scratch_n, int gsk, int gst,
-                  int gk, int gt, cudaStream_t s) {
+                  int gk, int gt, bool halpern, cudaStream_t s) {
   int kernels = 0;
   for (int j = 0; j < kCheckFrequency; ++j) {
     if (K.ts.ntiles > 0) ++kernels;
     if (Kt.ts.ntiles > 0) ++kernels;
-    launch_dual_step(ctl, K, it, j, gsk, s);
-    launch_primal_step(ctl, Kt, it, j, gst, s);
+    if (halpern) {
+      launch_halpern_primal(ctl, Kt, it, j, gst, s);
+      launch_halpern_dual(ctl, K, it, j, gsk, s);
+    } else {
+      launch_dual_step(ctl, K, it, j, gsk, s);
+      launch_primal_step(ctl, Kt, it, j, gst, s);
+    }
   }
   launch_eval(ctl, K, Kt, it, ev, red, gk, gt, -1, s);
   launch_decide_a(ctl, s);
@@ -794,7 +803,7 @@ int enqueue_chunk(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterV
 void Engine::enqueue_chunk_body() {
   chunk_kernels_ = enqueue_chunk(ctl_, K_.view64(), Kt_.view64(), iter_view(it64_), eval_view(),
                                  red_view(), scratch_n_, grid_step_k_, grid_step_t_, grid_k_,
-                                 grid_t_, stream_);
+                                 grid_t_, opt_.algorithm == 2, stream_);
 }
 
 int Engine::capture_chunk() {
@@ -817,7 +826,7 @@ int Engine::capture_chunk32() {
   SG_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
   chunk32_kernels_ = enqueue_chunk(ctl32_, K_.view32(), Kt_.view32(), it, inner_eval_view(),
                                    red_view(), scratch_n_, grid_step_k_, grid_step_t_, grid_k_,
-                                   grid_t_, stream_);
+                                   grid_t_, opt_.algorithm == 2, stream_);
   SG_TRY(cudaStreamEndCapture(stream_, &chunk32_graph_));
   SG_TRY(cudaGraphInstantiate(&chunk32_exec_, chunk32_graph_, 0));
   return kOk;

@@ -34,7 +34,8 @@ struct Options {
   int refine_max_rounds = 6;
   double inner_tol = 1e-4;
   int verbose = 0;
-  int algorithm = 0;        // 0 the reference's PDLP, 1 enhanced preconditioning + weight
+  int algorithm = 0;        // 0 the reference's PDLP, 1 enhanced preconditioning + weight,
+                            // 2 as 1 with the reflected Halpern iteration
   bool autotune = true;     // time candidate tile shapes of large operators at create
   int tile_split = 0;       // built-in rule's team split of medium rows (0: a warp per row)
 };

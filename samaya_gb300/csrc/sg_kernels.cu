@@ -278,6 +278,165 @@ __global__ void __launch_bounds__(kBlock, step_min_blocks<T>(VAR, false)) primal
 }
 
 // ------------------------------------------------------------------------------------------
+// Reflected Halpern PDHG (the engine's SG_ALGORITHM_HALPERN; no reference counterpart). With
+// T the PDHG map z = (v, y) -> (v^, y^) (primal first: v^ = proj(v - tau (c - K'y)),
+// y^ = y + sigma (K (2 v^ - v) - q)) and z0 the point of the last restart, one iteration is
+//   z+ = lambda (2 T(z) - z) + (1 - lambda) z0,  lambda = (k + 1) / (k + 2)
+// (Halpern's iteration on the reflected map 2T - I, nonexpansive, so z -> a fixed point of T).
+// The primal launch runs first: x^ and the reflected 2 x^ - x (written to Vbar, the dual
+// launch's SpMV input) and x+ from y; then the dual launch: the logicals' r^ from the old y,
+// y^, and r+, y+. T(z) lands in Verg / Yerg, the evaluation's second iterate and the answer.
+
+// z+ = N + w (z0 - N) with N = 2 z^ - z the reflected point and w = 1 - lambda = 1 / (k + 2).
+template <typename ACC>
+__device__ __forceinline__ ACC halpern_mix(ACC reflected, ACC z0, ACC w) {
+  return reflected + w * (z0 - reflected);
+}
+
+template <>
+__device__ __forceinline__ double halpern_mix<double>(double reflected, double z0, double w) {
+  return fma(w, z0 - reflected, reflected);
+}
+
+template <typename T, typename ACC>
+struct HalpernPrimalEpi {
+  const T* x;
+  T* x_new;
+  T* xbar;   // 2 x^ - x, the dual launch's SpMV input
+  T* xhat;   // x^ (T(z)'s primal part)
+  const T* x0;
+  const T* c;
+  const T* l;
+  const T* u;
+  ACC tau, w;
+  struct Pre {
+    ACC x, c, l, u, x0;
+  };
+  __device__ __forceinline__ Pre load(int j) const {
+    Pre p;
+    p.x = static_cast<ACC>(x[j]);
+    p.c = static_cast<ACC>(c[j]);
+    p.l = static_cast<ACC>(l[j]);
+    p.u = static_cast<ACC>(u[j]);
+    p.x0 = static_cast<ACC>(x0[j]);
+    return p;
+  }
+  __device__ __forceinline__ void row(int j, const ACC (&s)[1], const Pre& p) {
+    const ACC xh = clampv<ACC>(p.x - tau * (p.c + s[0]), p.l, p.u);
+    const ACC refl = extrapolate<ACC>(xh, p.x);
+    xhat[j] = static_cast<T>(xh);
+    xbar[j] = static_cast<T>(refl);
+    x_new[j] = static_cast<T>(halpern_mix<ACC>(refl, p.x0, w));
+  }
+  __device__ __forceinline__ void row(int j, const ACC (&s)[1]) { row(j, s, load(j)); }
+  __device__ __forceinline__ void long_row(int, int j, const ACC (&s)[1]) { row(j, s); }
+};
+
+template <typename T, typename ACC>
+struct HalpernDualEpi {
+  const T* y;
+  T* y_new;
+  T* yhat;
+  const T* y0;
+  const T* vr;   // r (n offset applied)
+  T* vr_new;
+  T* vr_hat;
+  const T* r0;
+  const T* c;
+  const T* l;
+  const T* u;
+  const T* q;
+  ACC sigma, tau, w;
+  struct Pre {
+    ACC y, r, c, l, u, q, y0, r0;
+  };
+  __device__ __forceinline__ Pre load(int i) const {
+    Pre p;
+    p.y = static_cast<ACC>(y[i]);
+    p.r = static_cast<ACC>(vr[i]);
+    p.c = static_cast<ACC>(c[i]);
+    p.l = static_cast<ACC>(l[i]);
+    p.u = static_cast<ACC>(u[i]);
+    p.q = q != nullptr ? static_cast<ACC>(q[i]) : ACC(0);
+    p.y0 = static_cast<ACC>(y0[i]);
+    p.r0 = static_cast<ACC>(r0[i]);
+    return p;
+  }
+  __device__ __forceinline__ void row(int i, const ACC (&s)[1], const Pre& p) {
+    // The logical's primal step uses the old dual (primal first), then the dual step sees the
+    // row's reflected logical: K (2 v^ - v) = A (2 x^ - x) - (2 r^ - r).
+    const ACC rh = clampv<ACC>(p.r - tau * (p.c - p.y), p.l, p.u);
+    const ACC rrefl = extrapolate<ACC>(rh, p.r);
+    ACC res = s[0] - rrefl;
+    if (q != nullptr) res -= p.q;
+    const ACC yh = p.y + sigma * res;
+    yhat[i] = static_cast<T>(yh);
+    vr_hat[i] = static_cast<T>(rh);
+    y_new[i] = static_cast<T>(halpern_mix<ACC>(extrapolate<ACC>(yh, p.y), p.y0, w));
+    vr_new[i] = static_cast<T>(halpern_mix<ACC>(rrefl, p.r0, w));
+  }
+  __device__ __forceinline__ void row(int i, const ACC (&s)[1]) { row(i, s, load(i)); }
+  __device__ __forceinline__ void long_row(int, int i, const ACC (&s)[1]) { row(i, s); }
+};
+
+template <typename T, int VAR>
+__global__ void __launch_bounds__(kBlock, step_min_blocks<T>(VAR, false)) halpern_primal_kernel(
+    const Ctl* __restrict__ ctl, OpView<T> Kt, IterView<T> it, int j) {
+  if (ctl->done) return;
+  const long long t = ctl->t + j;
+  if (t >= ctl->max_iter) return;
+  using ACC = Acc<T>;
+  const int p = static_cast<int>(t & 1);
+  // alpha = 1 / (k' + 1) with k' = k + 1: the Halpern weight 1 / (k + 2).
+  const StepScalars<ACC> sc = step_scalars<ACC>(ctl, ctl->k + j + 1);
+  HalpernPrimalEpi<T, ACC> epi;
+  epi.x = it.v(p);
+  epi.x_new = it.v(p ^ 1);
+  epi.xbar = it.Vbar;
+  epi.xhat = it.Verg;
+  epi.x0 = it.Vrst;
+  epi.c = it.cost;
+  epi.l = it.lower;
+  epi.u = it.upper;
+  epi.tau = sc.tau;
+  epi.w = sc.alpha;
+  Gather1<T, ACC> g{it.y(p)};
+  run_tiles<T, ACC, 1, Gather1<T, ACC>, HalpernPrimalEpi<T, ACC>, false, VAR == 1>(
+      Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
+}
+
+template <typename T, int VAR>
+__global__ void __launch_bounds__(kBlock, step_min_blocks<T>(VAR, true)) halpern_dual_kernel(
+    const Ctl* __restrict__ ctl, OpView<T> K, IterView<T> it, int j) {
+  if (ctl->done) return;
+  const long long t = ctl->t + j;
+  if (t >= ctl->max_iter) return;
+  using ACC = Acc<T>;
+  const int p = static_cast<int>(t & 1);
+  const StepScalars<ACC> sc = step_scalars<ACC>(ctl, ctl->k + j + 1);
+  HalpernDualEpi<T, ACC> epi;
+  const int n = it.n;
+  epi.y = it.y(p);
+  epi.y_new = it.y(p ^ 1);
+  epi.yhat = it.Yerg;
+  epi.y0 = it.Yrst;
+  epi.vr = it.v(p) + n;
+  epi.vr_new = it.v(p ^ 1) + n;
+  epi.vr_hat = it.Verg + n;
+  epi.r0 = it.Vrst + n;
+  epi.c = it.cost + n;
+  epi.l = it.lower + n;
+  epi.u = it.upper + n;
+  epi.q = it.rhs;
+  epi.sigma = sc.sigma;
+  epi.tau = sc.tau;
+  epi.w = sc.alpha;
+  Gather1<T, ACC> g{it.Vbar};
+  run_tiles<T, ACC, 1, Gather1<T, ACC>, HalpernDualEpi<T, ACC>, false, VAR == 1>(
+      K.ts, K.ptr, K.idx, K.val, g, epi);
+}
+
+// ------------------------------------------------------------------------------------------
 // Evaluation (pdhg_core.cu:102-144 / pdlp.cpp:411-488): the seven sums of the current and the
 // average iterate in the space before equilibration, plus the restart distances, from one
 // pass over each operator (both iterates share the matrix read).
@@ -669,7 +828,7 @@ __global__ void decide_a_kernel(Ctl* c) {
     c->meas[0][q] = wc[q];
     c->meas[1][q] = wa[q];
   }
-  if (converged(cur, c->tol)) {
+  if (!c->halpern && converged(cur, c->tol)) {
     set_answer(c, kOptimal, cur, t_new, 0);
     c->t = t_new;
     return;
@@ -682,12 +841,13 @@ __global__ void decide_a_kernel(Ctl* c) {
   if (c->stall_limit > 0) {
     const double ec = fmax(fmax(cur.rp, cur.rd), fabs(cur.rg));
     const double ea = fmax(fmax(avg.rp, avg.rd), fabs(avg.rg));
-    const double e = fmin(ec, ea);
+    const bool use_avg = c->halpern || ea < ec;
+    const double e = use_avg ? ea : ec;
     if (e < 0.8 * c->stall_best) {
       c->stall_best = e;
       c->stall_evals = 0;
     } else if (++c->stall_evals >= c->stall_limit) {
-      set_answer(c, kIterationLimit, ea < ec ? avg : cur, t_new, ea < ec ? 1 : 0);
+      set_answer(c, kIterationLimit, use_avg ? avg : cur, t_new, use_avg ? 1 : 0);
       c->t = t_new;
       return;
     }
@@ -725,8 +885,8 @@ __global__ void decide_b_kernel(Ctl* c) {
   const double omega = c->omega;
   const double kkt_cur = kkt_weighted(omega, cur);
   const double kkt_avg = kkt_weighted(omega, avg);
-  const bool to_average = kkt_avg < kkt_cur;
-  const double cand = fmin(kkt_cur, kkt_avg);
+  const bool to_average = c->halpern || kkt_avg < kkt_cur;
+  const double cand = to_average ? kkt_avg : kkt_cur;
   if (!(c->kkt_at_restart < INFINITY)) c->kkt_at_restart = cand;
   const bool restart = cand <= 0.2 * c->kkt_at_restart ||
                        (cand <= 0.8 * c->kkt_at_restart && cand > c->kkt_previous) ||
@@ -752,12 +912,14 @@ __global__ void decide_b_kernel(Ctl* c) {
     c->k = k_new;
   }
   c->t = t_new;
+  // Halpern: the answer is T(z) (within the bounds), not the Halpern iterate.
+  const int ans = c->halpern ? 1 : 0;
   if (c->t >= c->max_iter) {
-    set_answer(c, kIterationLimit, cur, c->max_iter, 0);
+    set_answer(c, kIterationLimit, ans ? avg : cur, c->max_iter, ans);
     return;
   }
   if (c->deadline_ns != 0ull && globaltimer_ns() > c->deadline_ns) {
-    set_answer(c, kTimeLimit, cur, c->t, 0);
+    set_answer(c, kTimeLimit, ans ? avg : cur, c->t, ans);
   }
 }
 
@@ -1397,6 +1559,14 @@ void configure_kernels() {
   cudaFuncSetAttribute(primal_step_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(dual_step_kernel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(primal_step_kernel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(halpern_dual_kernel<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(halpern_primal_kernel<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(halpern_dual_kernel<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(halpern_primal_kernel<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(halpern_dual_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(halpern_primal_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(halpern_dual_kernel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(halpern_primal_kernel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_farkas_cols_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_farkas_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(max_norm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
@@ -1428,6 +1598,30 @@ void launch_primal_step(const Ctl* ctl, const OpView<T>& Kt, const IterView<T>& 
     primal_step_kernel<T, 1><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
   } else {
     primal_step_kernel<T, 0><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
+  }
+}
+
+template <typename T>
+void launch_halpern_primal(const Ctl* ctl, const OpView<T>& Kt, const IterView<T>& it, int j,
+                           int grid, cudaStream_t s) {
+  if (Kt.ts.ntiles == 0) return;
+  const size_t sm = tile_smem_bytes(Kt.ts, 1, sizeof(T));
+  if (Kt.ts.variant == 1) {
+    halpern_primal_kernel<T, 1><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
+  } else {
+    halpern_primal_kernel<T, 0><<<grid, kBlock, sm, s>>>(ctl, Kt, it, j);
+  }
+}
+
+template <typename T>
+void launch_halpern_dual(const Ctl* ctl, const OpView<T>& K, const IterView<T>& it, int j,
+                         int grid, cudaStream_t s) {
+  if (K.ts.ntiles == 0) return;
+  const size_t sm = tile_smem_bytes(K.ts, 1, sizeof(T));
+  if (K.ts.variant == 1) {
+    halpern_dual_kernel<T, 1><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
+  } else {
+    halpern_dual_kernel<T, 0><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
   }
 }
 
@@ -1619,6 +1813,14 @@ template void launch_primal_step<double>(const Ctl*, const OpView<double>&,
                                          const IterView<double>&, int, int, cudaStream_t);
 template void launch_primal_step<float>(const Ctl*, const OpView<float>&, const IterView<float>&,
                                         int, int, cudaStream_t);
+template void launch_halpern_primal<double>(const Ctl*, const OpView<double>&,
+                                            const IterView<double>&, int, int, cudaStream_t);
+template void launch_halpern_primal<float>(const Ctl*, const OpView<float>&,
+                                           const IterView<float>&, int, int, cudaStream_t);
+template void launch_halpern_dual<double>(const Ctl*, const OpView<double>&,
+                                          const IterView<double>&, int, int, cudaStream_t);
+template void launch_halpern_dual<float>(const Ctl*, const OpView<float>&,
+                                         const IterView<float>&, int, int, cudaStream_t);
 template void launch_eval<double>(Ctl*, const OpView<double>&, const OpView<double>&,
                                   const IterView<double>&, const EvalView&, const RedView&, int,
                                   int, int, cudaStream_t);

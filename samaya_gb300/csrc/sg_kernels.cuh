@@ -64,6 +64,13 @@ void launch_dual_step(const Ctl* ctl, const OpView<T>& K, const IterView<T>& it,
 template <typename T>
 void launch_primal_step(const Ctl* ctl, const OpView<T>& Kt, const IterView<T>& it, int j,
                         int grid, cudaStream_t s);
+// Reflected Halpern PDHG steps (primal launch first, then dual; see sg_kernels.cu).
+template <typename T>
+void launch_halpern_primal(const Ctl* ctl, const OpView<T>& Kt, const IterView<T>& it, int j,
+                           int grid, cudaStream_t s);
+template <typename T>
+void launch_halpern_dual(const Ctl* ctl, const OpView<T>& K, const IterView<T>& it, int j,
+                         int grid, cudaStream_t s);
 template <typename T>
 void launch_eval(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
                  const EvalView& ev, const RedView& red, int grid_k, int grid_t,

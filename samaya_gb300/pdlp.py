@@ -27,6 +27,7 @@ FP32_REFINED = 1
 FP32_THEN_FP64 = 2
 REFERENCE = 0
 ENHANCED = 1
+HALPERN = 2
 
 
 @dataclass

@@ -149,25 +149,32 @@ def test_random_sparse_lp_objective_vs_dual_simplex(engine):
         assert abs(obj - ref_obj) <= 1e-4 * (1 + abs(ref_obj)), (obj, ref_obj)
 
 
-@pytest.mark.parametrize("precision", ["FP32_REFINED", "FP32_THEN_FP64"])
-def test_mixed_precision_reaches_fp64_tolerance(engine, precision):
-    """The FP32 paths (refinement; FP32 phase then FP64 phase) on the 200 x 500 random sparse LPs
-    at 1e-8: the FP64 relative KKT of the answer meets 1e-8, and the objective agrees with the
-    reference dual simplex to 1e-6 relative."""
+@pytest.mark.parametrize("precision,algorithm", [("FP32_REFINED", "ENHANCED"),
+                                                  ("FP32_THEN_FP64", "ENHANCED"),
+                                                  ("FP64", "HALPERN"),
+                                                  ("FP32_THEN_FP64", "HALPERN")])
+def test_mixed_precision_reaches_fp64_tolerance(engine, precision, algorithm):
+    """The FP32 paths (refinement; FP32 phase then FP64 phase) and the reflected Halpern
+    iteration on the 200 x 500 random sparse LPs at 1e-8: the FP64 relative KKT of the answer
+    meets 1e-8, the answer lies within its bounds, and the objective agrees with the reference
+    dual simplex to 1e-6 relative."""
     for case in load_group("config0_small"):
         opts = engine.PdlpOptions(tol=1e-8, precision=getattr(engine, precision),
-                                  algorithm=engine.ENHANCED)
+                                  algorithm=getattr(engine, algorithm))
         r = engine.solve_pdlp(case.lp, opts)
         assert r.status == engine.OPTIMAL, (precision, r.status_name, r.iterations)
         assert max(r.primal_residual, r.dual_residual, abs(r.gap)) < 1e-8
+        slack = 1e-9 * (1.0 + np.abs(r.x))  # the unscaling's round-off
+        assert np.all(r.x >= case.lp.lower - slack) and np.all(r.x <= case.lp.upper + slack)
         ref_obj = float(case.simplex[1])
         obj = model_objective(case, r.x)
         assert abs(obj - ref_obj) <= 1e-6 * (1 + abs(ref_obj)), (obj, ref_obj)
 
 
 def test_transport_mixed_precision_matches_fp64():
-    """A 100 x 200 transportation LP at 1e-8: both FP32 paths reach the FP64 path's objective to
-    1e-7 relative, and repeated runs of each path are bit-identical."""
+    """A 100 x 200 transportation LP at 1e-8: both FP32 paths and the Halpern iteration (FP64
+    and FP32 then FP64) reach the FP64 path's objective to 1e-7 relative, and repeated runs of
+    each are bit-identical."""
     import samaya_gb300 as sg
     from samaya_gb300.generators import transportation_lp
     from samaya_gb300.problem import make_problem
@@ -176,8 +183,9 @@ def test_transport_mixed_precision_matches_fp64():
     r64 = sg.solve_pdlp(lp, base)
     assert r64.status == sg.OPTIMAL
     o64 = float(np.dot(lp.cost, r64.x))
-    for prec in (sg.FP32_REFINED, sg.FP32_THEN_FP64):
-        opts = sg.PdlpOptions(tol=1e-8, algorithm=sg.ENHANCED, precision=prec)
+    for prec, alg in ((sg.FP32_REFINED, sg.ENHANCED), (sg.FP32_THEN_FP64, sg.ENHANCED),
+                      (sg.FP64, sg.HALPERN), (sg.FP32_THEN_FP64, sg.HALPERN)):
+        opts = sg.PdlpOptions(tol=1e-8, algorithm=alg, precision=prec)
         a = sg.solve_pdlp(lp, opts)
         b = sg.solve_pdlp(lp, opts)
         assert a.status == sg.OPTIMAL, (prec, a.status_name)
@@ -201,8 +209,8 @@ def test_solutions_pass_the_reference_verifier(engine):
     (tests/test_pdlp.cpp:497-540, which sends an answer that fails verification to crossover and
     the dual simplex) is that at least 80% pass; its own CPU PDLP passes every one of these, and
     so must the engine with the reference algorithm in FP64. Every precision mode with the
-    enhanced algorithm must reach the 80% bar on the 50 pdlp_random_feasible LPs and the 200 x
-    500 random sparse LPs together."""
+    enhanced algorithm, and the Halpern iteration, must reach the 80% bar on the 50
+    pdlp_random_feasible LPs and the 200 x 500 random sparse LPs together."""
     from samaya_gb300.problem import Scaling
     cases = [("feasible8", c) for c in load_group("feasible8") if c.ref_status == engine.OPTIMAL]
     cases += [("config0_small", c) for c in load_group("config0_small")]
@@ -210,7 +218,9 @@ def test_solutions_pass_the_reference_verifier(engine):
     modes = [("fp64-reference", engine.FP64, engine.REFERENCE)] + [
         (f"{name}-enhanced", prec, engine.ENHANCED) for name, prec in (
             ("fp64", engine.FP64), ("fp32-then-fp64", engine.FP32_THEN_FP64),
-            ("fp32-refined", engine.FP32_REFINED))]
+            ("fp32-refined", engine.FP32_REFINED))] + [
+        ("fp64-halpern", engine.FP64, engine.HALPERN),
+        ("fp32-then-fp64-halpern", engine.FP32_THEN_FP64, engine.HALPERN)]
     for mode, prec, alg in modes:
         failures[mode] = []
         for grp, case in cases:
