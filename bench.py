@@ -202,20 +202,23 @@ def traffic_summary():
         return {}
 
 
-def primal_step_bytes(lp, value_bytes):
+def primal_step_bytes(lp, value_bytes, halpern=False):
     """Compulsory bytes of one primal-step launch (rows of A' = the n columns): the nonzeros
     (value + int32 index), the n + 1 row starts, the m duals gathered once, and the column
-    epilogue: c, l, u, x, x_avg read; x_new, x_bar, x_avg written (8 n-vectors)."""
+    epilogue, 8 n-vectors: c, l, u, x, x_avg read and x_new, x_bar, x_avg written (classic);
+    c, l, u, x, x0 read and x_new, x_bar, x_hat written (Halpern)."""
     n, m, nnz = lp.n, lp.m, lp.nnz
     return nnz * (value_bytes + 4) + (n + 1) * 4 + m * value_bytes + 8 * n * value_bytes
 
 
-def dual_step_bytes(lp, value_bytes):
+def dual_step_bytes(lp, value_bytes, halpern=False):
     """Rows of A: nonzeros, m + 1 starts, x_bar gathered once (n), and the row epilogue:
-    y, r, r_bar, c_r, l_r, u_r, y_avg, r_avg read; y_new, r_new, r_bar, y_avg, r_avg written
-    (13 m-vectors; +1 with a right-hand side)."""
+    classic, 13 m-vectors (y, r, r_bar, c_r, l_r, u_r, y_avg, r_avg read; y_new, r_new, r_bar,
+    y_avg, r_avg written); Halpern, 11 (y, r, c_r, l_r, u_r, y0, r0 read; y_new, r_new, y_hat,
+    r_hat written). (The solves here have no right-hand side vector, which adds one.)"""
     n, m, nnz = lp.n, lp.m, lp.nnz
-    return nnz * (value_bytes + 4) + (m + 1) * 4 + n * value_bytes + 14 * m * value_bytes
+    vecs = 11 if halpern else 13
+    return nnz * (value_bytes + 4) + (m + 1) * 4 + n * value_bytes + vecs * m * value_bytes
 
 
 def cpu_reference_run(lp, cap_s=CPU_CAP_S):
@@ -472,21 +475,23 @@ def main():
     # Roofline of the dominant kernel: event-timed launches on the engine's stream.
     ms_dual, ms_primal, ms_eval = solver.time_kernels(20)
     vb = 4 if mixed else 8
-    pbytes = primal_step_bytes(lp, vb)
-    dbytes = dual_step_bytes(lp, vb)
+    halpern = args.algorithm == "halpern"
+    pbytes = primal_step_bytes(lp, vb, halpern)
+    dbytes = dual_step_bytes(lp, vb, halpern)
     peak, peak_kind = peak_hbm()
     # Both step kernels launch once per iteration: the dominant one is the slower.
     prec_key = "fp32" if mixed else "fp64"
     traffic = traffic_summary()
+    tkey = f"{args.workload}_{prec_key}" + ("_halpern" if halpern else "")
     steps = {
         "primal_step": {"kernel": "primal_step (A'y + projected x update + averages)",
                         "bytes_per_launch": pbytes, "ms_per_launch": ms_primal,
                         "achieved": pbytes / (ms_primal * 1e-3) / 1e9,
-                        "traffic": traffic.get(f"{args.workload}_{prec_key}_primal_step")},
+                        "traffic": traffic.get(f"{tkey}_primal_step")},
         "dual_step": {"kernel": "dual_step (A xbar + y update + logicals + averages)",
                       "bytes_per_launch": dbytes, "ms_per_launch": ms_dual,
                       "achieved": dbytes / (ms_dual * 1e-3) / 1e9,
-                      "traffic": traffic.get(f"{args.workload}_{prec_key}_dual_step")},
+                      "traffic": traffic.get(f"{tkey}_dual_step")},
     }
     top = max(steps, key=lambda k: steps[k]["ms_per_launch"])
     other = "dual_step" if top == "primal_step" else "primal_step"

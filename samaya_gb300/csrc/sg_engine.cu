@@ -4,6 +4,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <limits>
 #include <map>
 #include <mutex>
@@ -363,6 +365,43 @@ struct ShapeKey {
 
 std::mutex g_shape_mu;
 std::map<ShapeKey, TileShape> g_shape_cache;
+bool g_shape_file_read = false;
+
+// SG_TILE_CACHE names a text file that carries the tuner's choices across processes (so that a
+// profiler run, whose launches cannot be timed, uses the shapes a plain run picked): one line
+// per operator, the key's seven fields then the shape's five. Read once per process, appended
+// after each tuning. Call with g_shape_mu held.
+void read_shape_file() {
+  if (g_shape_file_read) return;
+  g_shape_file_read = true;
+  const char* path = std::getenv("SG_TILE_CACHE");
+  if (path == nullptr || *path == '\0') return;
+  FILE* f = std::fopen(path, "r");
+  if (f == nullptr) return;
+  ShapeKey k{};
+  TileShape sh;
+  while (std::fscanf(f, "%d %lld %d %lld %lld %lld %d %d %d %d %d %d", &k.rows, &k.nnz,
+                     &k.max_len, &k.over32, &k.over128, &k.over4096, &k.fp32, &sh.cap_nnz,
+                     &sh.cap_rows, &sh.warp_min, &sh.variant, &sh.split) == 12) {
+    if (sh.cap_nnz >= 256 && sh.cap_nnz <= 4 * kTileNnz && sh.cap_rows >= 1 &&
+        sh.cap_rows <= kTileRows && sh.warp_min >= 32 && (sh.variant == 0 || sh.variant == 1) &&
+        sh.split >= 0) {
+      g_shape_cache[k] = sh;
+    }
+  }
+  std::fclose(f);
+}
+
+void append_shape_file(const ShapeKey& k, const TileShape& sh) {
+  const char* path = std::getenv("SG_TILE_CACHE");
+  if (path == nullptr || *path == '\0') return;
+  FILE* f = std::fopen(path, "a");
+  if (f == nullptr) return;
+  std::fprintf(f, "%d %lld %d %lld %lld %lld %d %d %d %d %d %d\n", k.rows, k.nnz, k.max_len,
+               k.over32, k.over128, k.over4096, k.fp32, sh.cap_nnz, sh.cap_rows, sh.warp_min,
+               sh.variant, sh.split);
+  std::fclose(f);
+}
 
 ShapeKey shape_key(const DevOp& op, bool fp32) {
   ShapeKey k{op.rows, op.nnz, 0, 0, 0, 0, fp32 ? 1 : 0};
@@ -496,6 +535,7 @@ int Engine::tune_tiles(std::string* err) {
     if (tune) {
       key = shape_key(*op, fp32_);
       std::lock_guard<std::mutex> lock(g_shape_mu);
+      read_shape_file();
       auto it = g_shape_cache.find(key);
       if (it != g_shape_cache.end()) {
         best = it->second;
@@ -559,6 +599,7 @@ int Engine::tune_tiles(std::string* err) {
       }
       std::lock_guard<std::mutex> lock(g_shape_mu);
       g_shape_cache[key] = best;
+      append_shape_file(key, best);
     }
     const int rc = set_tiles(op, best);
     if (rc != kOk) {
@@ -1410,19 +1451,34 @@ namespace {
 template <typename T>
 int time_steps(Ctl* c, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
                const EvalView& ev, const RedView& red, int gsk, int gst, int gk, int gt,
-               int reps, cudaStream_t s, double* ms) {
+               bool halpern, int reps, cudaStream_t s, double* ms) {
   cudaEvent_t e[4];
   for (auto& x : e) {
     if (cudaEventCreate(&x) != cudaSuccess) return kErrCuda;
   }
+  // The step kernels the solve runs (classic or Halpern).
+  auto dual = [&](int r) {
+    if (halpern) {
+      launch_halpern_dual(c, K, it, r, gsk, s);
+    } else {
+      launch_dual_step(c, K, it, r, gsk, s);
+    }
+  };
+  auto primal = [&](int r) {
+    if (halpern) {
+      launch_halpern_primal(c, Kt, it, r, gst, s);
+    } else {
+      launch_primal_step(c, Kt, it, r, gst, s);
+    }
+  };
   for (int r = 0; r < 2; ++r) {
-    launch_dual_step(c, K, it, r, gsk, s);
-    launch_primal_step(c, Kt, it, r, gst, s);
+    dual(r);
+    primal(r);
   }
   cudaEventRecord(e[0], s);
-  for (int r = 0; r < reps; ++r) launch_dual_step(c, K, it, r & 1, gsk, s);
+  for (int r = 0; r < reps; ++r) dual(r & 1);
   cudaEventRecord(e[1], s);
-  for (int r = 0; r < reps; ++r) launch_primal_step(c, Kt, it, r & 1, gst, s);
+  for (int r = 0; r < reps; ++r) primal(r & 1);
   cudaEventRecord(e[2], s);
   for (int r = 0; r < reps; ++r) launch_eval(c, K, Kt, it, ev, red, gk, gt, 0, s);
   cudaEventRecord(e[3], s);
@@ -1457,10 +1513,12 @@ int Engine::time_kernels(int reps, double* ms_dual, double* ms_primal, double* m
     IterView<float> it = iter_view(it32_);
     it.rhs = it32_.rhs;
     rc = time_steps(c, K_.view32(), Kt_.view32(), it, inner_eval_view(), red_view(),
-                    grid_step_k_, grid_step_t_, grid_k_, grid_t_, reps, stream_, ms);
+                    grid_step_k_, grid_step_t_, grid_k_, grid_t_, opt_.algorithm == 2, reps,
+                    stream_, ms);
   } else {
     rc = time_steps(c, K_.view64(), Kt_.view64(), iter_view(it64_), eval_view(), red_view(),
-                    grid_step_k_, grid_step_t_, grid_k_, grid_t_, reps, stream_, ms);
+                    grid_step_k_, grid_step_t_, grid_k_, grid_t_, opt_.algorithm == 2, reps,
+                    stream_, ms);
   }
   if (rc != kOk) return rc;
   *ms_dual = ms[0];

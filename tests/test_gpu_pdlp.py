@@ -258,3 +258,38 @@ def test_autotuned_tiles_agree_with_the_built_in_rule(engine):
     o0 = float(np.dot(lp.cost, r0.x))
     o1 = float(np.dot(lp.cost, r1.x))
     assert abs(o0 - o1) <= 1e-3 * (1 + abs(o0)), (o0, o1)
+
+
+_TILE_CACHE_SCRIPT = """
+import sys
+sys.path.insert(0, {root!r})
+import samaya_gb300 as sg
+from samaya_gb300.generators import random_sparse_lp
+from samaya_gb300.problem import make_problem
+lp, _ = make_problem(random_sparse_lp(20000, 50000, seed=4))
+with sg.PdlpSolver(lp, sg.PdlpOptions(tol=1e-4, algorithm=sg.REFERENCE)) as s:
+    print(s.tile_shapes())
+"""
+
+
+def test_tile_cache_file_carries_the_tuned_shapes(tmp_path):
+    """SG_TILE_CACHE: a first process tunes the 20000 x 50000 LP's operators and appends its
+    choices to the file; a second process reads them instead of timing (same shapes, file not
+    grown)."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    path = tmp_path / "tiles.txt"
+    env = dict(os.environ, SG_TILE_CACHE=str(path))
+    script = _TILE_CACHE_SCRIPT.format(root=root)
+    first = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True,
+                           text=True, timeout=600)
+    assert first.returncode == 0, first.stderr
+    lines = path.read_text().splitlines()
+    assert len(lines) == 2 and all(len(x.split()) == 12 for x in lines), lines
+    second = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True,
+                            text=True, timeout=600)
+    assert second.returncode == 0, second.stderr
+    assert second.stdout == first.stdout
+    assert path.read_text().splitlines() == lines
