@@ -33,7 +33,7 @@ sys.path.insert(0, ROOT)
 METRIC = "PDLP time-to-1e-8 KKT (mixed vs FP64 GPU)"
 TOL = 1e-8
 CPU_CAP_S = 20.0
-SWITCH_TOL = 3e-6
+SWITCH_TOL = 1e-6
 ALGORITHM_NAMES = {
     "enhanced": "enhanced (inf-norm Ruiz + Pock-Chambolle, primal weight |c|/|b|)",
     "halpern": "halpern (enhanced scaling, reflected Halpern PDHG)",
