@@ -205,19 +205,22 @@ def traffic_summary():
 def primal_step_bytes(lp, value_bytes, halpern=False):
     """Compulsory bytes of one primal-step launch (rows of A' = the n columns): the nonzeros
     (value + int32 index), the n + 1 row starts, the m duals gathered once, and the column
-    epilogue, 8 n-vectors: c, l, u, x, x_avg read and x_new, x_bar, x_avg written (classic);
-    c, l, u, x, x0 read and x_new, x_bar, x_hat written (Halpern)."""
+    epilogue: classic, 8 n-vectors (c, l, u, x, x_avg read; x_new, x_bar, x_avg written);
+    Halpern, 7 (c, l, u, x, x0 read; x_new, x_bar written; x^ is written only by a chunk's last
+    step, before an evaluation)."""
     n, m, nnz = lp.n, lp.m, lp.nnz
-    return nnz * (value_bytes + 4) + (n + 1) * 4 + m * value_bytes + 8 * n * value_bytes
+    vecs = 7 if halpern else 8
+    return nnz * (value_bytes + 4) + (n + 1) * 4 + m * value_bytes + vecs * n * value_bytes
 
 
 def dual_step_bytes(lp, value_bytes, halpern=False):
     """Rows of A: nonzeros, m + 1 starts, x_bar gathered once (n), and the row epilogue:
     classic, 13 m-vectors (y, r, r_bar, c_r, l_r, u_r, y_avg, r_avg read; y_new, r_new, r_bar,
-    y_avg, r_avg written); Halpern, 11 (y, r, c_r, l_r, u_r, y0, r0 read; y_new, r_new, y_hat,
-    r_hat written). (The solves here have no right-hand side vector, which adds one.)"""
+    y_avg, r_avg written); Halpern, 9 (y, r, c_r, l_r, u_r, y0, r0 read; y_new, r_new written;
+    y^, r^ only by a chunk's last step). (The solves here have no right-hand side vector, which
+    adds one.)"""
     n, m, nnz = lp.n, lp.m, lp.nnz
-    vecs = 11 if halpern else 13
+    vecs = 9 if halpern else 13
     return nnz * (value_bytes + 4) + (m + 1) * 4 + n * value_bytes + vecs * m * value_bytes
 
 
