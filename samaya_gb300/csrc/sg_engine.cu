@@ -273,6 +273,16 @@ int Engine::create(Engine** out, int m, int n, const int64_t* colptr, const int3
   e->opt_ = opt;
   e->fp32_ = opt.precision == 1 || opt.precision == 2;
   e->switch_ = opt.precision == 2;
+  // Every structural column with the same bounds, each 0 or infinite (equilibration divides
+  // them by a positive factor, so they stay shared): the primal steps skip the bound vectors.
+  if (n > 0) {
+    const double lo = lower[0], hi = upper[0];
+    bool uniform = (lo == 0.0 || lo == -INFINITY) && (hi == 0.0 || hi == INFINITY);
+    for (int j = 1; uniform && j < n; ++j) uniform = lower[j] == lo && upper[j] == hi;
+    e->x_bounds_uniform_ = uniform;
+    e->x_lo_ = lo;
+    e->x_hi_ = hi;
+  }
   // K' = A^T by rows is the CSC of A; K = A by rows, by a stable counting sort.
   std::vector<int> tptr(static_cast<size_t>(n) + 1);
   for (int j = 0; j <= n; ++j) tptr[j] = static_cast<int>(colptr[j]);
@@ -700,6 +710,11 @@ IterView<T> Engine::iter_view(DevIter<T>& it) {
   v.rhs = nullptr;
   v.n = n_;
   v.m = m_;
+  // The shared column bounds hold for the problem itself (FP64 iterates, and the FP32 phase of
+  // the precision switch), not for the refinement's correction problems in the FP32 buffers.
+  v.xb_uniform = x_bounds_uniform_ && (std::is_same<T, double>::value || switch_) ? 1 : 0;
+  v.xb_lo = static_cast<T>(x_lo_);
+  v.xb_hi = static_cast<T>(x_hi_);
   return v;
 }
 

@@ -201,6 +201,8 @@ class Engine {
   int sm_count_ = 148;
   bool fp32_ = false;
   bool switch_ = false;   // FP32 PDLP, then FP64 PDLP from its answer
+  bool x_bounds_uniform_ = false;  // every structural column has the bounds [x_lo_, x_hi_]
+  double x_lo_ = 0.0, x_hi_ = 0.0;
   DevOp K_, Kt_;
   DevIter<double> it64_;
   DevIter<float> it32_;

@@ -124,14 +124,38 @@ struct DualEpi {
   __device__ __forceinline__ void long_row(int, int i, const ACC (&s)[1]) { row(i, s); }
 };
 
+// The bounds of column j: the shared pair when every column has it (no loads), else the
+// vectors.
+template <typename T, typename ACC>
+struct ColBounds {
+  const T* l;
+  const T* u;
+  int uniform;
+  ACC lo, hi;
+  __device__ __forceinline__ void load(int j, ACC& pl, ACC& pu) const {
+    if (uniform) {
+      pl = lo;
+      pu = hi;
+    } else {
+      pl = static_cast<ACC>(l[j]);
+      pu = static_cast<ACC>(u[j]);
+    }
+  }
+};
+
+template <typename T, typename ACC>
+__device__ __forceinline__ ColBounds<T, ACC> col_bounds(const IterView<T>& it) {
+  return ColBounds<T, ACC>{it.lower, it.upper, it.xb_uniform, static_cast<ACC>(it.xb_lo),
+                           static_cast<ACC>(it.xb_hi)};
+}
+
 template <typename T, typename ACC>
 struct PrimalEpi {
   const T* x;
   T* x_new;
   T* xbar;
   const T* c;
-  const T* l;
-  const T* u;
+  ColBounds<T, ACC> b;
   T* xerg;
   ACC tau, alpha, beta;
   struct Pre {
@@ -141,8 +165,7 @@ struct PrimalEpi {
     Pre p;
     p.x = static_cast<ACC>(x[j]);
     p.c = static_cast<ACC>(c[j]);
-    p.l = static_cast<ACC>(l[j]);
-    p.u = static_cast<ACC>(u[j]);
+    b.load(j, p.l, p.u);
     p.xerg = static_cast<ACC>(xerg[j]);
     return p;
   }
@@ -206,8 +229,8 @@ __device__ __forceinline__ StepScalars<ACC> step_scalars(const Ctl* __restrict__
 // tuner or the built-in rule):
 //   0: many CTAs per SM resident (operators of short rows, where occupancy hides the latency),
 //      as many as fit without spills: the primal step 6 (40 registers) in FP32 and 5 (48) in
-//      FP64; the dual step, whose epilogue preloads nine row values, 5 in FP32 and 4 (64) in
-//      FP64;
+//      FP64; the dual step, whose epilogue preloads eight or nine row values, 5 in FP32 and 3
+//      (80) in FP64;
 //   1: 128 registers, the warp-per-row and segment loops unrolled twice as deep (operators of
 //      long rows, whose few CTAs need more loads in flight each).
 // (Measured and not kept: a third variant loading a short row's first three pairs of
@@ -215,7 +238,7 @@ __device__ __forceinline__ StepScalars<ACC> step_scalars(const Ctl* __restrict__
 template <typename T>
 constexpr int step_min_blocks(int variant, bool dual) {
   if (variant == 1) return 2;
-  if (sizeof(T) == 8) return dual ? 4 : 5;
+  if (sizeof(T) == 8) return dual ? 3 : 5;
   return dual ? 5 : 6;
 }
 
@@ -266,8 +289,7 @@ __global__ void __launch_bounds__(kBlock, step_min_blocks<T>(VAR, false)) primal
   epi.x_new = it.v(p ^ 1);
   epi.xbar = it.Vbar;
   epi.c = it.cost;
-  epi.l = it.lower;
-  epi.u = it.upper;
+  epi.b = col_bounds<T, ACC>(it);
   epi.xerg = it.Verg;
   epi.tau = sc.tau;
   epi.alpha = sc.alpha;
@@ -314,8 +336,7 @@ struct HalpernPrimalEpi {
   T* xhat;   // x^ (T(z)'s primal part), written only when `hat`
   const T* x0;
   const T* c;
-  const T* l;
-  const T* u;
+  ColBounds<T, ACC> b;
   ACC tau, w;
   bool hat;
   struct Pre {
@@ -325,8 +346,7 @@ struct HalpernPrimalEpi {
     Pre p;
     p.x = static_cast<ACC>(x[j]);
     p.c = static_cast<ACC>(c[j]);
-    p.l = static_cast<ACC>(l[j]);
-    p.u = static_cast<ACC>(u[j]);
+    b.load(j, p.l, p.u);
     p.x0 = static_cast<ACC>(x0[j]);
     return p;
   }
@@ -408,8 +428,7 @@ __global__ void __launch_bounds__(kBlock, step_min_blocks<T>(VAR, false)) halper
   epi.xhat = it.Verg;
   epi.x0 = it.Vrst;
   epi.c = it.cost;
-  epi.l = it.lower;
-  epi.u = it.upper;
+  epi.b = col_bounds<T, ACC>(it);
   epi.tau = sc.tau;
   epi.w = sc.alpha;
   epi.hat = halpern_writes_hat(ctl, t, j);

@@ -30,6 +30,11 @@ struct IterView {
   const T* upper;  // n + m
   const T* rhs;    // m right-hand side q of [A -I] v = q (null: zero)
   int n, m;
+  // 1: every structural column has the bounds [xb_lo, xb_hi] (0 or infinite, so equilibration
+  // keeps them), and the primal steps read no bound vectors (16 MB an FP32 primal step of the
+  // transportation LP); 0: lower[j], upper[j].
+  int xb_uniform;
+  T xb_lo, xb_hi;
   // V[p], Y[p] by a select: indexing a kernel parameter's array with a runtime index makes
   // the compiler copy the whole view to local memory first.
   __host__ __device__ __forceinline__ T* v(int p) const { return p ? V[1] : V[0]; }
