@@ -229,16 +229,18 @@ __device__ __forceinline__ StepScalars<ACC> step_scalars(const Ctl* __restrict__
 // tuner or the built-in rule):
 //   0: many CTAs per SM resident (operators of short rows, where occupancy hides the latency),
 //      as many as fit without spills: the primal step 6 (40 registers) in FP32 and 5 (48) in
-//      FP64; the dual step, whose epilogue preloads eight or nine row values, 5 in FP32 and 3
-//      (80) in FP64;
+//      FP64; the dual step, whose epilogue preloads eight or nine row values, 5 in FP32 and 4
+//      (64) in FP64 (a few bytes spill; at 3 per SM, spill-free, the power-law LP's FP64 dual
+//      step took 108 us instead of 92);
 //   1: 128 registers, the warp-per-row and segment loops unrolled twice as deep (operators of
-//      long rows, whose few CTAs need more loads in flight each).
+//      long rows, whose few CTAs need more loads in flight each; at 3 CTAs per SM, 80
+//      registers, no faster on the transportation LP).
 // (Measured and not kept: a third variant loading a short row's first three pairs of
 // nonzeros together at 4 CTAs per SM; no faster on the transportation or power-law LPs.)
 template <typename T>
 constexpr int step_min_blocks(int variant, bool dual) {
   if (variant == 1) return 2;
-  if (sizeof(T) == 8) return dual ? 3 : 5;
+  if (sizeof(T) == 8) return dual ? 4 : 5;
   return dual ? 5 : 6;
 }
 
