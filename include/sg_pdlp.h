@@ -183,6 +183,15 @@ int sg_pdlp_time_kernels(sg_pdlp* handle, int reps, double* ms_dual, double* ms_
 int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_rows,
                        int* ntiles, int* variant, int* split);
 
+/* CSC -> CSR of an m x n matrix (the engine's row-major copy of A): row starts csr_ptr (m + 1),
+ * column indices csr_idx and values csr_val (a_colptr[n] each), every row's columns in
+ * increasing order, the result the reference's SparseMatrix::transpose gives
+ * (src/linalg/sparse_matrix.cpp:48-78). Checks the column starts, every row index and value;
+ * SG_ERR_INVALID_ARGUMENT when one is out of range or not finite. Host only (up to 16
+ * threads); no GPU needed. */
+int sg_csc_to_csr(int m, int n, const int64_t* a_colptr, const int32_t* a_rowidx,
+                  const double* a_val, int32_t* csr_ptr, int32_t* csr_idx, double* csr_val);
+
 /* Model -> LpProblem: samaya's power-of-two scaling and computational form, as
  * compute_scaling + make_problem compute them (reference src/linalg/scaling.cpp:130-200,
  * src/lp/lp_solver.cpp:28-51). The model is min/max obj'x s.t. row_lower <= A x <= row_upper,

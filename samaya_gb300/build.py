@@ -70,8 +70,8 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, list(extra_flags)), srcs))
     tmp = LIB_PATH + f".tmp{os.getpid()}"
-    subprocess.run([nvcc_path(), *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "static"],
-                   check=True)
+    subprocess.run([nvcc_path(), *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "static",
+                    "-lpthread"], check=True)
     os.replace(tmp, LIB_PATH)
     with open(stamp_path, "w") as f:
         f.write(digest)

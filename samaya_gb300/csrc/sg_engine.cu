@@ -14,6 +14,7 @@
 #include <type_traits>
 
 #include "sg_engine.cuh"
+#include "sg_transpose.h"
 #include "sg_refine.cuh"
 
 namespace sg {
@@ -245,13 +246,16 @@ int Engine::create(Engine** out, int m, int n, const int64_t* colptr, const int3
       return kErrInvalidArgument;
     }
   }
-  for (long long p = 0; p < nnz; ++p) {
-    if (rowidx[p] < 0 || rowidx[p] >= m) {
-      if (err) *err = "row index out of range";
-      return kErrInvalidArgument;
-    }
-    if (!std::isfinite(val[p])) {
-      if (err) *err = "matrix value not finite";
+  // K = A by rows (checking every row index and value on the way); K' = A^T by rows is the CSC
+  // of A.
+  std::vector<int> kptr(static_cast<size_t>(m) + 1, 0);
+  std::vector<int> kidx(static_cast<size_t>(std::max<long long>(nnz, 1)));
+  std::vector<double> kval(static_cast<size_t>(std::max<long long>(nnz, 1)));
+  {
+    const char* why = nullptr;
+    if (csc_to_csr(m, n, colptr, rowidx, val, kptr.data(), kidx.data(), kval.data(), 16,
+                   &why) != 0) {
+      if (err) *err = why;
       return kErrInvalidArgument;
     }
   }
@@ -283,24 +287,8 @@ int Engine::create(Engine** out, int m, int n, const int64_t* colptr, const int3
     e->x_lo_ = lo;
     e->x_hi_ = hi;
   }
-  // K' = A^T by rows is the CSC of A; K = A by rows, by a stable counting sort.
   std::vector<int> tptr(static_cast<size_t>(n) + 1);
   for (int j = 0; j <= n; ++j) tptr[j] = static_cast<int>(colptr[j]);
-  std::vector<int> kptr(static_cast<size_t>(m) + 1, 0);
-  for (long long p = 0; p < nnz; ++p) ++kptr[rowidx[p] + 1];
-  for (int i = 0; i < m; ++i) kptr[i + 1] += kptr[i];
-  std::vector<int> kidx(static_cast<size_t>(std::max<long long>(nnz, 1)));
-  std::vector<double> kval(static_cast<size_t>(std::max<long long>(nnz, 1)));
-  {
-    std::vector<int> next(kptr.begin(), kptr.end() - 1);
-    for (int j = 0; j < n; ++j) {
-      for (long long p = colptr[j]; p < colptr[j + 1]; ++p) {
-        const int q = next[rowidx[p]]++;
-        kidx[q] = j;
-        kval[q] = val[p];
-      }
-    }
-  }
   e->K_.rows = m;
   e->K_.cols = n;
   e->K_.nnz = nnz;

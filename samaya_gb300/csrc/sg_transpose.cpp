@@ -1,0 +1,132 @@
+// Host CSC -> CSR of the constraint matrix (the rows of K = A), checked and multi-threaded.
+//
+// The reference builds its row-major copy with a sequential counting sort,
+// SparseMatrix::transpose (src/linalg/sparse_matrix.cpp:48-78), before it uploads both operators
+// (src/gpu/pdhg_core.cu:172-190, 242-273). Here the same
+// stable counting sort runs over column ranges in parallel: every thread counts the rows of its
+// columns, a prefix over (row, thread) gives each thread its own slots in every row, and the
+// threads then place their entries in column order. The result is identical to the sequential
+// sort for any thread count (each row lists its columns in increasing order).
+#include "sg_transpose.h"
+
+#include <stdint.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <thread>
+#include <vector>
+
+#include "../../include/sg_pdlp.h"
+
+namespace sg {
+
+namespace {
+
+// Runs f(t) for t in [0, threads) on threads - 1 helpers and the caller.
+template <typename F>
+void parallel_for(int threads, const F& f) {
+  std::vector<std::thread> pool;
+  pool.reserve(static_cast<size_t>(std::max(0, threads - 1)));
+  for (int t = 1; t < threads; ++t) pool.emplace_back(f, t);
+  f(0);
+  for (auto& th : pool) th.join();
+}
+
+}  // namespace
+
+int csc_to_csr(int m, int n, const int64_t* colptr, const int32_t* rowidx, const double* val,
+               int* kptr, int* kidx, double* kval, int max_threads, const char** why) {
+  const long long nnz = colptr[n];
+  // Threads: one per ~512K nonzeros, at most max_threads (and 16), and few enough that the
+  // per-thread row counters (threads x m ints) stay small next to the matrix.
+  int threads = static_cast<int>(std::min<long long>(nnz / (1LL << 19) + 1, 16));
+  threads = std::min(threads, std::max(1, max_threads));
+  const unsigned hw = std::thread::hardware_concurrency();
+  if (hw > 0) threads = std::min(threads, static_cast<int>(hw));
+  while (threads > 1 && static_cast<long long>(threads) * m > std::max<long long>(nnz, 1) * 2) {
+    --threads;
+  }
+  threads = std::max(threads, 1);
+  // Column ranges of about equal nonzeros.
+  std::vector<int> col0(static_cast<size_t>(threads) + 1, n);
+  col0[0] = 0;
+  for (int t = 1; t < threads; ++t) {
+    const long long target = nnz * t / threads;
+    col0[t] = static_cast<int>(std::upper_bound(colptr, colptr + n + 1, target) - colptr) - 1;
+    col0[t] = std::max(col0[t], col0[t - 1]);
+  }
+  std::vector<std::vector<int>> cnt(static_cast<size_t>(threads));
+  std::atomic<int> bad{0};
+  parallel_for(threads, [&](int t) {
+    std::vector<int>& c = cnt[static_cast<size_t>(t)];
+    c.assign(static_cast<size_t>(m), 0);
+    for (int j = col0[t]; j < col0[t + 1]; ++j) {
+      for (long long p = colptr[j]; p < colptr[j + 1]; ++p) {
+        const int r = rowidx[p];
+        if (r < 0 || r >= m) {
+          bad.store(1);
+          return;
+        }
+        if (!std::isfinite(val[p])) {
+          bad.store(2);
+          return;
+        }
+        ++c[static_cast<size_t>(r)];
+      }
+    }
+  });
+  if (bad.load() != 0) {
+    if (why) *why = bad.load() == 1 ? "row index out of range" : "matrix value not finite";
+    return 1;
+  }
+  // Row starts, and each thread's first slot in every row (turning the counts into offsets).
+  kptr[0] = 0;
+  for (int i = 0; i < m; ++i) {
+    int off = kptr[i];
+    for (int t = 0; t < threads; ++t) {
+      const int c = cnt[static_cast<size_t>(t)][static_cast<size_t>(i)];
+      cnt[static_cast<size_t>(t)][static_cast<size_t>(i)] = off;
+      off += c;
+    }
+    kptr[i + 1] = off;
+  }
+  parallel_for(threads, [&](int t) {
+    std::vector<int>& next = cnt[static_cast<size_t>(t)];
+    for (int j = col0[t]; j < col0[t + 1]; ++j) {
+      for (long long p = colptr[j]; p < colptr[j + 1]; ++p) {
+        const int q = next[static_cast<size_t>(rowidx[p])]++;
+        kidx[q] = j;
+        kval[q] = val[p];
+      }
+    }
+  });
+  return 0;
+}
+
+}  // namespace sg
+
+extern "C" {
+
+/* See include/sg_pdlp.h. */
+int sg_csc_to_csr(int m, int n, const int64_t* a_colptr, const int32_t* a_rowidx,
+                  const double* a_val, int32_t* csr_ptr, int32_t* csr_idx, double* csr_val) {
+  if (m < 0 || n < 0 || a_colptr == nullptr || csr_ptr == nullptr || a_colptr[0] != 0) {
+    return SG_ERR_INVALID_ARGUMENT;
+  }
+  for (int j = 0; j < n; ++j) {
+    if (a_colptr[j + 1] < a_colptr[j]) return SG_ERR_INVALID_ARGUMENT;
+  }
+  const long long nnz = a_colptr[n];
+  if (nnz >= static_cast<long long>(INT32_MAX)) return SG_ERR_TOO_LARGE;
+  if (nnz > 0 && (a_rowidx == nullptr || a_val == nullptr || csr_idx == nullptr ||
+                  csr_val == nullptr)) {
+    return SG_ERR_INVALID_ARGUMENT;
+  }
+  const char* why = nullptr;
+  return sg::csc_to_csr(m, n, a_colptr, a_rowidx, a_val, csr_ptr, csr_idx, csr_val, 16, &why) == 0
+             ? SG_OK
+             : SG_ERR_INVALID_ARGUMENT;
+}
+
+}  // extern "C"

@@ -82,3 +82,78 @@ def _has_gpu():
         return torch.cuda.is_available()
     except Exception:
         return False
+
+
+def _csr_reference(m, n, colptr, rowidx, vals):
+    """Sequential stable counting sort (the reference's SparseMatrix::transpose,
+    src/linalg/sparse_matrix.cpp:48-78)."""
+    ptr = np.zeros(m + 1, dtype=np.int64)
+    np.add.at(ptr, rowidx.astype(np.int64) + 1, 1)
+    ptr = np.cumsum(ptr)
+    nxt = ptr[:-1].copy()
+    idx = np.zeros(len(rowidx), dtype=np.int32)
+    val = np.zeros(len(rowidx))
+    for j in range(n):
+        for p in range(colptr[j], colptr[j + 1]):
+            q = nxt[rowidx[p]]
+            nxt[rowidx[p]] += 1
+            idx[q] = j
+            val[q] = vals[p]
+    return ptr, idx, val
+
+
+def test_csc_to_csr_matches_the_sequential_transpose():
+    """The threaded CSC -> CSR (the engine's row-major copy of A) against the sequential
+    counting sort: a skewed 300 x 40000 matrix large enough for several threads (empty rows
+    and columns, one dense row), a transportation-shaped matrix, an empty matrix; errors for a
+    bad row index and a non-finite value."""
+    lib = _lib()
+    rng = np.random.default_rng(7)
+
+    def run(m, n, colptr, rowidx, vals):
+        ptr = np.zeros(m + 1, dtype=np.int32)
+        idx = np.zeros(max(len(rowidx), 1), dtype=np.int32)
+        val = np.zeros(max(len(rowidx), 1))
+        rc = lib.sg_csc_to_csr(m, n, _p(colptr, ctypes.c_int64), _p(rowidx, ctypes.c_int32),
+                               _p(vals, ctypes.c_double), _p(ptr, ctypes.c_int32),
+                               _p(idx, ctypes.c_int32), _p(val, ctypes.c_double))
+        return rc, ptr, idx[:len(rowidx)], val[:len(rowidx)]
+
+    m, n = 300, 40000
+    counts = rng.integers(0, 60, size=n)
+    counts[::7] = 0
+    cols = []
+    for j in range(n):
+        k = int(counts[j])
+        rows = rng.choice(np.arange(1, m), size=min(k, m - 1), replace=False)
+        if j % 3 == 0:
+            rows = np.union1d(rows, [0])  # row 0 dense
+        cols.append(np.sort(rows))
+    colptr = np.zeros(n + 1, dtype=np.int64)
+    colptr[1:] = np.cumsum([len(c) for c in cols])
+    rowidx = np.concatenate(cols).astype(np.int32)
+    vals = rng.standard_normal(len(rowidx))
+    rc, ptr, idx, val = run(m, n, colptr, rowidx, vals)
+    assert rc == 0
+    rptr, ridx, rval = _csr_reference(m, n, colptr, rowidx, vals)
+    assert np.array_equal(ptr, rptr) and np.array_equal(idx, ridx) and np.array_equal(val, rval)
+
+    s, d = 40, 90
+    j = np.arange(s * d)
+    colptr = (2 * np.arange(s * d + 1)).astype(np.int64)
+    rowidx = np.stack([j // d, s + j % d], axis=1).reshape(-1).astype(np.int32)
+    vals = np.ones(len(rowidx))
+    rc, ptr, idx, val = run(s + d, s * d, colptr, rowidx, vals)
+    rptr, ridx, rval = _csr_reference(s + d, s * d, colptr, rowidx, vals)
+    assert rc == 0 and np.array_equal(ptr, rptr) and np.array_equal(idx, ridx)
+
+    rc, ptr, _, _ = run(3, 2, np.zeros(3, dtype=np.int64), np.zeros(0, dtype=np.int32),
+                        np.zeros(0))
+    assert rc == 0 and np.array_equal(ptr, np.zeros(4))
+
+    colptr = np.array([0, 2, 3], dtype=np.int64)
+    rc, _, _, _ = run(2, 2, colptr, np.array([0, 5, 1], dtype=np.int32), np.ones(3))
+    assert rc == -1
+    rc, _, _, _ = run(2, 2, colptr, np.array([0, 1, 1], dtype=np.int32),
+                      np.array([1.0, np.inf, 2.0]))
+    assert rc == -1
