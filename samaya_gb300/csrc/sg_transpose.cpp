@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <new>
 #include <cmath>
 #include <thread>
 #include <vector>
@@ -23,12 +24,21 @@ namespace sg {
 
 namespace {
 
-// Runs f(t) for t in [0, threads) on threads - 1 helpers and the caller.
+// Runs f(t) for t in [0, threads) on up to threads - 1 helpers and the caller; parts whose
+// helper could not be started run on the caller. f must not throw.
 template <typename F>
 void parallel_for(int threads, const F& f) {
   std::vector<std::thread> pool;
-  pool.reserve(static_cast<size_t>(std::max(0, threads - 1)));
-  for (int t = 1; t < threads; ++t) pool.emplace_back(f, t);
+  int started = 1;
+  try {
+    pool.reserve(static_cast<size_t>(std::max(0, threads - 1)));
+    for (int t = 1; t < threads; ++t) {
+      pool.emplace_back(f, t);
+      ++started;
+    }
+  } catch (...) {
+  }
+  for (int t = started; t < threads; ++t) f(t);
   f(0);
   for (auto& th : pool) th.join();
 }
@@ -56,11 +66,12 @@ int csc_to_csr(int m, int n, const int64_t* colptr, const int32_t* rowidx, const
     col0[t] = static_cast<int>(std::upper_bound(colptr, colptr + n + 1, target) - colptr) - 1;
     col0[t] = std::max(col0[t], col0[t - 1]);
   }
-  std::vector<std::vector<int>> cnt(static_cast<size_t>(threads));
+  // Per-thread row counters, allocated here so that the workers never allocate.
+  std::vector<std::vector<int>> cnt(static_cast<size_t>(threads),
+                                    std::vector<int>(static_cast<size_t>(m), 0));
   std::atomic<int> bad{0};
   parallel_for(threads, [&](int t) {
     std::vector<int>& c = cnt[static_cast<size_t>(t)];
-    c.assign(static_cast<size_t>(m), 0);
     for (int j = col0[t]; j < col0[t + 1]; ++j) {
       for (long long p = colptr[j]; p < colptr[j + 1]; ++p) {
         const int r = rowidx[p];
@@ -123,10 +134,17 @@ int sg_csc_to_csr(int m, int n, const int64_t* a_colptr, const int32_t* a_rowidx
                   csr_val == nullptr)) {
     return SG_ERR_INVALID_ARGUMENT;
   }
-  const char* why = nullptr;
-  return sg::csc_to_csr(m, n, a_colptr, a_rowidx, a_val, csr_ptr, csr_idx, csr_val, 16, &why) == 0
-             ? SG_OK
-             : SG_ERR_INVALID_ARGUMENT;
+  try {
+    const char* why = nullptr;
+    return sg::csc_to_csr(m, n, a_colptr, a_rowidx, a_val, csr_ptr, csr_idx, csr_val, 16,
+                          &why) == 0
+               ? SG_OK
+               : SG_ERR_INVALID_ARGUMENT;
+  } catch (const std::bad_alloc&) {
+    return SG_ERR_OUT_OF_MEMORY;
+  } catch (...) {
+    return SG_ERR_INTERNAL;
+  }
 }
 
 }  // extern "C"
