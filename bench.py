@@ -528,7 +528,15 @@ def main():
                      "bytes_per_launch": steps[top]["bytes_per_launch"],
                      "ms_per_launch": steps[top]["ms_per_launch"],
                      "precision_timed": prec_key, other: steps[other],
-                     "evaluation_ms": ms_eval},
+                     "evaluation_ms": ms_eval,
+                     # One whole iteration (both fused steps): bytes over the sum of their
+                     # event-timed launches.
+                     "iteration": {
+                         "bytes": pbytes + dbytes, "ms": ms_primal + ms_dual,
+                         "achieved": (pbytes + dbytes) / ((ms_primal + ms_dual) * 1e-3) / 1e9,
+                         "frac": (pbytes + dbytes) / ((ms_primal + ms_dual) * 1e-3) / 1e9
+                         / peak}},
+        "iterations_per_s": last.iterations / t_step,
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1:
