@@ -637,7 +637,7 @@ __global__ void __launch_bounds__(kBlock) eval_cols_kernel(Ctl* ctl, OpView<T> K
 // equilibrated space (unit scales) with its own FP32 cost, bounds and right-hand side: FP32
 // products, row sums and terms (GB300's FP64 rate is a small fraction of its FP32 rate, and FP64
 // terms made these kernels arithmetic-bound), FP64 grid totals. Precision ~1e-6 relative is
-// ample for the inner tolerance; the refined point is judged by the FP64 evaluation above.
+// ample for the inner tolerance; the refined point is assessed by the FP64 evaluation above.
 
 __device__ __forceinline__ float bound_part32(float g, float lo, float up) {
   const bool hl = lo > -INFINITY;
