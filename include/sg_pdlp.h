@@ -183,6 +183,16 @@ int sg_pdlp_time_kernels(sg_pdlp* handle, int reps, double* ms_dual, double* ms_
 int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_rows,
                        int* ntiles, int* variant, int* split);
 
+/* The engine's partition of a CSR operator (row starts row_ptr, rows + 1) into tiles for a tile
+ * shape (nonzeros per tile, rows per short-row tile, warp-per-row threshold, team split; the
+ * fields sg_pdlp_tile_shape reports): nine int32 per tile in `tiles` (first row, end row, first
+ * nonzero, end nonzero, kind 0 short rows / 1 segment of a long row / 2 medium rows, warps per
+ * medium row, segment, segments of the row, long-row id), *ntiles and *nlong (split rows) set;
+ * SG_ERR_TOO_LARGE when more than max_tiles tiles (then *ntiles tells how many). No
+ * counterpart in the reference (its SpMV has no tiles); host only, no GPU needed. */
+int sg_build_tiles(int rows, const int32_t* row_ptr, int cap_nnz, int cap_rows, int warp_min,
+                   int split, int32_t* tiles, int max_tiles, int* ntiles, int* nlong);
+
 /* CSC -> CSR of an m x n matrix (the engine's row-major copy of A): row starts csr_ptr (m + 1),
  * column indices csr_idx and values csr_val (a_colptr[n] each), every row's columns in
  * increasing order, the result the reference's SparseMatrix::transpose gives

@@ -107,6 +107,8 @@ def _declare(lib):
         "sg_spmv": (I, [P, I, c_double_p, c_double_p]),
         "sg_pdlp_time_kernels": (I, [P, I, c_double_p, c_double_p, c_double_p]),
         "sg_pdlp_tile_shape": (I, [P, I] + [ctypes.POINTER(ctypes.c_int)] * 5),
+        "sg_build_tiles": (I, [I, c_int32_p, I, I, I, I, c_int32_p, I,
+                               ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
         "sg_csc_to_csr": (I, [I, I, c_int64_p, c_int32_p, c_double_p, c_int32_p, c_int32_p,
                               c_double_p]),
         "sg_scale_model": (I, [I, I, c_int64_p, c_int32_p, c_double_p, c_double_p, c_double_p,

@@ -6,6 +6,7 @@
 #include <exception>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/sg_pdlp.h"
 #include "sg_engine.cuh"
@@ -239,6 +240,43 @@ int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_ro
     return fail(SG_ERR_INVALID_ARGUMENT, "NULL output");
   }
   SG_SEAM(handle->engine->tile_shape(transpose, cap_nnz, cap_rows, ntiles, variant, split));
+}
+
+int sg_build_tiles(int rows, const int32_t* row_ptr, int cap_nnz, int cap_rows, int warp_min,
+                   int split, int32_t* tiles, int max_tiles, int* ntiles, int* nlong) {
+  if (rows < 0 || row_ptr == nullptr || ntiles == nullptr || nlong == nullptr ||
+      cap_nnz < 1 || cap_rows < 1 || warp_min < 0 || split < 0 || max_tiles < 0 ||
+      (max_tiles > 0 && tiles == nullptr)) {
+    return SG_ERR_INVALID_ARGUMENT;
+  }
+  try {
+    std::vector<int> ptr(row_ptr, row_ptr + rows + 1);
+    for (int r = 0; r < rows; ++r) {
+      if (ptr[r + 1] < ptr[r]) return SG_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<sg::Tile> out;
+    int nl = 0;
+    sg::build_tiles(ptr, cap_nnz, cap_rows, warp_min, split, &out, &nl);
+    *ntiles = static_cast<int>(out.size());
+    *nlong = nl;
+    if (static_cast<int>(out.size()) > max_tiles) return SG_ERR_TOO_LARGE;
+    for (size_t i = 0; i < out.size(); ++i) {
+      const sg::Tile& t = out[i];
+      int32_t* o = tiles + 9 * i;
+      o[0] = t.r0;
+      o[1] = t.r1;
+      o[2] = t.k0;
+      o[3] = t.k1;
+      o[4] = t.kind;
+      o[5] = t.team;
+      o[6] = t.seg;
+      o[7] = t.nseg;
+      o[8] = t.lrow;
+    }
+    return SG_OK;
+  } catch (...) {
+    return SG_ERR_INTERNAL;
+  }
 }
 
 int sg_spmv(sg_pdlp* handle, int transpose, const double* x, double* y) {
