@@ -230,17 +230,31 @@ def dual_step_bytes(lp, value_bytes, halpern=False):
     return nnz * (value_bytes + 4) + (m + 1) * 4 + n * value_bytes + vecs * m * value_bytes
 
 
+def oracle_problem(model):
+    """The LpProblem of a model built by the oracle's restatement of the reference's
+    compute_scaling + make_problem (bit-identical to the reference's): the reference arm loads no
+    library of the engine."""
+    from oracle import oracle as o
+    from samaya_gb300.model import LpProblem
+    col, row = o.compute_scaling(model.m, model.n, model.colptr, model.rowidx, model.vals)
+    colptr, rowidx, vals, cost, lower, upper = o.make_problem(model, col, row)
+    return LpProblem(m=model.m, n=model.n, colptr=colptr, rowidx=rowidx, vals=vals, cost=cost,
+                     lower=lower, upper=upper)
+
+
 def cpu_reference_run(lp, cap_s=CPU_CAP_S):
-    """The reference's CPU PDLP (oracle port of src/lp/pdlp.cpp, one core) on the LP to 1e-8
-    with a time cap: (seconds, converged, iterations, worst relative residual)."""
+    """The reference's CPU PDLP (oracle port of src/lp/pdlp.cpp, one core) on the LP to the
+    tolerance with a time cap: (seconds, converged, iterations, relative [primal, dual, gap] at
+    the end)."""
     from oracle import oracle as o
     t0 = time.perf_counter()
     r = o.pdlp_solve(*lp.arrays(), tol=TOL, max_iter=-1, time_limit=cap_s)
     dt = time.perf_counter() - t0
-    last = r.stats.get("last", (r.primal_residual, r.dual_residual, r.gap))
-    worst = max(last[0], last[1], abs(last[2])) if r.status != o.OPTIMAL else max(
-        r.primal_residual, r.dual_residual, abs(r.gap))
-    return dt, r.status == o.OPTIMAL, r.iterations, worst
+    if r.status == o.OPTIMAL:
+        last = (r.primal_residual, r.dual_residual, r.gap)
+    else:
+        last = r.stats.get("last", (r.primal_residual, r.dual_residual, r.gap))
+    return dt, r.status == o.OPTIMAL, r.iterations, [float(q) for q in last]
 
 
 def _device_clock_line(line, clk):
@@ -382,24 +396,25 @@ def run_reference(args):
                           "a time and has no adjoint: no counterpart of this workload"}))
         return 0
     model, cfg = workload(args.workload)
-    from samaya_gb300.problem import make_problem
-    lp, _ = make_problem(model)
+    lp = oracle_problem(model)
     times, info = [], None
     for i in range(args.warmup + args.steps):
-        dt, conv, iters, worst = cpu_reference_run(lp)
+        dt, conv, iters, last = cpu_reference_run(lp)
         if i >= args.warmup:
             times.append(dt)
-            info = (conv, iters, worst)
+            info = (conv, iters, last)
     value = sum(times) / len(times)
     sample = (f"reference CPU PDLP (oracle port of samaya src/lp/pdlp.cpp, bit-identical to it) "
-              f"to 1e-8 capped at {CPU_CAP_S:.0f} s per step on the same LP; converged="
-              f"{info[0]}, {info[1]} iterations, worst relative residual {info[2]:.2e}")
+              f"to {TOL:g} capped at {CPU_CAP_S:.0f} s per step on the same LP; converged="
+              f"{info[0]}, {info[1]} iterations, relative primal / dual / gap at the end "
+              f"{info[2][0]:.2e} / {info[2][1]:.2e} / {info[2][2]:.2e}")
     line = {"metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": dict(cfg, tol=TOL), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "s", "cores": 1, "kind": "port",
-                             "sample": sample, "converged": info[0]},
+                             "sample": sample, "converged": info[0], "iterations": info[1],
+                             "relative_kkt": info[2]},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -540,14 +555,15 @@ def main():
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1:
-        dt, conv, iters, worst = cpu_reference_run(lp)
+        dt, conv, iters, last_res = cpu_reference_run(lp)
         line["cpu_baseline"] = {
             "value": dt, "unit": "s", "cores": 1, "kind": "port",
-            "sample": f"reference CPU PDLP (oracle port of samaya src/lp/pdlp.cpp) to 1e-8 "
+            "sample": f"reference CPU PDLP (oracle port of samaya src/lp/pdlp.cpp) to {TOL:g} "
                       f"capped at {CPU_CAP_S:.0f} s on the same LP: converged={conv}, "
-                      f"{iters} iterations, worst relative residual {worst:.2e} (value is a "
-                      f"lower bound of its time to 1e-8 when not converged)",
-            "converged": conv}
+                      f"{iters} iterations, relative primal / dual / gap at the end "
+                      f"{last_res[0]:.2e} / {last_res[1]:.2e} / {last_res[2]:.2e} (value is a "
+                      f"lower bound of its time to the tolerance when not converged)",
+            "converged": conv, "iterations": iters, "relative_kkt": last_res}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -70,6 +70,10 @@ typedef struct sg_pdlp_opts {
   int tile_split;            /* built-in rule: medium rows (more than 128 nonzeros) longer than
                                 this many nonzeros are summed by a team of 2-8 warps; 0
                                 (default): one warp per row */
+  double artificial_restart; /* a restart is forced once the iterations since the last one
+                                reach this fraction of all iterations (0, default: 0.36, the
+                                reference's, with SG_ALGORITHM_REFERENCE; 0.1 with ENHANCED
+                                and HALPERN); values outside (0, 1) mean the default */
 } sg_pdlp_opts;
 
 /* Algorithm variants. REFERENCE follows samaya's PDLP step for step (L2 Ruiz, fixed step
@@ -167,6 +171,32 @@ int sg_pdhg_restart_to(sg_pdlp* handle, int which);
 /* PdhgDevice::download (pdhg_core.cu:382-402); any pointer may be NULL. */
 int sg_pdhg_download(sg_pdlp* handle, double* v, double* v_new, double* y, double* y_new,
                      double* v_erg, double* y_erg);
+
+/* The device setup of a solve, read back: the equilibration factors (col_scale n, row_scale
+ * m: the reference's ruiz_equilibration, src/lp/pdlp.cpp:109-187, for SG_ALGORITHM_REFERENCE),
+ * the operator-norm estimate ||[A_eq -I]|| (estimate_operator_norm, pdlp.cpp:36-103) and the
+ * step size eta = 0.99 / ||[A_eq -I]|| (pdlp.cpp:311-315). Any output may be NULL. Diagnostics
+ * for parity tests; the next solve starts afresh. */
+int sg_pdlp_equilibration(sg_pdlp* handle, double* col_scale, double* row_scale,
+                          double* operator_norm, double* step_size);
+
+/* Seam extensions with no counterpart in the reference (whose device path is FP64 PDHG with
+ * averaging only), for step-level parity of the FP32 and Halpern kernels.
+ * sg_pdhg_set_state sets the point the next single step starts from: v (n + m) and y (m) as
+ * the current iterate, the extrapolated point equal to v (a first step, v_prev = v), the anchor
+ * / restart point (v_anchor, y_anchor), averages zero. precision SG_PRECISION_FP64 keeps the
+ * FP64 set; an FP32 precision (the handle must come from sg_pdlp_create with an FP32 precision)
+ * rounds the uploaded problem values, cost, bounds and the given vectors to FP32, after which
+ * sg_pdhg_step, sg_pdhg_halpern_step, sg_pdhg_evaluate (then in the given problem's own space,
+ * unit scales), sg_pdhg_restart_to and sg_pdhg_download (widened to FP64) run the FP32
+ * kernels. Call after sg_pdhg_set_original. */
+int sg_pdhg_set_state(sg_pdlp* handle, int precision, const double* v, const double* y,
+                      const double* v_anchor, const double* y_anchor);
+/* One reflected Halpern iteration z+ = (2 T(z) - z) + (z0 - (2 T(z) - z)) / (k + 2) (T the PDHG
+ * map in primal-first order, z0 the anchor, k iterations since the anchor), with the solve's
+ * two launches; T(z) is written to the average slots (v_erg, y_erg of sg_pdhg_download). Call
+ * sg_pdhg_advance after it, as after sg_pdhg_step. */
+int sg_pdhg_halpern_step(sg_pdlp* handle, double tau, double sigma, long long k);
 
 /* Device time of the engine's hot kernels, measured with CUDA events on the engine's own stream
  * after a solve: the average milliseconds of one dual step (rows of A), one primal step
@@ -277,18 +307,22 @@ int sg_batch_unroll_adjoint(sg_batch* handle, const double* grad_v, double* grad
                             double* grad_lower, double* grad_upper);
 
 /* ---- Allocation-free SpMV. This entry point has no counterpart in the reference: it is for
- * callers that cannot call cudaMalloc (work recorded into a CUDA graph, a memory pool or budget
- * that forbids driver allocations, device memory handed out by another runtime). It computes
- * y = A x for A in CSR form (m rows, nnz nonzeros, 32-bit row starts) where every array is a
- * DEVICE pointer owned by the caller, on `stream` (a cudaStream_t; NULL for the default
- * stream), and allocates nothing: its only scratch is a file-scope device array of
- * SG_SPMV_NOALLOC_MAX_CHUNKS carry records (16 bytes each, 1 MiB) that every GPU loading the
- * library holds until the process exits. Matrices with more than
- * SG_SPMV_NOALLOC_MAX_CHUNKS * 2048 nonzeros are refused with SG_ERR_TOO_LARGE.
- * The first call on a device looks the scratch's device address up (once per device); make
- * that first call before any stream capture. All calls share the scratch, so calls that
- * overlap on the GPU (concurrent streams, or several host threads) race; serialise them.
- * Deterministic: a re-run gives the same bits. Returns SG_OK or an SG_ERR_* code. */
+ * callers that cannot call cudaMalloc (a solver running under a memory pool or budget that
+ * forbids driver allocations, or a plug-in whose device memory is handed out by another
+ * runtime). It computes y = A x for A in CSR form (m rows, 32-bit row starts d_row_ptr[m + 1],
+ * nnz = d_row_ptr[m] nonzeros) where every array is a DEVICE pointer owned by the caller, on
+ * `stream` (a cudaStream_t; NULL for the default stream), and allocates nothing: its only
+ * scratch is a file-scope device array of SG_SPMV_NOALLOC_MAX_CHUNKS carry records (16 bytes
+ * each, 1 MiB) that every GPU loading the library holds until the process exits. `nnz` sizes
+ * the launch and must equal d_row_ptr[m] (the kernels take the bounds from the device's
+ * d_row_ptr[m], so a different count still writes every row, with a launch sized for it).
+ * Matrices with more than SG_SPMV_NOALLOC_MAX_CHUNKS * 2048 nonzeros are refused with
+ * SG_ERR_TOO_LARGE. The first call on a device looks the scratch's device address up (once per
+ * device, with that device current); make that first call before any stream capture. A
+ * cudaDeviceReset makes that address stale: do not call this entry point after one. All calls
+ * share the scratch, so calls that overlap on the GPU (concurrent streams, or several host
+ * threads) race; serialise them. Deterministic: a re-run gives the same bits. Returns SG_OK or
+ * an SG_ERR_* code (message in sg_pdlp_last_error). */
 #define SG_SPMV_NOALLOC_MAX_CHUNKS 65536
 int sg_spmv_noalloc(int m, long long nnz, const int* d_row_ptr, const int* d_col_idx,
                     const double* d_val, const double* d_x, double* d_y, void* stream);

@@ -187,6 +187,30 @@ def pdhg_steps(m, n, colptr, rowidx, vals, cost, lower, upper, tau, sigma, steps
     return st
 
 
+def halpern_steps(m, n, colptr, rowidx, vals, cost, lower, upper, tau, sigma, steps, k, v, y,
+                  v0, y0):
+    """Reflected Halpern PDHG iterations on an equilibrated problem (the engine's Halpern
+    variant; no reference counterpart): returns dict(v, y, v_hat, y_hat) after ``steps``
+    iterations from z = (v, y) with anchor (v0, y0), k iterations since the anchor."""
+    out = {"v": np.ascontiguousarray(v, dtype=np.float64).copy(),
+           "y": np.ascontiguousarray(y if m else np.zeros(1), dtype=np.float64).copy(),
+           "v_hat": np.zeros(n + m), "y_hat": np.zeros(max(m, 1))}
+    anchors = [np.ascontiguousarray(a, dtype=np.float64) for a in
+               (v0, y0 if m else np.zeros(1))]
+    arrs = [np.ascontiguousarray(a, dtype=t) for a, t in (
+        (colptr, np.int64), (rowidx, np.int32), (vals, np.float64), (cost, np.float64),
+        (lower, np.float64), (upper, np.float64))]
+    lib().orc_halpern_steps(ctypes.c_int(m), ctypes.c_int(n), _p(arrs[0], I64),
+                            _p(arrs[1], I32), _p(arrs[2], D), _p(arrs[3], D), _p(arrs[4], D),
+                            _p(arrs[5], D), D(tau), D(sigma), ctypes.c_int(steps),
+                            ctypes.c_longlong(k), _p(out["v"], D), _p(out["y"], D),
+                            _p(anchors[0], D), _p(anchors[1], D), _p(out["v_hat"], D),
+                            _p(out["y_hat"], D))
+    out["y"] = out["y"][:m]
+    out["y_hat"] = out["y_hat"][:m]
+    return out
+
+
 def eval_sums(m, n, colptr, rowidx, vals, cost, lower, upper, cs, rs, v, y):
     """The seven evaluation sums (primal_sq, dual_sq, primal_obj, dual_obj, x_sq, r_sq, y_sq)."""
     out = np.zeros(7)

@@ -17,6 +17,9 @@
  *   orc_pdlp_solve        src/lp/pdlp.cpp:250-1193         (the CPU branch of solve_pdlp_once)
  *   orc_eval_sums         src/lp/pdlp.cpp:411-488          (the seven evaluation sums)
  *   orc_pdhg_steps        src/lp/pdlp.cpp:574-651          (fixed-step PDHG, for kernel parity)
+ * and one method with no reference counterpart (the engine's Halpern variant, restated from its
+ * publication; its parity is by value against the engine's kernels, not pinned to the reference):
+ *   orc_halpern_steps     reflected Halpern PDHG (Lu and Yang, cuPDLPx, 2025)
  */
 #define _POSIX_C_SOURCE 200809L
 #include <math.h>
@@ -1010,6 +1013,59 @@ void orc_pdhg_steps(int m, int n, const int64_t* colptr, const int32_t* rowidx,
   }
   free(v_bar); free(v_new); free(y_new); free(res); free(aty);
   csc_free(&A); csc_free(&At);
+}
+
+/* `steps` reflected Halpern PDHG iterations on an already equilibrated problem. No reference
+ * counterpart: the reference runs PDHG with averaging only. This is the published restarted
+ * Halpern PDHG for LP (H. Lu and J. Yang, "cuPDLPx", 2025: Halpern's iteration on the
+ * reflected PDHG map) as the engine's SG_ALGORITHM_HALPERN runs it, in plain FP64 for the
+ * step-level parity of its kernels. With T the PDHG map in primal-first order,
+ *   v^ = proj(v - tau (cost + [A -I]'y)),   y^ = y + sigma [A -I] (2 v^ - v),
+ * one iteration is z+ = R + w (z0 - R), R = 2 T(z) - z, w = 1 / (k + 2), k += 1.
+ * v (n + m), y (m): the current iterate z, updated in place; v0, y0: the anchor z0;
+ * v_hat, y_hat: T(z) of the last step. */
+void orc_halpern_steps(int m, int n, const int64_t* colptr, const int32_t* rowidx,
+                       const double* vals, const double* cost, const double* lower,
+                       const double* upper, double tau, double sigma, int steps, long long k,
+                       double* v, double* y, const double* v0, const double* y0, double* v_hat,
+                       double* y_hat) {
+  const int nt = n + m;
+  csc_t A = csc_copy(m, n, colptr, rowidx, vals);
+  double* refl = (double*)xmalloc((size_t)nt, sizeof(double));
+  double* res = (double*)xmalloc((size_t)m, sizeof(double));
+  for (int s = 0; s < steps; ++s) {
+    /* Primal half: structurals from A'y (column sums), logicals from -y. */
+    for (int j = 0; j < n; ++j) {
+      double aty = 0.0;
+      for (int64_t p = A.start[j]; p < A.start[j + 1]; ++p) aty += A.value[p] * y[A.index[p]];
+      double val = v[j] - tau * (cost[j] + aty);
+      if (lower[j] > -ORC_INF && val < lower[j]) val = lower[j];
+      if (upper[j] < ORC_INF && val > upper[j]) val = upper[j];
+      v_hat[j] = val;
+    }
+    for (int i = 0; i < m; ++i) {
+      double val = v[n + i] - tau * (cost[n + i] - y[i]);
+      if (lower[n + i] > -ORC_INF && val < lower[n + i]) val = lower[n + i];
+      if (upper[n + i] < ORC_INF && val > upper[n + i]) val = upper[n + i];
+      v_hat[n + i] = val;
+    }
+    for (int q = 0; q < nt; ++q) refl[q] = 2.0 * v_hat[q] - v[q];
+    /* Dual half at the reflected primal point. */
+    for (int i = 0; i < m; ++i) res[i] = 0.0;
+    for (int j = 0; j < n; ++j) {
+      for (int64_t p = A.start[j]; p < A.start[j + 1]; ++p) res[A.index[p]] += A.value[p] * refl[j];
+    }
+    const double w = 1.0 / (double)(k + 2);
+    for (int i = 0; i < m; ++i) {
+      y_hat[i] = y[i] + sigma * (res[i] - refl[n + i]);
+      const double ry = 2.0 * y_hat[i] - y[i];
+      y[i] = ry + w * (y0[i] - ry);
+    }
+    for (int q = 0; q < nt; ++q) v[q] = refl[q] + w * (v0[q] - refl[q]);
+    ++k;
+  }
+  free(refl); free(res);
+  csc_free(&A);
 }
 
 /* The seven evaluation sums of an iterate (scaled v: n + m, y: m) of the problem whose

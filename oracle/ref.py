@@ -14,7 +14,10 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(_HERE, "_ref", "libsamaya_ref.so")
-REFERENCE_ROOT = os.environ.get("SAMAYA_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: SAMAYA_REFERENCE_ROOT, else a sibling directory `reference` of this
+# repository's root.
+REFERENCE_ROOT = os.path.abspath(os.environ.get(
+    "SAMAYA_REFERENCE_ROOT", os.path.join(_HERE, "..", "..", "reference")))
 
 D = ctypes.c_double
 I64 = ctypes.c_int64

@@ -24,7 +24,7 @@ class Opts(ctypes.Structure):
                 ("refine_max_rounds", ctypes.c_int), ("inner_tol", ctypes.c_double),
                 ("verbose", ctypes.c_int), ("algorithm", ctypes.c_int),
                 ("autotune", ctypes.c_int),
-                ("tile_split", ctypes.c_int)]
+                ("tile_split", ctypes.c_int), ("artificial_restart", ctypes.c_double)]
 
 
 class Result(ctypes.Structure):
@@ -104,6 +104,9 @@ def _declare(lib):
         "sg_pdhg_restart_to": (I, [P, I]),
         "sg_pdhg_download": (I, [P, c_double_p, c_double_p, c_double_p, c_double_p, c_double_p,
                                  c_double_p]),
+        "sg_pdlp_equilibration": (I, [P, c_double_p, c_double_p, c_double_p, c_double_p]),
+        "sg_pdhg_set_state": (I, [P, I, c_double_p, c_double_p, c_double_p, c_double_p]),
+        "sg_pdhg_halpern_step": (I, [P, D, D, LL]),
         "sg_spmv": (I, [P, I, c_double_p, c_double_p]),
         "sg_pdlp_time_kernels": (I, [P, I, c_double_p, c_double_p, c_double_p]),
         "sg_pdlp_tile_shape": (I, [P, I] + [ctypes.POINTER(ctypes.c_int)] * 5),

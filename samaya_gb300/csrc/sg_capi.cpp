@@ -41,10 +41,19 @@ sg::Options to_options(const sg_pdlp_opts* o) {
                                                          : 0;
   opt.autotune = o->autotune != 0;
   opt.tile_split = o->tile_split > 0 ? o->tile_split : 0;
+  opt.artificial_restart =
+      o->artificial_restart > 0 && o->artificial_restart < 1 ? o->artificial_restart : 0.0;
   return opt;
 }
 
 }  // namespace
+
+namespace sg {
+
+// The thread's last-error text, for entry points outside this file.
+void set_last_error(const char* message) { g_last_error = message ? message : ""; }
+
+}  // namespace sg
 
 extern "C" {
 
@@ -223,6 +232,24 @@ int sg_pdhg_restart_to(sg_pdlp* handle, int which) {
 int sg_pdhg_download(sg_pdlp* handle, double* v, double* v_new, double* y, double* y_new,
                      double* v_erg, double* y_erg) {
   SG_SEAM(handle->engine->seam_download(v, v_new, y, y_new, v_erg, y_erg));
+}
+
+int sg_pdlp_equilibration(sg_pdlp* handle, double* col_scale, double* row_scale,
+                          double* operator_norm, double* step_size) {
+  SG_SEAM(handle->engine->equilibration(col_scale, row_scale, operator_norm, step_size));
+}
+
+int sg_pdhg_set_state(sg_pdlp* handle, int precision, const double* v, const double* y,
+                      const double* v_anchor, const double* y_anchor) {
+  if (precision != SG_PRECISION_FP64 && precision != SG_PRECISION_FP32_REFINED &&
+      precision != SG_PRECISION_FP32_THEN_FP64) {
+    return fail(SG_ERR_INVALID_ARGUMENT, "unknown precision");
+  }
+  SG_SEAM(handle->engine->seam_set_state(precision, v, y, v_anchor, y_anchor));
+}
+
+int sg_pdhg_halpern_step(sg_pdlp* handle, double tau, double sigma, long long k) {
+  SG_SEAM(handle->engine->seam_halpern_step(tau, sigma, k));
 }
 
 int sg_pdlp_time_kernels(sg_pdlp* handle, int reps, double* ms_dual, double* ms_primal,

@@ -119,10 +119,17 @@ struct Ctl {
   int halpern;    // 1: reflected Halpern PDHG (the answer and restarts use T(z), the second
                   // evaluated iterate; the Halpern iterate itself may leave the bounds)
   // Stall test of the FP32 solves: stop when the better iterate's largest relative residual has
-  // not fallen below 0.8 x its best for stall_limit evaluations (0: off).
+  // not fallen below 0.8 x its best for stall_limit evaluations (0: off), counting only
+  // evaluations below stall_floor: above it a slow stretch is the method's (FP64 would crawl
+  // there too), not FP32's precision floor.
   double stall_best;
+  double stall_floor;
   int stall_evals;
   int stall_limit;
+  // Artificial restart: a restart is forced once the iterations since the last one reach this
+  // fraction of all iterations (the reference's 0.36, pdlp.cpp:1075-1131; the engine's own
+  // algorithms default to 0.1).
+  double art_frac;
 };
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {

@@ -765,6 +765,13 @@ int Engine::setup_device(const double* rhs_orig) {
   // PDHG iterates, which the Halpern iterates are not).
   h.halpern = opt_.algorithm == 2 ? 1 : 0;
   h.no_detect = h.halpern;
+  // The reference's artificial-restart fraction for its own algorithm; the engine's algorithms
+  // restart more often (0.1): on the 1M x 2M power-law LP the primal weight otherwise sits for
+  // hundreds of thousands of iterations at a value 1000x too small (FP64 Halpern: 1e-8 in 52 s
+  // at 0.1, relative primal residual 2.5e-6 after 60 s at 0.36), and the transportation LP
+  // takes 1,984 instead of 2,112 FP64 iterations.
+  h.art_frac = opt_.artificial_restart > 0 ? opt_.artificial_restart
+                                           : (opt_.algorithm == 0 ? 0.36 : 0.1);
   SG_TRY(cudaMemcpyAsync(ctl_, &h, sizeof(Ctl), cudaMemcpyHostToDevice, s));
   SG_TRY(cudaStreamSynchronize(s));  // h lives on this stack frame
   const OpView<double> K = K_.view64();
@@ -810,6 +817,28 @@ int Engine::setup_device(const double* rhs_orig) {
     SG_TRY(cudaMemsetAsync(p, 0, static_cast<size_t>(m_) * sizeof(double), s));
   }
   SG_TRY(cudaGetLastError());
+  return kOk;
+}
+
+int Engine::equilibration(double* col_scale, double* row_scale, double* op_norm,
+                          double* step_size) {
+  std::string* err = nullptr;
+  seam_mode_ = false;
+  int rc = setup_device(nullptr);
+  if (rc != kOk) return rc;
+  SG_TRY(cudaStreamSynchronize(stream_));
+  if (col_scale && n_ > 0) {
+    SG_TRY(cudaMemcpy(col_scale, cs_, static_cast<size_t>(n_) * sizeof(double),
+                      cudaMemcpyDeviceToHost));
+  }
+  if (row_scale && m_ > 0) {
+    SG_TRY(cudaMemcpy(row_scale, rs_, static_cast<size_t>(m_) * sizeof(double),
+                      cudaMemcpyDeviceToHost));
+  }
+  Ctl h;
+  SG_TRY(cudaMemcpy(&h, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  if (op_norm) *op_norm = h.op_norm;
+  if (step_size) *step_size = h.eta;
   return kOk;
 }
 
@@ -925,6 +954,14 @@ int Engine::run_loop(double deadline_s, SolveInfo* info, cudaGraphExec_t exec, C
     SG_TRY(cudaEventSynchronize(ev_[head]));
     head = (head + 1) % 4;
     --count;
+    if (opt_.verbose >= 2) {
+      // Trace of the last evaluation the control block holds (a later in-flight copy may have
+      // overwritten the completed one: the trace is at least as recent as the chunk).
+      const Ctl& h = *ctl_host_;
+      printf("it %8lld restarts %5lld omega %.3e | cur p %.2e d %.2e g %+.2e | "
+             "avg p %.2e d %.2e g %+.2e\n", h.t, h.restarts, h.omega, h.meas[0][0],
+             h.meas[0][1], h.meas[0][2], h.meas[1][0], h.meas[1][1], h.meas[1][2]);
+    }
     // The done flag of a completed copy (later copies only ever set it too).
     if (ctl_host_->done) break;
     if (deadline_s > 0 && now_s() > deadline_s) {
@@ -1341,6 +1378,7 @@ int Engine::seam_set_original(const double* cs, const double* rs, const double* 
     SG_TRY(cudaMemcpyAsync(ctl_, &h, sizeof(Ctl), cudaMemcpyHostToDevice, s));
     SG_TRY(cudaStreamSynchronize(s));
     seam_mode_ = true;
+    seam_fp32_ = false;
     seam_steps_ = 0;
   }
   SG_TRY(cudaMemcpyAsync(cs_, cs, static_cast<size_t>(n_) * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -1354,25 +1392,143 @@ int Engine::seam_set_original(const double* cs, const double* rs, const double* 
   return kOk;
 }
 
+int Engine::seam_ctl_write(double tau, double sigma, long long t, long long k,
+                           long long max_iter) {
+  std::string* err = nullptr;
+  SG_TRY(cudaStreamSynchronize(stream_));
+  SG_TRY(cudaMemcpy(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  ctl_host_->tau = tau;
+  ctl_host_->sigma = sigma;
+  ctl_host_->t = t;
+  ctl_host_->k = k;
+  ctl_host_->done = 0;
+  ctl_host_->max_iter = max_iter;
+  SG_TRY(cudaMemcpy(ctl_, ctl_host_, sizeof(Ctl), cudaMemcpyHostToDevice));
+  return kOk;
+}
+
 int Engine::seam_step(double tau, double sigma, long long iter) {
   std::string* err = nullptr;
   if (!seam_mode_) return kErrNotReady;
   // Step sizes and counters through the control block: t = steps taken (buffer parity),
   // k = `iter` (the averaging weight 1 / (iter + 1)).
-  SG_TRY(cudaStreamSynchronize(stream_));
-  SG_TRY(cudaMemcpy(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
-  ctl_host_->tau = tau;
-  ctl_host_->sigma = sigma;
-  ctl_host_->t = seam_steps_;
-  ctl_host_->k = iter;
-  ctl_host_->done = 0;
-  ctl_host_->max_iter = std::numeric_limits<long long>::max();
-  SG_TRY(cudaMemcpy(ctl_, ctl_host_, sizeof(Ctl), cudaMemcpyHostToDevice));
-  IterView<double> it = iter_view(it64_);
-  launch_dual_step(ctl_, K_.view64(), it, 0, grid_step_k_, stream_);
-  launch_primal_step(ctl_, Kt_.view64(), it, 0, grid_step_t_, stream_);
+  int rc = seam_ctl_write(tau, sigma, seam_steps_, iter, std::numeric_limits<long long>::max());
+  if (rc != kOk) return rc;
+  if (seam_fp32_) {
+    IterView<float> it = iter_view(it32_);
+    launch_dual_step(ctl_, K_.view32(), it, 0, grid_step_k_, stream_);
+    launch_primal_step(ctl_, Kt_.view32(), it, 0, grid_step_t_, stream_);
+  } else {
+    IterView<double> it = iter_view(it64_);
+    launch_dual_step(ctl_, K_.view64(), it, 0, grid_step_k_, stream_);
+    launch_primal_step(ctl_, Kt_.view64(), it, 0, grid_step_t_, stream_);
+  }
   SG_TRY(cudaGetLastError());
   SG_TRY(cudaStreamSynchronize(stream_));
+  return kOk;
+}
+
+// One reflected Halpern iteration with the solve's kernels: the primal launch, then the dual
+// launch, Halpern weight 1 / (k + 2); the iteration limit is set to this step so that the
+// kernels also write T(z) into the average slots (as a chunk's last step does).
+int Engine::seam_halpern_step(double tau, double sigma, long long k) {
+  std::string* err = nullptr;
+  if (!seam_mode_) return kErrNotReady;
+  if (k < 0) return kErrInvalidArgument;
+  int rc = seam_ctl_write(tau, sigma, seam_steps_, k, seam_steps_ + 1);
+  if (rc != kOk) return rc;
+  if (seam_fp32_) {
+    IterView<float> it = iter_view(it32_);
+    launch_halpern_primal(ctl_, Kt_.view32(), it, 0, grid_step_t_, stream_);
+    launch_halpern_dual(ctl_, K_.view32(), it, 0, grid_step_k_, stream_);
+  } else {
+    IterView<double> it = iter_view(it64_);
+    launch_halpern_primal(ctl_, Kt_.view64(), it, 0, grid_step_t_, stream_);
+    launch_halpern_dual(ctl_, K_.view64(), it, 0, grid_step_k_, stream_);
+  }
+  SG_TRY(cudaGetLastError());
+  SG_TRY(cudaStreamSynchronize(stream_));
+  return kOk;
+}
+
+namespace {
+
+template <typename T>
+int upload_as(const double* src, T* dst, size_t count, cudaStream_t s) {
+  if (count == 0) return kOk;
+  std::vector<T> h(count);
+  for (size_t i = 0; i < count; ++i) h[i] = static_cast<T>(src[i]);
+  if (cudaMemcpyAsync(dst, h.data(), count * sizeof(T), cudaMemcpyHostToDevice, s) !=
+      cudaSuccess) {
+    return kErrCuda;
+  }
+  // The staging vector must outlive the copy.
+  return cudaStreamSynchronize(s) == cudaSuccess ? kOk : kErrCuda;
+}
+
+template <typename T>
+int download_as(const T* src, double* dst, size_t count) {
+  if (dst == nullptr || count == 0) return kOk;
+  std::vector<T> h(count);
+  if (cudaMemcpy(h.data(), src, count * sizeof(T), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    return kErrCuda;
+  }
+  for (size_t i = 0; i < count; ++i) dst[i] = static_cast<double>(h[i]);
+  return kOk;
+}
+
+template <typename T>
+int set_iterate_state(DevIter<T>& it, int p, size_t nt, size_t m, const double* v,
+                      const double* y, const double* v0, const double* y0, cudaStream_t s) {
+  int rc = kOk;
+  for (T* dst : {it.V[p], it.Vbar}) {
+    if (rc == kOk) rc = upload_as(v, dst, nt, s);
+  }
+  if (rc == kOk) rc = upload_as(v0, it.Vrst, nt, s);
+  if (rc == kOk) rc = upload_as(y, it.Y[p], m, s);
+  if (rc == kOk) rc = upload_as(y0, it.Yrst, m, s);
+  if (rc != kOk) return rc;
+  if (cudaMemsetAsync(it.Verg, 0, nt * sizeof(T), s) != cudaSuccess) return kErrCuda;
+  if (m > 0 && cudaMemsetAsync(it.Yerg, 0, m * sizeof(T), s) != cudaSuccess) return kErrCuda;
+  return kOk;
+}
+
+}  // namespace
+
+// The iterate the next single step starts from: current point v (n + m) and y (m) in the
+// buffers of the current step parity, the extrapolated point equal to v (the reference's first
+// step, v_prev = v), the anchor / restart point (v0, y0), averages zero. precision 1 uses the
+// FP32 set (needs an engine created with an FP32 precision): the uploaded values, cost and
+// bounds are rounded to FP32 here, and every later step, evaluation and download of the seam
+// runs the FP32 kernels.
+int Engine::seam_set_state(int precision, const double* v, const double* y, const double* v0,
+                           const double* y0) {
+  std::string* err = nullptr;
+  if (!seam_mode_) return kErrNotReady;
+  if (precision != 0 && !fp32_) return kErrInvalidArgument;
+  if (v == nullptr || v0 == nullptr || (m_ > 0 && (y == nullptr || y0 == nullptr))) {
+    return kErrInvalidArgument;
+  }
+  cudaStream_t s = stream_;
+  const size_t nt = static_cast<size_t>(n_) + m_;
+  const size_t m = static_cast<size_t>(m_);
+  const int p = static_cast<int>(seam_steps_ & 1);
+  SG_TRY(cudaStreamSynchronize(s));
+  seam_fp32_ = precision != 0;
+  int rc;
+  if (seam_fp32_) {
+    launch_convert(K_.val, K_.val32, nnz_, s);
+    launch_convert(Kt_.val, Kt_.val32, nnz_, s);
+    launch_convert(it64_.cost, it32_.cost, static_cast<long long>(nt), s);
+    launch_convert(it64_.lower, it32_.lower, static_cast<long long>(nt), s);
+    launch_convert(it64_.upper, it32_.upper, static_cast<long long>(nt), s);
+    SG_TRY(cudaGetLastError());
+    rc = set_iterate_state(it32_, p, nt, m, v, y, v0, y0, s);
+  } else {
+    rc = set_iterate_state(it64_, p, nt, m, v, y, v0, y0, s);
+  }
+  if (rc != kOk) return rc;
+  SG_TRY(cudaStreamSynchronize(s));
   return kOk;
 }
 
@@ -1382,31 +1538,38 @@ int Engine::seam_advance() {
   return kOk;
 }
 
-int Engine::seam_evaluate(int which, double* sums7) {
+// The evaluation kernels on the seam's iterate (v_new after step()) and average: FP64 in the
+// space before equilibration (the given scales and original data), FP32 in the given problem's
+// own space (the FP32 evaluation of the inner solves, unit scales).
+int Engine::seam_eval_launch() {
   std::string* err = nullptr;
-  if (!seam_mode_) return kErrNotReady;
-  IterView<double> it = iter_view(it64_);
-  const int parity = static_cast<int>((seam_steps_ + 1) & 1);  // v_new after step()
-  launch_eval(ctl_, K_.view64(), Kt_.view64(), it, eval_view(), red_view(), grid_k_, grid_t_,
-              parity, stream_);
+  const int parity = static_cast<int>((seam_steps_ + 1) & 1);
+  if (seam_fp32_) {
+    launch_eval(ctl_, K_.view32(), Kt_.view32(), iter_view(it32_), eval_view(), red_view(),
+                grid_k_, grid_t_, parity, stream_);
+  } else {
+    launch_eval(ctl_, K_.view64(), Kt_.view64(), iter_view(it64_), eval_view(), red_view(),
+                grid_k_, grid_t_, parity, stream_);
+  }
   SG_TRY(cudaGetLastError());
   SG_TRY(cudaStreamSynchronize(stream_));
   SG_TRY(cudaMemcpy(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  return kOk;
+}
+
+int Engine::seam_evaluate(int which, double* sums7) {
+  if (!seam_mode_) return kErrNotReady;
+  const int rc = seam_eval_launch();
+  if (rc != kOk) return rc;
   const int w = which == 0 ? 0 : 1;
   for (int q = 0; q < 7; ++q) sums7[q] = ctl_host_->eval_c[w * 7 + q] + ctl_host_->eval_r[w * 7 + q];
   return kOk;
 }
 
 int Engine::seam_restart_distance(int which, double* dv, double* dy) {
-  std::string* err = nullptr;
   if (!seam_mode_) return kErrNotReady;
-  IterView<double> it = iter_view(it64_);
-  const int parity = static_cast<int>((seam_steps_ + 1) & 1);
-  launch_eval(ctl_, K_.view64(), Kt_.view64(), it, eval_view(), red_view(), grid_k_, grid_t_,
-              parity, stream_);
-  SG_TRY(cudaGetLastError());
-  SG_TRY(cudaStreamSynchronize(stream_));
-  SG_TRY(cudaMemcpy(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  const int rc = seam_eval_launch();
+  if (rc != kOk) return rc;
   const int a = which == 0 ? 14 : 16;
   *dv = ctl_host_->eval_c[a] + ctl_host_->eval_r[a];
   *dy = ctl_host_->eval_r[a + 1];
@@ -1423,7 +1586,11 @@ int Engine::seam_restart_to(int which) {
   ctl_host_->restart_pending = 1;
   ctl_host_->restart_to_avg = which == 0 ? 0 : 1;
   SG_TRY(cudaMemcpy(ctl_, ctl_host_, sizeof(Ctl), cudaMemcpyHostToDevice));
-  launch_restart(ctl_, iter_view(it64_), stream_);
+  if (seam_fp32_) {
+    launch_restart(ctl_, iter_view(it32_), stream_);
+  } else {
+    launch_restart(ctl_, iter_view(it64_), stream_);
+  }
   SG_TRY(cudaGetLastError());
   SG_TRY(cudaStreamSynchronize(stream_));
   ctl_host_->restart_pending = 0;
@@ -1440,13 +1607,21 @@ int Engine::seam_download(double* v, double* v_new, double* y, double* y_new, do
   const size_t m = static_cast<size_t>(m_);
   const int p = static_cast<int>(seam_steps_ & 1);
   SG_TRY(cudaStreamSynchronize(stream_));
-  if (v) SG_TRY(cudaMemcpy(v, it64_.V[p], nt * sizeof(double), cudaMemcpyDeviceToHost));
-  if (v_new) SG_TRY(cudaMemcpy(v_new, it64_.V[p ^ 1], nt * sizeof(double), cudaMemcpyDeviceToHost));
-  if (y && m) SG_TRY(cudaMemcpy(y, it64_.Y[p], m * sizeof(double), cudaMemcpyDeviceToHost));
-  if (y_new && m) SG_TRY(cudaMemcpy(y_new, it64_.Y[p ^ 1], m * sizeof(double), cudaMemcpyDeviceToHost));
-  if (v_erg) SG_TRY(cudaMemcpy(v_erg, it64_.Verg, nt * sizeof(double), cudaMemcpyDeviceToHost));
-  if (y_erg && m) SG_TRY(cudaMemcpy(y_erg, it64_.Yerg, m * sizeof(double), cudaMemcpyDeviceToHost));
-  return kOk;
+  int rc = kOk;
+  auto get = [&](auto& it) {
+    if (rc == kOk) rc = download_as(it.V[p], v, nt);
+    if (rc == kOk) rc = download_as(it.V[p ^ 1], v_new, nt);
+    if (rc == kOk) rc = download_as(it.Y[p], y, m);
+    if (rc == kOk) rc = download_as(it.Y[p ^ 1], y_new, m);
+    if (rc == kOk) rc = download_as(it.Verg, v_erg, nt);
+    if (rc == kOk) rc = download_as(it.Yerg, y_erg, m);
+  };
+  if (seam_fp32_) {
+    get(it32_);
+  } else {
+    get(it64_);
+  }
+  return rc;
 }
 
 namespace {

@@ -38,6 +38,7 @@ struct Options {
                             // 2 as 1 with the reflected Halpern iteration
   bool autotune = true;     // time candidate tile shapes of large operators at create
   int tile_split = 0;       // built-in rule's team split of medium rows (0: a warp per row)
+  double artificial_restart = 0.0;  // forced-restart fraction (0: 0.36 reference, 0.1 others)
 };
 
 // Tile shape of an operator: nonzeros per tile (and per long-row segment), rows per short-row
@@ -144,6 +145,15 @@ class Engine {
   int seam_restart_to(int which);
   int seam_download(double* v, double* v_new, double* y, double* y_new, double* v_erg,
                     double* y_erg);
+  // Seam extensions with no counterpart in the reference: the storage precision and iterate
+  // state the single steps start from (current point, anchor), and one reflected Halpern
+  // iteration, so that the FP32 step kernels and the Halpern kernels are checked step by step.
+  int seam_set_state(int precision, const double* v, const double* y, const double* v0,
+                     const double* y0);
+  int seam_halpern_step(double tau, double sigma, long long k);
+  // The device setup of a solve (equilibration, operator-norm estimate, step size), read
+  // back: col_scale (n), row_scale (m), ||[A_eq -I]|| and eta. Any output may be null.
+  int equilibration(double* col_scale, double* row_scale, double* op_norm, double* step_size);
   // y = K x (rows of A) or y = K' x through the tile kernel (FP64).
   int spmv(int transpose, const double* x, double* y);
   // Average device milliseconds of the step kernels and the evaluation (CUDA events).
@@ -238,6 +248,9 @@ class Engine {
   int chunk_kernels_ = 0;
   long long seam_steps_ = 0;
   bool seam_mode_ = false;
+  bool seam_fp32_ = false;   // the seam's steps, evaluation and download use the FP32 set
+  int seam_ctl_write(double tau, double sigma, long long t, long long k, long long max_iter);
+  int seam_eval_launch();
   cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
   // Mixed-precision path: the inner solves' control block and graph, the correction problem
   // (FP64 evaluation copy), unit scales for its evaluation, and the residual vectors.

@@ -881,7 +881,7 @@ __global__ void decide_a_kernel(Ctl* c) {
     if (e < 0.8 * c->stall_best) {
       c->stall_best = e;
       c->stall_evals = 0;
-    } else if (++c->stall_evals >= c->stall_limit) {
+    } else if (e < c->stall_floor && ++c->stall_evals >= c->stall_limit) {
       set_answer(c, kIterationLimit, use_avg ? avg : cur, t_new, use_avg ? 1 : 0);
       c->t = t_new;
       return;
@@ -925,7 +925,7 @@ __global__ void decide_b_kernel(Ctl* c) {
   if (!(c->kkt_at_restart < INFINITY)) c->kkt_at_restart = cand;
   const bool restart = cand <= 0.2 * c->kkt_at_restart ||
                        (cand <= 0.8 * c->kkt_at_restart && cand > c->kkt_previous) ||
-                       static_cast<double>(k_new) >= 0.36 * static_cast<double>(iter + 1);
+                       static_cast<double>(k_new) >= c->art_frac * static_cast<double>(iter + 1);
   c->kkt_previous = cand;
   c->last_kkt = cand;
   if (restart) {

@@ -1,11 +1,11 @@
 // y = A x for a CSR matrix already in device memory, with no allocation of any kind.
 //
-// Some callers cannot call cudaMalloc: code that records work into a CUDA graph, runs under a
-// memory pool or budget that forbids driver allocations, or lives in a process whose device
-// memory is handed out by another runtime. This entry point serves them: the caller passes
-// device pointers for every input and output, and the only scratch the kernels need — one carry
-// record per chunk of nonzeros — sits in a file-scope __device__ array that every GPU loading
-// the library holds until the process exits.
+// Some callers cannot call cudaMalloc: a solver running under a memory pool or budget that
+// forbids driver allocations, or a plug-in living in a process whose device memory is handed
+// out by another runtime. This entry point serves them: the caller passes device pointers for
+// every input and output, and the only scratch the kernels need — one carry record per chunk
+// of nonzeros — sits in a file-scope __device__ array that every GPU loading the library holds
+// until the process exits.
 //
 // Work split (deterministic, no atomics): the nonzeros are cut into chunks of kChunkNnz; the CTA
 // of a chunk owns the rows that start inside it and sums each owned row up to the chunk's end;
@@ -19,6 +19,10 @@
 #include <mutex>
 
 #include "../../include/sg_pdlp.h"
+
+namespace sg {
+void set_last_error(const char* message);  // sg_capi.cpp
+}  // namespace sg
 
 namespace {
 
@@ -60,10 +64,14 @@ __global__ void __launch_bounds__(kThreads) spmv_chunk_kernel(int m, const int* 
                                                               Carry* __restrict__ carry,
                                                               int chunks) {
   const int c = blockIdx.x;
+  // The matrix's own nonzero count decides the chunk bounds: chunks past it are empty, and the
+  // last chunk runs to its end (owned rows and the carried row alike), so a grid sized from a
+  // count that differs from row_ptr[m] still writes every row once.
   const long long nnz = ptr[m];
-  const long long k0 = static_cast<long long>(c) * kChunkNnz;
-  const long long k1 = k0 + kChunkNnz < nnz ? k0 + kChunkNnz : nnz;
   const bool last_chunk = c == chunks - 1;
+  long long k0 = static_cast<long long>(c) * kChunkNnz;
+  if (k0 > nnz) k0 = nnz;
+  const long long k1 = last_chunk ? nnz : (k0 + kChunkNnz < nnz ? k0 + kChunkNnz : nnz);
   // Rows starting in [k0, k1); the last chunk takes every row starting at or after k0.
   const int r_begin = c == 0 ? 0 : lower_bound_ptr(ptr, 0, m, k0);
   const int r_end = last_chunk ? m : lower_bound_ptr(ptr, 0, m, k1);
@@ -115,7 +123,8 @@ __global__ void spmv_carry_kernel(double* __restrict__ y, const Carry* __restric
 }
 
 // The scratch's device address, looked up once per device (cudaGetSymbolAddress, with that
-// device current).
+// device current). A cudaDeviceReset of the device unloads the module and makes the address
+// stale; sg_spmv_noalloc is not meant to be called after one.
 std::mutex g_setup_mutex;
 Carry* g_carry_ptr[64] = {nullptr};
 
@@ -133,6 +142,11 @@ int scratch_for_current_device(Carry** out) {
   return SG_OK;
 }
 
+int refuse(int code, const char* message) {
+  sg::set_last_error(message);
+  return code;
+}
+
 }  // namespace
 
 extern "C" int sg_spmv_noalloc(int m, long long nnz, const int* d_row_ptr, const int* d_col_idx,
@@ -140,18 +154,39 @@ extern "C" int sg_spmv_noalloc(int m, long long nnz, const int* d_row_ptr, const
                                void* stream) {
   if (m < 0 || nnz < 0 || d_row_ptr == nullptr || d_y == nullptr ||
       (nnz > 0 && (d_col_idx == nullptr || d_val == nullptr || d_x == nullptr))) {
-    return SG_ERR_INVALID_ARGUMENT;
+    return refuse(SG_ERR_INVALID_ARGUMENT, "sg_spmv_noalloc: negative size or NULL pointer");
   }
   const long long chunks_ll = nnz == 0 ? 1 : (nnz + kChunkNnz - 1) / kChunkNnz;
-  if (chunks_ll > kMaxChunks) return SG_ERR_TOO_LARGE;
+  if (chunks_ll > kMaxChunks) {
+    return refuse(SG_ERR_TOO_LARGE,
+                  "sg_spmv_noalloc: more nonzeros than its fixed scratch covers "
+                  "(SG_SPMV_NOALLOC_MAX_CHUNKS * 2048)");
+  }
   if (m == 0) return SG_OK;
   Carry* carry = nullptr;
   const int rc = scratch_for_current_device(&carry);
-  if (rc != SG_OK) return rc;
-  const int chunks = static_cast<int>(chunks_ll);
+  if (rc != SG_OK) return refuse(rc, "sg_spmv_noalloc: no scratch address on this device");
+  int chunks = static_cast<int>(chunks_ll);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  spmv_chunk_kernel<<<chunks, kThreads, 0, s>>>(m, d_row_ptr, d_col_idx, d_val, d_x, d_y, carry,
-                                                chunks);
-  spmv_carry_kernel<<<(chunks + 255) / 256, 256, 0, s>>>(d_y, carry, chunks);
-  return cudaGetLastError() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
+  // cudaLaunchKernel reports the error of this launch only (the caller's earlier errors stay
+  // where they are).
+  const int* rp = d_row_ptr;
+  const int* ci = d_col_idx;
+  const double* va = d_val;
+  const double* xv = d_x;
+  double* yv = d_y;
+  void* chunk_args[] = {&m, &rp, &ci, &va, &xv, &yv, &carry, &chunks};
+  cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(spmv_chunk_kernel),
+                                   dim3(chunks), dim3(kThreads), chunk_args, 0, s);
+  if (e == cudaSuccess) {
+    const Carry* cc = carry;
+    void* carry_args[] = {&yv, &cc, &chunks};
+    e = cudaLaunchKernel(reinterpret_cast<const void*>(spmv_carry_kernel),
+                         dim3((chunks + 255) / 256), dim3(256), carry_args, 0, s);
+  }
+  if (e != cudaSuccess) {
+    sg::set_last_error(cudaGetErrorString(e));
+    return SG_ERR_CUDA;
+  }
+  return SG_OK;
 }

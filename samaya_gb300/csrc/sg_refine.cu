@@ -211,6 +211,7 @@ __global__ void ir_update_kernel(const Ctl* __restrict__ c32, IterView<float> it
 __global__ void ir_reset_kernel(Ctl* c, double tol, long long max_iter, int stall_limit) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   c->stall_best = INFINITY;
+  c->stall_floor = fmin(1e-4, 100.0 * tol);
   c->stall_evals = 0;
   c->stall_limit = stall_limit;
   c->t = 0;

@@ -44,6 +44,7 @@ class PdlpOptions:
     verbose: int = 0
     autotune: bool = True
     tile_split: int = 0
+    artificial_restart: float = 0.0
 
     def to_c(self) -> _native.Opts:
         o = _native.Opts()
@@ -58,6 +59,7 @@ class PdlpOptions:
         o.verbose = int(self.verbose)
         o.autotune = 1 if self.autotune else 0
         o.tile_split = int(self.tile_split)
+        o.artificial_restart = float(self.artificial_restart)
         return o
 
 
@@ -125,6 +127,19 @@ class PdlpSolver:
                                                      ctypes.byref(b), ctypes.byref(c)),
                       "sg_pdlp_time_kernels")
         return a.value, b.value, c.value
+
+    def equilibration(self):
+        """The device setup of a solve, read back: (col_scale, row_scale, operator norm of
+        [A_eq -I], step size 0.99 / norm)."""
+        lp = self.lp
+        cs = np.zeros(max(lp.n, 1))
+        rs = np.zeros(max(lp.m, 1))
+        norm, eta = ctypes.c_double(0), ctypes.c_double(0)
+        _native.check(self._lib.sg_pdlp_equilibration(self._h, _ptr(cs, ctypes.c_double),
+                                                      _ptr(rs, ctypes.c_double),
+                                                      ctypes.byref(norm), ctypes.byref(eta)),
+                      "sg_pdlp_equilibration")
+        return cs[:lp.n], rs[:lp.m], norm.value, eta.value
 
     def tile_shapes(self):
         """{"A": (nonzeros per tile, rows per short-row tile, tiles, step kernel variant,
@@ -253,6 +268,24 @@ class PdhgDevice:
 
     def advance(self):
         _native.check(self._lib.sg_pdhg_advance(self._h), "sg_pdhg_advance")
+
+    def set_state(self, v, y, v_anchor, y_anchor, precision: int = FP64):
+        """The point the next single step starts from (current v, y; extrapolated point v;
+        anchor / restart point; averages zero). An FP32 ``precision`` (the device must have
+        been created with an FP32 precision) rounds the problem and the vectors to FP32 and
+        runs the FP32 kernels from then on."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (v, y, v_anchor, y_anchor)]
+        if self.m == 0:
+            arrs[1] = arrs[3] = np.zeros(1)
+        _native.check(self._lib.sg_pdhg_set_state(self._h, int(precision),
+                                                  *[_ptr(a, ctypes.c_double) for a in arrs]),
+                      "sg_pdhg_set_state")
+
+    def halpern_step(self, tau, sigma, k):
+        """One reflected Halpern iteration (weight 1 / (k + 2) toward the anchor); T(z) lands in
+        the average slots."""
+        _native.check(self._lib.sg_pdhg_halpern_step(self._h, tau, sigma, k),
+                      "sg_pdhg_halpern_step")
 
     def evaluate(self, which) -> np.ndarray:
         out = np.zeros(7)

@@ -74,3 +74,26 @@ def load_group(name):
 
 GROUPS = ["basic", "feasible8", "vs_simplex10", "infeasible8", "loose8", "gpu_vs_cpu6",
           "repeatable30", "config0_small"]
+
+
+def highs_objective(model):
+    """(status, objective) of a Model from scipy's HiGHS (scipy.optimize.linprog), an optimum
+    independent of the reference and of the engine; status 0 is optimal."""
+    import scipy.sparse as sp
+    from scipy.optimize import linprog
+    A = sp.csc_matrix((model.vals, model.rowidx, model.colptr), shape=(model.m, model.n)).tocsr()
+    eq = model.row_lower == model.row_upper
+    ub = ~eq & np.isfinite(model.row_upper)
+    lb = ~eq & np.isfinite(model.row_lower)
+    A_ub = sp.vstack([A[ub], -A[lb]]) if (ub.any() or lb.any()) else None
+    b_ub = np.concatenate([model.row_upper[ub], -model.row_lower[lb]]) if A_ub is not None \
+        else None
+    sign = -1.0 if model.maximize else 1.0
+    r = linprog(sign * model.obj, A_ub=A_ub, b_ub=b_ub, A_eq=A[eq] if eq.any() else None,
+                b_eq=model.row_upper[eq] if eq.any() else None,
+                bounds=np.column_stack([model.col_lower, model.col_upper]), method="highs",
+                options={"primal_feasibility_tolerance": 1e-10,
+                         "dual_feasibility_tolerance": 1e-10})
+    if r.status != 0:
+        return int(r.status), None
+    return 0, sign * float(r.fun) + model.obj_offset

@@ -56,54 +56,66 @@ def test_batch_matches_reference_families(engine):
     s.close()
 
 
-def test_batch_uneven_sizes_match_single_solves(engine):
-    """Random sparse LPs of uneven sizes (m from 60 to 600): each batched answer matches the
-    single-LP engine's objective to 1e-6 relative at 1e-6, FP64 and FP32 storage."""
+def _oracle_objective(lp, tol):
+    """The reference's CPU PDLP (the oracle) on an LpProblem: (status, objective c'v)."""
+    from oracle import oracle as o
+    r = o.pdlp_solve(*lp.arrays(), tol=tol)
+    return r.status, float(np.dot(lp.cost, r.x))
+
+
+def test_batch_uneven_sizes_match_the_oracle(engine, oracle):
+    """Random sparse LPs of uneven sizes (m from 60 to 400) in one launch, FP64 at 1e-7 and
+    FP32 storage at 1e-4: every batched answer is optimal with the objective of the
+    reference's CPU PDLP (the oracle, 1e-8) within 1e-5 relative (FP64) and 1e-3 (FP32)."""
     from samaya_gb300.batch import BatchSolver
     from samaya_gb300.generators import random_sparse_lp
     from samaya_gb300.problem import make_problem
     rng = np.random.default_rng(5)
     probs = []
-    for k in range(12):
-        m = int(rng.integers(60, 600))
+    for k in range(8):
+        m = int(rng.integers(60, 400))
         n = int(np.ceil(m * rng.uniform(2, 3)))
         lp, _ = make_problem(random_sparse_lp(m, n, seed=100 + k))
         probs.append(lp)
-    opts = engine.PdlpOptions(tol=1e-6, algorithm=engine.ENHANCED)
-    res = BatchSolver.from_problems(probs, opts).solve()
-    for lp, r in zip(probs, res):
-        single = engine.solve_pdlp(lp, opts)
-        assert r.status == single.status == engine.OPTIMAL
-        a = float(np.dot(lp.cost, r.x))
-        b = float(np.dot(lp.cost, single.x))
-        assert abs(a - b) <= 1e-6 * (1 + abs(b)) * 10, (a, b)
-    res32 = BatchSolver.from_problems(probs, engine.PdlpOptions(
-        tol=1e-4, algorithm=engine.ENHANCED, precision=engine.FP32_REFINED)).solve()
-    for lp, r in zip(probs, res32):
-        single = engine.solve_pdlp(lp, engine.PdlpOptions(tol=1e-6, algorithm=engine.ENHANCED))
-        assert r.status == engine.OPTIMAL
-        a = float(np.dot(lp.cost, r.x))
-        b = float(np.dot(lp.cost, single.x))
-        assert abs(a - b) <= 1e-3 * (1 + abs(b)), (a, b)
+    refs = [_oracle_objective(lp, 1e-8) for lp in probs]
+    assert all(st == oracle.OPTIMAL for st, _ in refs)
+    for prec, tol, bar in ((engine.FP64, 1e-7, 1e-5), (engine.FP32_REFINED, 1e-4, 1e-3)):
+        res = BatchSolver.from_problems(probs, engine.PdlpOptions(
+            tol=tol, algorithm=engine.ENHANCED, precision=prec)).solve()
+        for lp, r, (_, ref) in zip(probs, res, refs):
+            assert r.status == engine.OPTIMAL
+            a = float(np.dot(lp.cost, r.x))
+            assert abs(a - ref) <= bar * (1 + abs(ref)), (prec, a, ref)
 
 
-def test_batch_shared_matrix_node_relaxations(engine):
-    """Facility location node relaxations sharing one matrix: every node's objective matches a
-    single-LP solve of that node to 1e-5 relative."""
+def test_batch_shared_matrix_node_relaxations(engine, oracle):
+    """Facility-location node relaxations sharing one matrix (20 facilities x 60 customers, 8
+    nodes with 5% of the open variables fixed) in one launch at 1e-8: every node's batched
+    answer is optimal with the node's independent optimum (scipy HiGHS) to 1e-6 relative, and,
+    mapped back to the node's model, at least 80% pass the verifier restatement (the
+    reference's acceptance bar for PDLP answers, tests/test_pdlp.cpp:497-540). (The
+    reference's CPU PDLP stops at its iteration limit on three of these nodes, so it cannot
+    serve as their optimum.)"""
+    import dataclasses
+
+    from conftest import highs_objective
     from samaya_gb300.batch import BatchSolver
     from samaya_gb300.generators import facility_location_lp, facility_node_bounds
-    from samaya_gb300.problem import make_problem
+    from samaya_gb300.problem import make_problem, model_solution
     model = facility_location_lp(20, 60, seed=3)
     lp, sc = make_problem(model)
-    bounds = _node_problems(lp, sc, model, facility_node_bounds(model, 20, 8, seed=4))
-    opts = engine.PdlpOptions(tol=1e-6, algorithm=engine.ENHANCED)
+    node_bounds = facility_node_bounds(model, 20, 8, seed=4)
+    bounds = _node_problems(lp, sc, model, node_bounds)
+    opts = engine.PdlpOptions(tol=1e-8, algorithm=engine.ENHANCED)
     res = BatchSolver.shared(lp, bounds, opts).solve()
-    for (lo, up), r in zip(bounds, res):
-        node = engine.LpProblem(m=lp.m, n=lp.n, colptr=lp.colptr, rowidx=lp.rowidx, vals=lp.vals,
-                                cost=lp.cost, lower=lo, upper=up)
-        single = engine.solve_pdlp(node, opts)
-        assert r.status == single.status
-        if r.status == engine.OPTIMAL:
-            a = float(np.dot(lp.cost, r.x))
-            b = float(np.dot(lp.cost, single.x))
-            assert abs(a - b) <= 1e-5 * (1 + abs(b)), (a, b)
+    verified, reports = 0, []
+    for (mlo, mup), r in zip(node_bounds, res):
+        node_model = dataclasses.replace(model, col_lower=mlo, col_upper=mup)
+        st, ref = highs_objective(node_model)
+        assert st == 0 and r.status == engine.OPTIMAL, (st, r.status)
+        x, _, dual, obj = model_solution(node_model, sc, r.x, r.y)
+        assert abs(obj - ref) <= 1e-6 * (1 + abs(ref)), (obj, ref)
+        ok, rep = oracle.verify_lp(node_model, x, dual)
+        verified += int(ok)
+        reports.append(rep)
+    assert verified >= 0.8 * len(res), reports

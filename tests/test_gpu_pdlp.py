@@ -293,3 +293,39 @@ def test_tile_cache_file_carries_the_tuned_shapes(tmp_path):
     assert second.returncode == 0, second.stderr
     assert second.stdout == first.stdout
     assert path.read_text().splitlines() == lines
+
+
+def test_reference_algorithm_iteration_counts_match_the_reference(engine):
+    """SG_ALGORITHM_REFERENCE in FP64 follows the reference's CPU PDLP step for step: on the
+    parity fixtures it stops with the reference's status after the reference's number of
+    iterations (every evaluation, restart and primal-weight decision the same), whenever the
+    reference itself stops before its iteration limit."""
+    counted, differ = 0, []
+    for group in ("feasible8", "vs_simplex10", "gpu_vs_cpu6", "repeatable30", "config0_small"):
+        for case in load_group(group):
+            r = solve(engine, case, algorithm=engine.REFERENCE)
+            counted += 1
+            if r.status != case.ref_status or r.iterations != case.ref_iterations:
+                differ.append((group, case.k, r.status, case.ref_status, r.iterations,
+                               case.ref_iterations))
+    assert counted > 100
+    assert not differ, differ
+
+
+def test_device_equilibration_and_step_size_match_the_oracle(engine, oracle):
+    """The device setup of the reference algorithm — 10 passes of L2 Ruiz
+    (pdlp.cpp:109-187), the power-iteration estimate of ||[A_eq -I]|| (pdlp.cpp:36-103) and
+    eta = 0.99 / ||[A_eq -I]|| (pdlp.cpp:311-315) — against the oracle's to 1e-12 relative."""
+    from samaya_gb300.generators import random_sparse_lp
+    from samaya_gb300.problem import make_problem
+    cases = [c.lp for c in load_group("feasible8")[:10] if c.lp.m > 0]
+    cases += [c.lp for c in load_group("config0_small")]
+    cases.append(make_problem(random_sparse_lp(2000, 5000, seed=0))[0])
+    for lp in cases:
+        with engine.PdlpSolver(lp, engine.PdlpOptions(algorithm=engine.REFERENCE)) as s:
+            cs, rs, norm, eta = s.equilibration()
+        o_rs, o_cs, _, _, o_norm = oracle.setup(*lp.arrays()[:5])
+        assert np.max(np.abs(cs - o_cs) / np.abs(o_cs)) <= 1e-12
+        assert np.max(np.abs(rs - o_rs) / np.abs(o_rs)) <= 1e-12
+        assert abs(norm - o_norm) <= 1e-12 * o_norm
+        assert abs(eta - 0.99 / o_norm) <= 1e-12 * eta
