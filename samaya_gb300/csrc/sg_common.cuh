@@ -119,9 +119,9 @@ struct Ctl {
   int halpern;    // 1: reflected Halpern PDHG (the answer and restarts use T(z), the second
                   // evaluated iterate; the Halpern iterate itself may leave the bounds)
   // Stall test of the FP32 solves: stop when the better iterate's largest relative residual has
-  // not fallen below 0.8 x its best for stall_limit evaluations (0: off), counting only
-  // evaluations below stall_floor: above it a slow stretch is the method's (FP64 would crawl
-  // there too), not FP32's precision floor.
+  // not fallen below 0.8 x its best for stall_limit evaluations (0: off) while below
+  // stall_floor, or for 8 x stall_limit evaluations above it (there a slow stretch is more
+  // often the method's own, which FP64 would crawl through too, than FP32's precision floor).
   double stall_best;
   double stall_floor;
   int stall_evals;

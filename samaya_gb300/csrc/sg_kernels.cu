@@ -881,7 +881,7 @@ __global__ void decide_a_kernel(Ctl* c) {
     if (e < 0.8 * c->stall_best) {
       c->stall_best = e;
       c->stall_evals = 0;
-    } else if (e < c->stall_floor && ++c->stall_evals >= c->stall_limit) {
+    } else if (++c->stall_evals >= (e < c->stall_floor ? c->stall_limit : 8 * c->stall_limit)) {
       set_answer(c, kIterationLimit, use_avg ? avg : cur, t_new, use_avg ? 1 : 0);
       c->t = t_new;
       return;

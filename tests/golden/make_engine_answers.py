@@ -1,14 +1,15 @@
 """Answers of the GB300 engine for the crossover-seeding measurement (needs a GB300).
 
 For each LP below, solves its LpProblem (compute_scaling + make_problem, the same problem
-samaya's solve_pdlp_lp builds without presolve) with the engine to 1e-8 (FP32 then FP64,
-Halpern: the bench's mode) and stores the answer in the LpProblem's space —
+samaya's solve_pdlp_lp builds without presolve) with the engine to 1e-8 — in the bench's mode
+(FP32 then FP64, Halpern), or where that stops at its iteration limit, FP64 Halpern, then FP64
+with the reference algorithm — and stores the answer in the LpProblem's space:
 tests/golden/engine_answers.npz: <name>_x (n + m), <name>_y (m), <name>_meta (status,
-iterations). tests/test_shim.py replays these answers into samaya's own Solver (crossover on) on
+iterations, mode: 0 FP32 then FP64 Halpern, 1 FP64 Halpern, 2 FP64 reference). tests/test_shim.py replays these answers into samaya's own Solver (crossover on) on
 a machine with the samaya checkout and measures the simplex work left after the crossover.
 Run from the repository root on a GPU machine:
 
-    python tests/golden/make_engine_answers.py
+    python tests/golden/make_engine_answers.py [output.npz]
 """
 from __future__ import annotations
 
@@ -33,20 +34,25 @@ def crossover_lps():
             ("random500", g.random_sparse_lp(500, 1200, seed=0))]
 
 
-def main():
+def main(out_path=OUT):
     import samaya_gb300 as sg
     from samaya_gb300.problem import make_problem
     out = {}
+    modes = [dict(precision=sg.FP32_THEN_FP64, algorithm=sg.HALPERN, inner_tol=1e-6),
+             dict(precision=sg.FP64, algorithm=sg.HALPERN),
+             dict(precision=sg.FP64, algorithm=sg.REFERENCE)]
     for name, model in crossover_lps():
         lp, _ = make_problem(model)
-        r = sg.solve_pdlp(lp, sg.PdlpOptions(tol=1e-8, precision=sg.FP32_THEN_FP64,
-                                             algorithm=sg.HALPERN, inner_tol=1e-6))
+        for mode, kw in enumerate(modes):
+            r = sg.solve_pdlp(lp, sg.PdlpOptions(tol=1e-8, **kw))
+            print(name, mode, r.status_name, r.iterations, flush=True)
+            if r.status == sg.OPTIMAL:
+                break
         out[f"{name}_x"] = r.x
         out[f"{name}_y"] = r.y
-        out[f"{name}_meta"] = np.array([r.status, r.iterations], dtype=np.int64)
-        print(name, r.status_name, r.iterations, flush=True)
-    np.savez_compressed(OUT, **out)
+        out[f"{name}_meta"] = np.array([r.status, r.iterations, mode], dtype=np.int64)
+    np.savez_compressed(out_path, **out)
 
 
 if __name__ == "__main__":
-    main()
+    main(*sys.argv[1:2])
