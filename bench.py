@@ -47,11 +47,14 @@ PRECISION_NAMES = {
 }
 
 
-def solver_options(args, precision):
-    """PdlpOptions of a precision mode with the chosen algorithm."""
+def solver_options(args, precision, time_limit=None):
+    """PdlpOptions of a precision mode with the chosen algorithm (time_limit: seconds, None for
+    none)."""
     import samaya_gb300 as sg
     prec = {"mixed": sg.FP32_THEN_FP64, "refined": sg.FP32_REFINED, "fp64": sg.FP64}[precision]
     kw = {"inner_tol": args.switch_tol} if precision == "mixed" else {}
+    if time_limit is not None:
+        kw["time_limit"] = time_limit
     alg = ALGORITHM_IDS[getattr(args, "algorithm", "enhanced")]
     return sg.PdlpOptions(tol=TOL, algorithm=alg, precision=prec,
                           max_iterations=getattr(args, "max_iterations", -1) if args.profile
@@ -69,9 +72,19 @@ def parse():
                     help="transport (the headline), powerlaw, random (2000 x 5000): one LP to "
                          "1e-8; batchA / batchB: LPs/s of the batched engine against sequential "
                          "solves; diff: the differentiable layer's forward and backward")
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "refined", "fp64"],
+    ap.add_argument("--precision", default="auto",
+                    choices=["auto", "mixed", "refined", "fp64"],
                     help="mixed: FP32 PDLP then FP64 PDLP from its answer; refined: FP32 "
-                         "iterations with FP64 iterative refinement; fp64: FP64 throughout")
+                         "iterations with FP64 iterative refinement; fp64: FP64 throughout; "
+                         "auto: fp64 on the power-law LP (FP32 storage of its iterate leaves a "
+                         "1e-5 relative residual floor there), mixed otherwise")
+    ap.add_argument("--other-time-limit", type=float, default=150.0,
+                    help="seconds each comparison solve (the other precisions, the largest "
+                         "configuration's modes) may take before it stops with status "
+                         "time_limit")
+    ap.add_argument("--no-largest", action="store_true",
+                    help="skip the power-law LP (the largest configuration) measurement that "
+                         "the transportation line carries")
     ap.add_argument("--switch-tol", type=float, default=SWITCH_TOL,
                     help="relative KKT at which the mixed path leaves FP32")
     ap.add_argument("--profile", action="store_true",
@@ -89,8 +102,10 @@ def parse():
                          "random sparse LPs, enhanced otherwise)")
     args = ap.parse_args()
     if args.algorithm == "auto":
-        args.algorithm = {"transport": "halpern", "random": "reference",
+        args.algorithm = {"transport": "halpern", "random": "reference", "powerlaw": "halpern",
                           "batchA": "reference"}.get(args.workload, "enhanced")
+    if args.precision == "auto":
+        args.precision = "fp64" if args.workload == "powerlaw" else "mixed"
     global TOL
     TOL = args.tol
     return args
@@ -204,13 +219,14 @@ def traffic_summary():
 
 def primal_step_bytes(lp, value_bytes, halpern=False):
     """Compulsory bytes of one primal-step launch (rows of A' = the n columns): the nonzeros
-    (value + int32 index), the n + 1 row starts, the m duals gathered once, and the column
-    epilogue: classic, 8 n-vectors (c, l, u, x, x_avg read; x_new, x_bar, x_avg written);
-    Halpern, 7 (c, l, u, x, x0 read; x_new, x_bar written; x^ is written only by a chunk's last
-    step, before an evaluation). When every column has the same bounds, each 0 or infinite
-    (the transportation LP: x >= 0), the engine reads no bound vectors: 2 fewer."""
+    (value + int32 index), the n + 1 row starts, the duals of the rows with nonzeros gathered
+    once, and the column epilogue: classic, 8 n-vectors (c, l, u, x, x_avg read; x_new, x_bar,
+    x_avg written); Halpern, 7 (c, l, u, x, x0 read; x_new, x_bar written; x^ is written only by
+    a chunk's last step, before an evaluation). When every column has the same bounds, each 0
+    or infinite (the transportation LP: x >= 0), the engine reads no bound vectors: 2 fewer."""
     import numpy as np
-    n, m, nnz = lp.n, lp.m, lp.nnz
+    n, nnz = lp.n, lp.nnz
+    m = int(np.count_nonzero(np.bincount(lp.rowidx[:nnz], minlength=lp.m)))
     vecs = 7 if halpern else 8
     lo, up = lp.lower[:n], lp.upper[:n]
     if n > 0 and lo[0] in (0.0, -np.inf) and up[0] in (0.0, np.inf) and np.all(lo == lo[0]) \
@@ -219,14 +235,19 @@ def primal_step_bytes(lp, value_bytes, halpern=False):
     return nnz * (value_bytes + 4) + (n + 1) * 4 + m * value_bytes + vecs * n * value_bytes
 
 
-def dual_step_bytes(lp, value_bytes, halpern=False):
+def dual_step_bytes(lp, value_bytes, halpern=False, step_rows=None):
     """Rows of A: nonzeros, m + 1 starts, x_bar gathered once (n), and the row epilogue:
     classic, 13 m-vectors (y, r, r_bar, c_r, l_r, u_r, y_avg, r_avg read; y_new, r_new, r_bar,
     y_avg, r_avg written); Halpern, 9 (y, r, c_r, l_r, u_r, y0, r0 read; y_new, r_new written;
     y^, r^ only by a chunk's last step). (The solves here have no right-hand side vector, which
-    adds one.)"""
+    adds one.) With step_rows < m (inert rows left out: no nonzeros, a logical that stays 0),
+    the epilogue covers the stepped rows only, which the launch reads from a row list (4 bytes
+    each) beside their starts."""
     n, m, nnz = lp.n, lp.m, lp.nnz
     vecs = 9 if halpern else 13
+    if step_rows is not None and step_rows < m:
+        return (nnz * (value_bytes + 4) + step_rows * 8 + n * value_bytes
+                + vecs * step_rows * value_bytes)
     return nnz * (value_bytes + 4) + (m + 1) * 4 + n * value_bytes + vecs * m * value_bytes
 
 
@@ -480,18 +501,22 @@ def main():
     for name in PRECISION_NAMES:
         if name == args.precision:
             continue
-        with sg.PdlpSolver(lp, solver_options(args, name)) as so:
-            so.solve(download=False)
-            ro = [so.solve(download=False) for _ in range(max(1, min(args.steps, 3)))]
+        with sg.PdlpSolver(lp, solver_options(args, name, args.other_time_limit)) as so:
+            first = so.solve(download=False)
+            reps = max(1, min(args.steps, 3)) if first.device_ms < 10e3 else 1
+            ro = [first] if reps == 1 and first.device_ms >= 10e3 else [
+                so.solve(download=False) for _ in range(reps)]
         others[name] = {"seconds": sum(r.device_ms for r in ro) / len(ro) / 1e3,
-                        "iterations": ro[-1].iterations, "status": ro[-1].status_name}
+                        "iterations": ro[-1].iterations, "status": ro[-1].status_name,
+                        "relative_kkt": [ro[-1].primal_residual, ro[-1].dual_residual,
+                                         ro[-1].gap]}
     # End to end through the C ABI from pinned host buffers.
     e2e_times = []
     h2d = (lp.colptr.nbytes + lp.rowidx.nbytes + lp.vals.nbytes + lp.cost.nbytes +
            lp.lower.nbytes + lp.upper.nbytes)
     d2h = 8 * (lp.n + lp.m) + 8 * lp.m
     pinned = _pinned_problem(lp)
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(max(1, min(args.steps, 3)) if t_step < 10.0 else 1):
         t0 = time.perf_counter()
         r = sg.solve_pdlp(pinned, opts)
         e2e_times.append(time.perf_counter() - t0)
@@ -501,7 +526,7 @@ def main():
     vb = 4 if mixed else 8
     halpern = args.algorithm == "halpern"
     pbytes = primal_step_bytes(lp, vb, halpern)
-    dbytes = dual_step_bytes(lp, vb, halpern)
+    dbytes = dual_step_bytes(lp, vb, halpern, solver.step_rows()[0])
     peak, peak_kind = peak_hbm()
     # Both step kernels launch once per iteration: the dominant one is the slower.
     prec_key = "fp32" if mixed else "fp64"
@@ -555,6 +580,14 @@ def main():
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1:
+        line["e2e"]["from_model"] = setup_paths(model, opts)
+        line["e2e"]["cold_process_s"] = cold_e2e(lp, args, args.precision)
+        line["e2e"]["cold_process"] = (
+            "the same call in a fresh process: library load, CUDA context, checks, transpose, "
+            "upload, the tile tuner's first timing of both operators (cached afterwards), "
+            "solve, download")
+        if args.workload == "transport" and not args.no_largest:
+            line["largest_config"] = largest_config(args)
         dt, conv, iters, last_res = cpu_reference_run(lp)
         line["cpu_baseline"] = {
             "value": dt, "unit": "s", "cores": 1, "kind": "port",
@@ -569,6 +602,129 @@ def main():
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+_COLD_SCRIPT = """
+import json, sys, time
+sys.path.insert(0, {root!r})
+import numpy as np
+import samaya_gb300 as sg
+from samaya_gb300.model import LpProblem
+import torch
+z = np.load({path!r})
+def pin(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+lp = LpProblem(m=int(z["m"]), n=int(z["n"]), **{{k: pin(z[k]) for k in
+               ("colptr", "rowidx", "vals", "cost", "lower", "upper")}})
+opts = sg.PdlpOptions(**json.loads({opts!r}))
+t0 = time.perf_counter()
+r = sg.solve_pdlp(lp, opts)
+dt = time.perf_counter() - t0
+print(json.dumps({{"seconds": dt, "status": r.status_name}}))
+"""
+
+
+def setup_paths(model, opts, reps=2):
+    """The model's setup to a solved answer in the model's space, two ways (best of reps):
+    host scaling + computational form (sg_scale_model) + sg_pdlp_create (host transpose,
+    upload), against sg_pdlp_create_model (one upload, the same steps on the device); each then
+    solves, downloads and maps the answer back. Seconds of each and of its setup part."""
+    import samaya_gb300 as sg
+    from samaya_gb300.problem import make_problem, model_solution
+    out = {}
+    for name in ("host_setup", "device_setup"):
+        best = None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            if name == "host_setup":
+                lp, sc = make_problem(model)
+                s = sg.PdlpSolver(lp, opts)
+            else:
+                s = sg.PdlpSolver.from_model(model, opts)
+                sc = s.scaling
+            t1 = time.perf_counter()
+            r = s.solve()
+            model_solution(model, sc, r.x, r.y)
+            t2 = time.perf_counter()
+            s.close()
+            if best is None or t2 - t0 < best[0]:
+                best = (t2 - t0, t1 - t0, r.status_name)
+        out[name] = {"seconds": best[0], "setup_seconds": best[1], "status": best[2]}
+    return out
+
+
+def cold_e2e(lp, args, precision):
+    """Seconds of one solve_pdlp through the C ABI from pinned host buffers in a fresh process
+    (None if it fails): what a caller pays the first time, the tile tuner included."""
+    import tempfile
+    o = solver_options(args, precision)
+    kw = {k: getattr(o, k) for k in ("tol", "precision", "algorithm", "inner_tol")}
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "lp.npz")
+        import numpy as np
+        np.savez(path, m=lp.m, n=lp.n, colptr=lp.colptr, rowidx=lp.rowidx, vals=lp.vals,
+                 cost=lp.cost, lower=lp.lower, upper=lp.upper)
+        script = _COLD_SCRIPT.format(root=ROOT, path=path, opts=json.dumps(kw))
+        env = dict(os.environ)
+        env.pop("SG_TILE_CACHE", None)
+        p = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True,
+                           env=env, timeout=1200)
+    try:
+        out = json.loads(p.stdout.strip().splitlines()[-1])
+        return out["seconds"] if out["status"] == "optimal" else None
+    except Exception:
+        return None
+
+
+def largest_config(args):
+    """The power-law LP (the largest configuration: 1e6 x 2e6, 12M nonzeros, Zipf(1.5) rows)
+    to the tolerance in each precision mode with the Halpern iteration: one timed solve each
+    (device time; a solve takes tens of seconds, so it is not repeated; each stops at
+    --other-time-limit), the step kernels' roofline in FP64 and FP32 storage, and the
+    reference's CPU PDLP (the oracle port, one core) on a capped run of the same LP."""
+    import samaya_gb300 as sg
+    from samaya_gb300.problem import make_problem
+    model, cfg = workload("powerlaw")
+    lp, _ = make_problem(model)
+    a2 = argparse.Namespace(**vars(args))
+    a2.algorithm = "halpern"
+    peak, peak_kind = peak_hbm()
+    traffic = traffic_summary()
+    modes = {}
+    for name in ("fp64", "refined", "mixed"):
+        with sg.PdlpSolver(lp, solver_options(a2, name, args.other_time_limit)) as s:
+            r = s.solve(download=False)
+            entry = {"seconds": r.device_ms / 1e3, "iterations": r.iterations,
+                     "status": r.status_name,
+                     "relative_kkt": [r.primal_residual, r.dual_residual, r.gap],
+                     "refinement_rounds": r.refinement_rounds}
+            if name in ("fp64", "refined"):
+                md, mp, _ = s.time_kernels(20)
+                vb = 8 if name == "fp64" else 4
+                db = dual_step_bytes(lp, vb, True, s.step_rows()[0])
+                pb = primal_step_bytes(lp, vb, True)
+                key = "powerlaw_fp64_halpern" if vb == 8 else "powerlaw_fp32_halpern"
+                entry["step_kernels"] = {
+                    "storage": "fp64" if vb == 8 else "fp32",
+                    "dual_step": {"ms": md, "bytes": db, "achieved_gbs": db / (md * 1e-3) / 1e9,
+                                  "frac": db / (md * 1e-3) / 1e9 / peak,
+                                  "traffic": traffic.get(f"{key}_dual_step")},
+                    "primal_step": {"ms": mp, "bytes": pb,
+                                    "achieved_gbs": pb / (mp * 1e-3) / 1e9,
+                                    "frac": pb / (mp * 1e-3) / 1e9 / peak,
+                                    "traffic": traffic.get(f"{key}_primal_step")},
+                    "peak_gbs": peak, "peak_kind": peak_kind}
+        modes[name] = entry
+    optimal = {k: v for k, v in modes.items() if v["status"] == "optimal"}
+    dt, conv, iters, last_res = cpu_reference_run(oracle_problem(model))
+    return {"config": dict(cfg, tol=TOL, algorithm=ALGORITHM_NAMES["halpern"]),
+            "modes": modes,
+            "fastest_optimal": min(optimal, key=lambda k: optimal[k]["seconds"]) if optimal
+            else None,
+            "cpu_baseline": {"value": dt, "unit": "s", "cores": 1, "kind": "port",
+                             "converged": conv, "iterations": iters, "relative_kkt": last_res,
+                             "sample": f"reference CPU PDLP (oracle port) capped at "
+                                       f"{CPU_CAP_S:.0f} s on the same LP"}}
 
 
 def _pinned_problem(lp):

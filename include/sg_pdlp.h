@@ -74,6 +74,10 @@ typedef struct sg_pdlp_opts {
                                 reach this fraction of all iterations (0, default: 0.36, the
                                 reference's, with SG_ALGORITHM_REFERENCE; 0.1 with ENHANCED
                                 and HALPERN); values outside (0, 1) mean the default */
+  int keep_inert_rows;       /* 0 (default): rows with no nonzeros whose logical has no cost
+                                and 0 within its bounds are left out of the solves' step
+                                launches (their dual and logical stay 0 in every iterate, so
+                                the answer is the same bits); 1: every row is stepped */
 } sg_pdlp_opts;
 
 /* Algorithm variants. REFERENCE follows samaya's PDLP step for step (L2 Ruiz, fixed step
@@ -213,6 +217,10 @@ int sg_pdlp_time_kernels(sg_pdlp* handle, int reps, double* ms_dual, double* ms_
 int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_rows,
                        int* ntiles, int* variant, int* split);
 
+/* The rows of A the solves' dual steps run over (m, unless inert rows are left out: see
+ * sg_pdlp_opts.keep_inert_rows) and the tiles over them. Diagnostics. */
+int sg_pdlp_step_rows(sg_pdlp* handle, int* rows, int* tiles);
+
 /* The engine's partition of a CSR operator (row starts row_ptr, rows + 1) into tiles for a tile
  * shape (nonzeros per tile, rows per short-row tile, warp-per-row threshold, team split; the
  * fields sg_pdlp_tile_shape reports): nine int32 per tile in `tiles` (first row, end row, first
@@ -244,6 +252,33 @@ int sg_scale_model(int m, int n, const int64_t* a_colptr, const int32_t* a_rowid
                    int maximize, int64_t* lp_colptr, int32_t* lp_rowidx, double* lp_val,
                    double* cost, double* lower, double* upper, double* col_scale,
                    double* row_scale, int64_t* lp_nnz);
+
+/* sg_scale_model computed on the GPU (the reference's compute_scaling + make_problem, src/
+ * linalg/scaling.cpp:79-149, src/lp/lp_solver.cpp:28-51, restated as device kernels): the same
+ * arguments and the same bits as sg_scale_model (the extremes are min / max, the factors the
+ * same IEEE products, square roots and quotients; a factor whose nearest power of two turns on
+ * the last bit of its logarithm is finished on the host by sg_scale_model's own rule). Needs a
+ * GB300 (SG_ERR_NO_DEVICE otherwise); SG_ERR_INVALID_ARGUMENT for a row index out of range or
+ * a value that is not finite. */
+int sg_scale_model_device(int m, int n, const int64_t* a_colptr, const int32_t* a_rowidx,
+                          const double* a_val, const double* obj, const double* col_lower,
+                          const double* col_upper, const double* row_lower,
+                          const double* row_upper, int maximize, int64_t* lp_colptr,
+                          int32_t* lp_rowidx, double* lp_val, double* cost, double* lower,
+                          double* upper, double* col_scale, double* row_scale, int64_t* lp_nnz);
+
+/* An engine handle straight from a model: compute_scaling + make_problem and the CSC -> CSR
+ * transpose of the engine's row-major copy (src/linalg/sparse_matrix.cpp:48-78) run on the GPU
+ * on a single upload of the model, instead of on the host before sg_pdlp_create (samaya's
+ * solve_pdlp_lp setup, src/core/solver.cpp:395-405, without its presolve). The handle's
+ * problem is the model's LpProblem (the one sg_scale_model gives), so sg_pdlp_solve answers in
+ * its space; col_scale (n) and row_scale (m), when not NULL, receive the factors that
+ * sg_unscale_solution takes to map the answer back. */
+int sg_pdlp_create_model(sg_pdlp** handle, int m, int n, const int64_t* a_colptr,
+                         const int32_t* a_rowidx, const double* a_val, const double* obj,
+                         const double* col_lower, const double* col_upper,
+                         const double* row_lower, const double* row_upper, int maximize,
+                         const sg_pdlp_opts* opts, double* col_scale, double* row_scale);
 
 /* A PDLP answer (LpProblem space, x_lp n + m, y_lp m) back to the model, as samaya's
  * solve_pdlp_lp maps it (reference src/core/solver.cpp:415-432): column values x (n), row

@@ -24,7 +24,8 @@ class Opts(ctypes.Structure):
                 ("refine_max_rounds", ctypes.c_int), ("inner_tol", ctypes.c_double),
                 ("verbose", ctypes.c_int), ("algorithm", ctypes.c_int),
                 ("autotune", ctypes.c_int),
-                ("tile_split", ctypes.c_int), ("artificial_restart", ctypes.c_double)]
+                ("tile_split", ctypes.c_int), ("artificial_restart", ctypes.c_double),
+                ("keep_inert_rows", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -110,6 +111,7 @@ def _declare(lib):
         "sg_spmv": (I, [P, I, c_double_p, c_double_p]),
         "sg_pdlp_time_kernels": (I, [P, I, c_double_p, c_double_p, c_double_p]),
         "sg_pdlp_tile_shape": (I, [P, I] + [ctypes.POINTER(ctypes.c_int)] * 5),
+        "sg_pdlp_step_rows": (I, [P] + [ctypes.POINTER(ctypes.c_int)] * 2),
         "sg_build_tiles": (I, [I, c_int32_p, I, I, I, I, c_int32_p, I,
                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
         "sg_csc_to_csr": (I, [I, I, c_int64_p, c_int32_p, c_double_p, c_int32_p, c_int32_p,
@@ -120,6 +122,13 @@ def _declare(lib):
                                c_double_p, c_int64_p]),
         "sg_unscale_solution": (I, [I, I, c_double_p, c_double_p, I, c_double_p, c_double_p,
                                     c_double_p, c_double_p, c_double_p]),
+        "sg_scale_model_device": (I, [I, I, c_int64_p, c_int32_p, c_double_p, c_double_p,
+                                      c_double_p, c_double_p, c_double_p, c_double_p, I,
+                                      c_int64_p, c_int32_p, c_double_p, c_double_p, c_double_p,
+                                      c_double_p, c_double_p, c_double_p, c_int64_p]),
+        "sg_pdlp_create_model": (I, [h, I, I, c_int64_p, c_int32_p, c_double_p, c_double_p,
+                                     c_double_p, c_double_p, c_double_p, c_double_p, I,
+                                     ctypes.POINTER(Opts), c_double_p, c_double_p]),
     }
     for name, (res, args) in sig.items():
         if hasattr(lib, name):

@@ -10,6 +10,7 @@
 
 #include "../../include/sg_pdlp.h"
 #include "sg_engine.cuh"
+#include "sg_setup_device.cuh"
 
 struct sg_pdlp {
   sg::Engine* engine = nullptr;
@@ -43,6 +44,7 @@ sg::Options to_options(const sg_pdlp_opts* o) {
   opt.tile_split = o->tile_split > 0 ? o->tile_split : 0;
   opt.artificial_restart =
       o->artificial_restart > 0 && o->artificial_restart < 1 ? o->artificial_restart : 0.0;
+  opt.skip_inert_rows = o->keep_inert_rows == 0;
   return opt;
 }
 
@@ -98,6 +100,73 @@ int sg_pdlp_create(sg_pdlp** handle, int m, int n, const int64_t* a_colptr,
     return fail(SG_ERR_OUT_OF_MEMORY, "host allocation failed");
   } catch (const std::exception& ex) {
     return fail(SG_ERR_INTERNAL, ex.what());
+  } catch (...) {
+    return fail(SG_ERR_INTERNAL, "unexpected exception");
+  }
+}
+
+int sg_pdlp_create_model(sg_pdlp** handle, int m, int n, const int64_t* a_colptr,
+                         const int32_t* a_rowidx, const double* a_val, const double* obj,
+                         const double* col_lower, const double* col_upper,
+                         const double* row_lower, const double* row_upper, int maximize,
+                         const sg_pdlp_opts* opts, double* col_scale, double* row_scale) {
+  if (handle == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "handle is NULL");
+  *handle = nullptr;
+  try {
+    sg::ModelView mv;
+    mv.m = m;
+    mv.n = n;
+    mv.colptr = a_colptr;
+    mv.rowidx = a_rowidx;
+    mv.val = a_val;
+    mv.obj = obj;
+    mv.col_lower = col_lower;
+    mv.col_upper = col_upper;
+    mv.row_lower = row_lower;
+    mv.row_upper = row_upper;
+    mv.maximize = maximize;
+    std::string why;
+    sg::Engine* e = nullptr;
+    const int rc = sg::create_engine_from_model(&e, mv, to_options(opts), col_scale, row_scale,
+                                                &why);
+    if (rc != sg::kOk) return fail(rc, why);
+    *handle = new sg_pdlp{e};
+    return SG_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(SG_ERR_OUT_OF_MEMORY, "host allocation failed");
+  } catch (const std::exception& ex) {
+    return fail(SG_ERR_INTERNAL, ex.what());
+  } catch (...) {
+    return fail(SG_ERR_INTERNAL, "unexpected exception");
+  }
+}
+
+int sg_scale_model_device(int m, int n, const int64_t* a_colptr, const int32_t* a_rowidx,
+                          const double* a_val, const double* obj, const double* col_lower,
+                          const double* col_upper, const double* row_lower,
+                          const double* row_upper, int maximize, int64_t* lp_colptr,
+                          int32_t* lp_rowidx, double* lp_val, double* cost, double* lower,
+                          double* upper, double* col_scale, double* row_scale, int64_t* lp_nnz) {
+  try {
+    sg::ModelView mv;
+    mv.m = m;
+    mv.n = n;
+    mv.colptr = a_colptr;
+    mv.rowidx = a_rowidx;
+    mv.val = a_val;
+    mv.obj = obj;
+    mv.col_lower = col_lower;
+    mv.col_upper = col_upper;
+    mv.row_lower = row_lower;
+    mv.row_upper = row_upper;
+    mv.maximize = maximize;
+    std::string why;
+    const int rc = sg::scale_model_device(mv, lp_colptr, lp_rowidx, lp_val, cost, lower, upper,
+                                          col_scale, row_scale, lp_nnz, &why);
+    if (rc != sg::kOk) return fail(rc, why);
+    return SG_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(SG_ERR_OUT_OF_MEMORY, "host allocation failed");
   } catch (...) {
     return fail(SG_ERR_INTERNAL, "unexpected exception");
   }
@@ -267,6 +336,11 @@ int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_ro
     return fail(SG_ERR_INVALID_ARGUMENT, "NULL output");
   }
   SG_SEAM(handle->engine->tile_shape(transpose, cap_nnz, cap_rows, ntiles, variant, split));
+}
+
+int sg_pdlp_step_rows(sg_pdlp* handle, int* rows, int* tiles) {
+  if (rows == nullptr || tiles == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "NULL output");
+  SG_SEAM(handle->engine->step_rows(rows, tiles));
 }
 
 int sg_build_tiles(int rows, const int32_t* row_ptr, int cap_nnz, int cap_rows, int warp_min,

@@ -47,7 +47,15 @@ struct TileSet {
   int cap_nnz;      // nonzeros per tile at most (shared-memory staging capacity)
   int cap_rows;     // rows per tile at most
   int variant;      // step kernels: 0 high occupancy, 1 deep unroll of medium and long rows
+  // Null: the tiles' rows are the operator's rows. Otherwise the tiles cover a subsequence of
+  // the rows (rows that are left out are empty, so every nonzero position is unchanged), and
+  // a tile's row index v stands for rows[v].
+  const int* rows;
 };
+
+__device__ __forceinline__ int tile_row(const TileSet& ts, int v) {
+  return ts.rows != nullptr ? __ldg(ts.rows + v) : v;
+}
 
 constexpr int kMaxVec = 2;
 constexpr int kWarpRowMin = 128;             // rows longer than this get a warp (tile kind 2)

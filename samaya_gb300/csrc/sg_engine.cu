@@ -169,6 +169,10 @@ Engine::~Engine() {
     dfree(op->tiles);
     dfree(op->seg_part);
     dfree(op->lcount);
+    dfree(op->act_rows);
+    dfree(op->act_tiles);
+    dfree(op->act_seg_part);
+    dfree(op->act_lcount);
   }
   for (double** p : {&it64_.V[0], &it64_.V[1], &it64_.Vbar, &it64_.Y[0], &it64_.Y[1],
                      &it64_.Verg, &it64_.Yerg, &it64_.Vrst, &it64_.Yrst, &it64_.cost,
@@ -335,8 +339,102 @@ int Engine::create(Engine** out, int m, int n, const int64_t* colptr, const int3
     delete e;
     return code;
   }
+  {
+    std::vector<char> inert(static_cast<size_t>(m));
+    for (int i = 0; i < m; ++i) {
+      inert[i] = kptr[i + 1] == kptr[i] && cost[n + i] == 0.0 && lower[n + i] <= 0.0 &&
+                 upper[n + i] >= 0.0;
+    }
+    rc = e->set_active_rows(inert, &why);
+  }
   // Tiles of both operators (tuned or by the built-in rule), then the grids.
-  rc = e->tune_tiles(&why);
+  if (rc == kOk) rc = e->tune_tiles(&why);
+  if (rc != kOk) {
+    if (err) *err = why;
+    delete e;
+    return rc;
+  }
+  *out = e;
+  return kOk;
+}
+
+int Engine::create_from_device(Engine** out, const DeviceLp& d, const Options& opt,
+                               std::string* err) {
+  *out = nullptr;
+  if (d.m < 0 || d.n < 0 || d.kptr_host.size() != static_cast<size_t>(d.m) + 1 ||
+      d.tptr_host.size() != static_cast<size_t>(d.n) + 1) {
+    if (err) *err = "invalid argument";
+    return kErrInvalidArgument;
+  }
+  if (d.nnz >= static_cast<long long>(std::numeric_limits<int>::max()) ||
+      static_cast<long long>(d.n) + d.m >= std::numeric_limits<int>::max()) {
+    if (err) *err = "matrix too large for 32-bit offsets";
+    return kErrTooLarge;
+  }
+  if (device_info(nullptr, nullptr, nullptr, 0) != kOk) {
+    if (err) *err = "no sm_103 GPU";
+    return kErrNoDevice;
+  }
+  Engine* e = new Engine();
+  e->m_ = d.m;
+  e->n_ = d.n;
+  e->nnz_ = d.nnz;
+  e->opt_ = opt;
+  e->fp32_ = opt.precision == 1 || opt.precision == 2;
+  e->switch_ = opt.precision == 2;
+  e->x_bounds_uniform_ = d.x_uniform;
+  e->x_lo_ = d.x_lo;
+  e->x_hi_ = d.x_hi;
+  e->K_.rows = d.m;
+  e->K_.cols = d.n;
+  e->K_.nnz = d.nnz;
+  e->K_.host_ptr = d.kptr_host;
+  e->Kt_.rows = d.n;
+  e->Kt_.cols = d.m;
+  e->Kt_.nnz = d.nnz;
+  e->Kt_.host_ptr = d.tptr_host;
+  std::string why;
+  int rc = e->alloc_all(&why);
+  if (rc != kOk) {
+    if (err) *err = why;
+    delete e;
+    return rc;
+  }
+  cudaStream_t s = e->stream_;
+  const size_t nb = static_cast<size_t>(d.nnz);
+  const size_t nt = static_cast<size_t>(d.n) + d.m;
+  auto dd = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    if (bytes == 0) return cudaSuccess;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s);
+  };
+  cudaError_t ce = dd(e->K_.ptr, d.kptr, (static_cast<size_t>(d.m) + 1) * sizeof(int));
+  if (ce == cudaSuccess) ce = dd(e->K_.idx, d.kidx, nb * sizeof(int));
+  if (ce == cudaSuccess) ce = dd(e->K_.val_orig, d.kval, nb * sizeof(double));
+  if (ce == cudaSuccess) ce = dd(e->Kt_.ptr, d.tptr, (static_cast<size_t>(d.n) + 1) * sizeof(int));
+  if (ce == cudaSuccess) ce = dd(e->Kt_.idx, d.tidx, nb * sizeof(int));
+  if (ce == cudaSuccess) ce = dd(e->Kt_.val_orig, d.tval, nb * sizeof(double));
+  if (ce == cudaSuccess) ce = dd(e->cost_orig_, d.cost, nt * sizeof(double));
+  if (ce == cudaSuccess) ce = dd(e->lower_orig_, d.lower, nt * sizeof(double));
+  if (ce == cudaSuccess) ce = dd(e->upper_orig_, d.upper, nt * sizeof(double));
+  std::vector<double> u0 = power_start(d.m);
+  if (ce == cudaSuccess && !u0.empty()) {
+    ce = cudaMemcpyAsync(e->u0_, u0.data(), u0.size() * sizeof(double), cudaMemcpyHostToDevice,
+                         s);
+  }
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&e->sm_count_, cudaDevAttrMultiProcessorCount, dev);
+  }
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) {
+    if (err) *err = std::string("device copy: ") + cudaGetErrorString(ce);
+    const int code = ce == cudaErrorMemoryAllocation ? kErrOutOfMemory : kErrCuda;
+    delete e;
+    return code;
+  }
+  rc = e->set_active_rows(d.row_inert, &why);
+  if (rc == kOk) rc = e->tune_tiles(&why);
   if (rc != kOk) {
     if (err) *err = why;
     delete e;
@@ -402,7 +500,9 @@ void append_shape_file(const ShapeKey& k, const TileShape& sh) {
 }
 
 ShapeKey shape_key(const DevOp& op, bool fp32) {
-  ShapeKey k{op.rows, op.nnz, 0, 0, 0, 0, fp32 ? 1 : 0};
+  // The rows the step kernel runs over (inert rows left out are empty).
+  const int rows = op.act_rows != nullptr ? static_cast<int>(op.act_list.size()) : op.rows;
+  ShapeKey k{rows, op.nnz, 0, 0, 0, 0, fp32 ? 1 : 0};
   for (int r = 0; r < op.rows; ++r) {
     const int len = op.host_ptr[r + 1] - op.host_ptr[r];
     k.max_len = std::max(k.max_len, len);
@@ -437,17 +537,60 @@ TileShape Engine::default_shape(const DevOp& op) const {
   return sh;
 }
 
-// Builds an operator's tiles for a shape and uploads them (replacing earlier ones).
+// The rows of K the solves iterate over: every row but the inert ones (an empty row whose
+// logical has no cost and 0 within its bounds), when the option allows and some row is inert.
+int Engine::set_active_rows(const std::vector<char>& inert, std::string* err) {
+  if (!opt_.skip_inert_rows || inert.size() != static_cast<size_t>(m_)) return kOk;
+  std::vector<int> act;
+  act.reserve(static_cast<size_t>(m_));
+  for (int i = 0; i < m_; ++i) {
+    if (!inert[i]) act.push_back(i);
+  }
+  if (act.size() == static_cast<size_t>(m_)) return kOk;
+  for (int i = 0; i < m_; ++i) {
+    if (inert[i] && K_.host_ptr[i + 1] != K_.host_ptr[i]) {
+      if (err) *err = "inert row with nonzeros";
+      return kErrInternal;
+    }
+  }
+  K_.act_list = std::move(act);
+  SG_TRY(dalloc(&K_.act_rows, K_.act_list.size()));
+  if (!K_.act_list.empty()) {
+    SG_TRY(cudaMemcpy(K_.act_rows, K_.act_list.data(), K_.act_list.size() * sizeof(int),
+                      cudaMemcpyHostToDevice));
+  }
+  return kOk;
+}
+
+// Builds an operator's tiles for a shape and uploads them (replacing earlier ones); with
+// active rows, also the tiles over those rows.
 int Engine::set_tiles(DevOp* op, const TileShape& shape) {
   std::string* err = nullptr;
   std::vector<Tile> tiles;
   int nlong = 0;
   build_tiles(op->host_ptr, shape.cap_nnz, shape.cap_rows, shape.warp_min, shape.split, &tiles,
               &nlong);
+  std::vector<Tile> act_tiles;
+  int act_nlong = 0;
+  if (op->act_rows != nullptr) {
+    // The active rows' starts: the rows left out are empty, so consecutive active rows are
+    // contiguous in the nonzeros and the tiles' nonzero ranges are the operator's own.
+    const std::vector<int>& a = op->act_list;
+    std::vector<int> vp(a.size() + 1, 0);
+    for (size_t v = 0; v < a.size(); ++v) {
+      vp[v] = op->host_ptr[a[v]];
+      vp[v + 1] = op->host_ptr[a[v] + 1];
+    }
+    build_tiles(vp, shape.cap_nnz, shape.cap_rows, shape.warp_min, shape.split, &act_tiles,
+                &act_nlong);
+  }
   SG_TRY(cudaStreamSynchronize(stream_));
   dfree(op->tiles);
   dfree(op->seg_part);
   dfree(op->lcount);
+  dfree(op->act_tiles);
+  dfree(op->act_seg_part);
+  dfree(op->act_lcount);
   op->cap_nnz = shape.cap_nnz;
   op->cap_rows = shape.cap_rows;
   op->warp_min = shape.warp_min;
@@ -463,6 +606,19 @@ int Engine::set_tiles(DevOp* op, const TileShape& shape) {
   SG_TRY(dalloc(&op->seg_part, tiles.size() * kMaxVec));
   SG_TRY(dalloc(&op->lcount, std::max(nlong, 1)));
   SG_TRY(cudaMemsetAsync(op->lcount, 0, std::max(nlong, 1) * sizeof(unsigned), stream_));
+  if (op->act_rows != nullptr) {
+    op->act_ntiles = static_cast<int>(act_tiles.size());
+    op->act_nlong = act_nlong;
+    SG_TRY(dalloc(&op->act_tiles, act_tiles.size()));
+    if (!act_tiles.empty()) {
+      SG_TRY(cudaMemcpyAsync(op->act_tiles, act_tiles.data(), act_tiles.size() * sizeof(Tile),
+                             cudaMemcpyHostToDevice, stream_));
+    }
+    SG_TRY(dalloc(&op->act_seg_part, act_tiles.size() * kMaxVec));
+    SG_TRY(dalloc(&op->act_lcount, std::max(act_nlong, 1)));
+    SG_TRY(cudaMemsetAsync(op->act_lcount, 0, std::max(act_nlong, 1) * sizeof(unsigned),
+                           stream_));
+  }
   SG_TRY(cudaStreamSynchronize(stream_));
   return kOk;
 }
@@ -488,7 +644,8 @@ double Engine::time_step_kernel(bool dual, int reps) {
     if (fp32_) {
       IterView<float> it = iter_view(it32_);
       if (dual) {
-        launch_dual_step(c, K_.view32(), it, j, std::max(1, std::min(K_.ntiles, 65535)), stream_);
+        launch_dual_step(c, K_.step32(), it, j, std::max(1, std::min(K_.step_tiles(), 65535)),
+                         stream_);
       } else {
         launch_primal_step(c, Kt_.view32(), it, j, std::max(1, std::min(Kt_.ntiles, 65535)),
                            stream_);
@@ -496,7 +653,8 @@ double Engine::time_step_kernel(bool dual, int reps) {
     } else {
       IterView<double> it = iter_view(it64_);
       if (dual) {
-        launch_dual_step(c, K_.view64(), it, j, std::max(1, std::min(K_.ntiles, 65535)), stream_);
+        launch_dual_step(c, K_.step64(), it, j, std::max(1, std::min(K_.step_tiles(), 65535)),
+                         stream_);
       } else {
         launch_primal_step(c, Kt_.view64(), it, j, std::max(1, std::min(Kt_.ntiles, 65535)),
                            stream_);
@@ -606,7 +764,7 @@ int Engine::tune_tiles(std::string* err) {
     }
   }
   dfree(long_terms_);
-  const int maxlong = std::max(std::max(K_.nlong, Kt_.nlong), 1);
+  const int maxlong = std::max(std::max(std::max(K_.nlong, K_.act_nlong), Kt_.nlong), 1);
   if (dalloc(&long_terms_, static_cast<size_t>(maxlong) * kMaxSums) != cudaSuccess) {
     if (err) *err = "out of device memory";
     return kErrOutOfMemory;
@@ -616,7 +774,8 @@ int Engine::tune_tiles(std::string* err) {
   const int eval_cap = sm_count_ * 2;
   grid_k_ = std::max(1, std::min(K_.ntiles, eval_cap));
   grid_t_ = std::max(1, std::min(Kt_.ntiles, eval_cap));
-  grid_step_k_ = std::max(1, std::min(K_.ntiles, 65535));
+  grid_step_k_ = std::max(1, std::min(K_.step_tiles(), 65535));
+  grid_full_k_ = std::max(1, std::min(K_.ntiles, 65535));
   grid_step_t_ = std::max(1, std::min(Kt_.ntiles, 65535));
   return kOk;
 }
@@ -847,19 +1006,21 @@ int Engine::equilibration(double* col_scale, double* row_scale, double* op_norm,
 namespace {
 
 // The kernels of one chunk; returns how many launches it records.
+// Ks is K over the active rows (the steps), K over every row (evaluation and detection).
 template <typename T>
-int enqueue_chunk(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
-                  const EvalView& ev, const RedView& red, double* scratch_n, int gsk, int gst,
-                  int gk, int gt, bool halpern, cudaStream_t s) {
+int enqueue_chunk(Ctl* ctl, const OpView<T>& Ks, const OpView<T>& K, const OpView<T>& Kt,
+                  const IterView<T>& it, const EvalView& ev, const RedView& red,
+                  double* scratch_n, int gsk, int gst, int gk, int gt, bool halpern,
+                  cudaStream_t s) {
   int kernels = 0;
   for (int j = 0; j < kCheckFrequency; ++j) {
-    if (K.ts.ntiles > 0) ++kernels;
+    if (Ks.ts.ntiles > 0) ++kernels;
     if (Kt.ts.ntiles > 0) ++kernels;
     if (halpern) {
       launch_halpern_primal(ctl, Kt, it, j, gst, s);
-      launch_halpern_dual(ctl, K, it, j, gsk, s);
+      launch_halpern_dual(ctl, Ks, it, j, gsk, s);
     } else {
-      launch_dual_step(ctl, K, it, j, gsk, s);
+      launch_dual_step(ctl, Ks, it, j, gsk, s);
       launch_primal_step(ctl, Kt, it, j, gst, s);
     }
   }
@@ -874,9 +1035,10 @@ int enqueue_chunk(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterV
 }  // namespace
 
 void Engine::enqueue_chunk_body() {
-  chunk_kernels_ = enqueue_chunk(ctl_, K_.view64(), Kt_.view64(), iter_view(it64_), eval_view(),
-                                 red_view(), scratch_n_, grid_step_k_, grid_step_t_, grid_k_,
-                                 grid_t_, opt_.algorithm == 2, stream_);
+  chunk_kernels_ = enqueue_chunk(ctl_, K_.step64(), K_.view64(), Kt_.view64(),
+                                 iter_view(it64_), eval_view(), red_view(), scratch_n_,
+                                 grid_step_k_, grid_step_t_, grid_k_, grid_t_,
+                                 opt_.algorithm == 2, stream_);
 }
 
 int Engine::capture_chunk() {
@@ -897,9 +1059,10 @@ int Engine::capture_chunk32() {
   IterView<float> it = iter_view(it32_);
   it.rhs = it32_.rhs;
   SG_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-  chunk32_kernels_ = enqueue_chunk(ctl32_, K_.view32(), Kt_.view32(), it, inner_eval_view(),
-                                   red_view(), scratch_n_, grid_step_k_, grid_step_t_, grid_k_,
-                                   grid_t_, opt_.algorithm == 2, stream_);
+  chunk32_kernels_ = enqueue_chunk(ctl32_, K_.step32(), K_.view32(), Kt_.view32(), it,
+                                   inner_eval_view(), red_view(), scratch_n_, grid_step_k_,
+                                   grid_step_t_, grid_k_, grid_t_, opt_.algorithm == 2,
+                                   stream_);
   SG_TRY(cudaStreamEndCapture(stream_, &chunk32_graph_));
   SG_TRY(cudaGraphInstantiate(&chunk32_exec_, chunk32_graph_, 0));
   return kOk;
@@ -1416,11 +1579,11 @@ int Engine::seam_step(double tau, double sigma, long long iter) {
   if (rc != kOk) return rc;
   if (seam_fp32_) {
     IterView<float> it = iter_view(it32_);
-    launch_dual_step(ctl_, K_.view32(), it, 0, grid_step_k_, stream_);
+    launch_dual_step(ctl_, K_.view32(), it, 0, grid_full_k_, stream_);
     launch_primal_step(ctl_, Kt_.view32(), it, 0, grid_step_t_, stream_);
   } else {
     IterView<double> it = iter_view(it64_);
-    launch_dual_step(ctl_, K_.view64(), it, 0, grid_step_k_, stream_);
+    launch_dual_step(ctl_, K_.view64(), it, 0, grid_full_k_, stream_);
     launch_primal_step(ctl_, Kt_.view64(), it, 0, grid_step_t_, stream_);
   }
   SG_TRY(cudaGetLastError());
@@ -1440,11 +1603,11 @@ int Engine::seam_halpern_step(double tau, double sigma, long long k) {
   if (seam_fp32_) {
     IterView<float> it = iter_view(it32_);
     launch_halpern_primal(ctl_, Kt_.view32(), it, 0, grid_step_t_, stream_);
-    launch_halpern_dual(ctl_, K_.view32(), it, 0, grid_step_k_, stream_);
+    launch_halpern_dual(ctl_, K_.view32(), it, 0, grid_full_k_, stream_);
   } else {
     IterView<double> it = iter_view(it64_);
     launch_halpern_primal(ctl_, Kt_.view64(), it, 0, grid_step_t_, stream_);
-    launch_halpern_dual(ctl_, K_.view64(), it, 0, grid_step_k_, stream_);
+    launch_halpern_dual(ctl_, K_.view64(), it, 0, grid_full_k_, stream_);
   }
   SG_TRY(cudaGetLastError());
   SG_TRY(cudaStreamSynchronize(stream_));
@@ -1627,9 +1790,9 @@ int Engine::seam_download(double* v, double* v_new, double* y, double* y_new, do
 namespace {
 
 template <typename T>
-int time_steps(Ctl* c, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
-               const EvalView& ev, const RedView& red, int gsk, int gst, int gk, int gt,
-               bool halpern, int reps, cudaStream_t s, double* ms) {
+int time_steps(Ctl* c, const OpView<T>& Ks, const OpView<T>& K, const OpView<T>& Kt,
+               const IterView<T>& it, const EvalView& ev, const RedView& red, int gsk, int gst,
+               int gk, int gt, bool halpern, int reps, cudaStream_t s, double* ms) {
   cudaEvent_t e[4];
   for (auto& x : e) {
     if (cudaEventCreate(&x) != cudaSuccess) return kErrCuda;
@@ -1637,9 +1800,9 @@ int time_steps(Ctl* c, const OpView<T>& K, const OpView<T>& Kt, const IterView<T
   // The step kernels the solve runs (classic or Halpern).
   auto dual = [&](int r) {
     if (halpern) {
-      launch_halpern_dual(c, K, it, r, gsk, s);
+      launch_halpern_dual(c, Ks, it, r, gsk, s);
     } else {
-      launch_dual_step(c, K, it, r, gsk, s);
+      launch_dual_step(c, Ks, it, r, gsk, s);
     }
   };
   auto primal = [&](int r) {
@@ -1690,11 +1853,11 @@ int Engine::time_kernels(int reps, double* ms_dual, double* ms_primal, double* m
   if (fp32_) {
     IterView<float> it = iter_view(it32_);
     it.rhs = it32_.rhs;
-    rc = time_steps(c, K_.view32(), Kt_.view32(), it, inner_eval_view(), red_view(),
+    rc = time_steps(c, K_.step32(), K_.view32(), Kt_.view32(), it, inner_eval_view(), red_view(),
                     grid_step_k_, grid_step_t_, grid_k_, grid_t_, opt_.algorithm == 2, reps,
                     stream_, ms);
   } else {
-    rc = time_steps(c, K_.view64(), Kt_.view64(), iter_view(it64_), eval_view(), red_view(),
+    rc = time_steps(c, K_.step64(), K_.view64(), Kt_.view64(), iter_view(it64_), eval_view(), red_view(),
                     grid_step_k_, grid_step_t_, grid_k_, grid_t_, opt_.algorithm == 2, reps,
                     stream_, ms);
   }

@@ -39,6 +39,7 @@ struct Options {
   bool autotune = true;     // time candidate tile shapes of large operators at create
   int tile_split = 0;       // built-in rule's team split of medium rows (0: a warp per row)
   double artificial_restart = 0.0;  // forced-restart fraction (0: 0.36 reference, 0.1 others)
+  bool skip_inert_rows = true;      // leave inert rows (see DevOp::act_rows) out of the solves
 };
 
 // Tile shape of an operator: nonzeros per tile (and per long-row segment), rows per short-row
@@ -87,6 +88,18 @@ struct DevOp {
   int variant = 0;
   int split = 0;
   std::vector<int> host_ptr;
+  // The rows the solves iterate over, when some rows are inert: an empty row whose logical has
+  // no cost and 0 within its bounds keeps y_i = r_i = 0 in every iterate (every iterate starts
+  // at 0, and its step only ever adds 0), so the solves' launches leave it out. act_list
+  // (host, increasing) and act_rows (device) hold the other rows; act_* the tiles over them
+  // (their row index v stands for act_rows[v]); act_rows null: every row is in.
+  std::vector<int> act_list;
+  int* act_rows = nullptr;
+  Tile* act_tiles = nullptr;
+  int act_ntiles = 0;
+  int act_nlong = 0;
+  double* act_seg_part = nullptr;
+  unsigned* act_lcount = nullptr;
 
   TileSet tileset() const {
     TileSet t;
@@ -98,10 +111,26 @@ struct DevOp {
     t.cap_nnz = cap_nnz;
     t.cap_rows = cap_rows;
     t.variant = variant;
+    t.rows = nullptr;
     return t;
   }
+  TileSet act_tileset() const {
+    if (act_rows == nullptr) return tileset();
+    TileSet t = tileset();
+    t.tiles = act_tiles;
+    t.ntiles = act_ntiles;
+    t.nlong = act_nlong;
+    t.seg_part = act_seg_part;
+    t.lcount = act_lcount;
+    t.rows = act_rows;
+    return t;
+  }
+  int step_tiles() const { return act_rows == nullptr ? ntiles : act_ntiles; }
   OpView<double> view64() const { return OpView<double>{ptr, idx, val, rows, tileset()}; }
   OpView<float> view32() const { return OpView<float>{ptr, idx, val32, rows, tileset()}; }
+  // The views of the solves' iteration launches (steps, evaluation, decisions, detection).
+  OpView<double> step64() const { return OpView<double>{ptr, idx, val, rows, act_tileset()}; }
+  OpView<float> step32() const { return OpView<float>{ptr, idx, val32, rows, act_tileset()}; }
 };
 
 // Iterate storage of one precision.
@@ -120,6 +149,27 @@ struct DevIter {
   T* rhs = nullptr;
 };
 
+// An LpProblem already in device memory (built there by sg_setup_device.cu): A by rows (K) and
+// by columns (the rows of K'), cost / lower / upper (n + m); the row starts also on the host
+// (the tile partition is built on the host).
+struct DeviceLp {
+  int m = 0, n = 0;
+  long long nnz = 0;
+  const int* kptr = nullptr;
+  const int* kidx = nullptr;
+  const double* kval = nullptr;
+  const int* tptr = nullptr;
+  const int* tidx = nullptr;
+  const double* tval = nullptr;
+  const double* cost = nullptr;
+  const double* lower = nullptr;
+  const double* upper = nullptr;
+  std::vector<int> kptr_host, tptr_host;
+  std::vector<char> row_inert;  // m: empty row, no cost, 0 within its bounds (may be empty)
+  bool x_uniform = false;  // every structural column has the bounds [x_lo, x_hi], 0 or infinite
+  double x_lo = 0.0, x_hi = 0.0;
+};
+
 class Engine {
  public:
   ~Engine();
@@ -128,6 +178,10 @@ class Engine {
   static int create(Engine** out, int m, int n, const int64_t* colptr, const int32_t* rowidx,
                     const double* val, const double* cost, const double* lower,
                     const double* upper, const Options& opt, std::string* err);
+  // The same from an LpProblem built in device memory (copied device to device; the caller
+  // keeps its buffers).
+  static int create_from_device(Engine** out, const DeviceLp& lp, const Options& opt,
+                                std::string* err);
 
   // Full PDLP solve (setup on the device, graph-replayed iterations). Outputs in the
   // LpProblem's space: x (n + m), y (m), dual_ray (m), primal_ray (n); any may be null.
@@ -159,6 +213,12 @@ class Engine {
   // Average device milliseconds of the step kernels and the evaluation (CUDA events).
   int time_kernels(int reps, double* ms_dual, double* ms_primal, double* ms_eval);
   int tile_capacity(int transpose) const { return transpose ? Kt_.cap_nnz : K_.cap_nnz; }
+  // The rows of A the solves' dual steps run over, and their tiles.
+  int step_rows(int* rows, int* tiles) const {
+    *rows = K_.act_rows != nullptr ? static_cast<int>(K_.act_list.size()) : m_;
+    *tiles = K_.step_tiles();
+    return kOk;
+  }
   int tile_shape(int transpose, int* cap_nnz, int* cap_rows, int* ntiles, int* variant,
                  int* split) const {
     const DevOp& op = transpose ? Kt_ : K_;
@@ -201,13 +261,15 @@ class Engine {
   int check(cudaError_t e, const char* what);
   TileShape default_shape(const DevOp& op) const;
   int set_tiles(DevOp* op, const TileShape& shape);
+  int set_active_rows(const std::vector<char>& inert, std::string* err);
   int tune_tiles(std::string* err);
   double time_step_kernel(bool dual, int reps);
 
   int m_ = 0, n_ = 0;
   long long nnz_ = 0;
   Options opt_;
-  int grid_k_ = 1, grid_t_ = 1, grid_step_k_ = 1, grid_step_t_ = 1;
+  // grid_step_k_: the dual steps of the solves (active rows); grid_full_k_: every row.
+  int grid_k_ = 1, grid_t_ = 1, grid_step_k_ = 1, grid_step_t_ = 1, grid_full_k_ = 1;
   int sm_count_ = 148;
   bool fp32_ = false;
   bool switch_ = false;   // FP32 PDLP, then FP64 PDLP from its answer

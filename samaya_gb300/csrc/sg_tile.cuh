@@ -176,21 +176,22 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
       for (int rr = 0; rr < rounds; ++rr) {
         const int lr = rr * kBlock + tid;
         const bool valid = lr < nrows;
-        int b = 0, e = 0;
+        int b = 0, e = 0, row = 0;
         if (valid) {
-          b = ldg(ptr + tile.r0 + lr);
-          e = ldg(ptr + tile.r0 + lr + 1);
+          row = tile_row(ts, tile.r0 + lr);
+          b = ldg(ptr + row);
+          e = ldg(ptr + row + 1);
         }
         const bool shortrow = valid && e - b <= 32;
         if constexpr (has_pre<Epi>::value) {
           typename Epi::Pre pre;
-          if (shortrow) pre = epi.load(tile.r0 + lr);
+          if (shortrow) pre = epi.load(row);
           if (shortrow) {
             ACC s[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) s[v] = ACC(0);
             short_row_sum<T, NV, MAXRED>(b, e, idx, val, prod, s);
-            epi.row(tile.r0 + lr, s, pre);
+            epi.row(row, s, pre);
           }
         } else {
           if (shortrow) {
@@ -198,7 +199,7 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
 #pragma unroll
             for (int v = 0; v < NV; ++v) s[v] = ACC(0);
             short_row_sum<T, NV, MAXRED>(b, e, idx, val, prod, s);
-            epi.row(tile.r0 + lr, s);
+            epi.row(row, s);
           }
         }
         unsigned pending = __ballot_sync(0xffffffffu, valid && !shortrow);
@@ -207,6 +208,7 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
           pending &= pending - 1u;
           const int rb = __shfl_sync(0xffffffffu, b, src);
           const int re = __shfl_sync(0xffffffffu, e, src);
+          const int rrow = __shfl_sync(0xffffffffu, row, src);
           ACC s[NV];
 #pragma unroll
           for (int v = 0; v < NV; ++v) s[v] = ACC(0);
@@ -224,7 +226,7 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
               s[v] = combine<MAXRED>(s[v], __shfl_down_sync(0xffffffffu, s[v], o));
             }
           }
-          if (lane == 0) epi.row(tile.r0 + rr * kBlock + (tid & ~31) + src, s);
+          if (lane == 0) epi.row(rrow, s);
         }
       }
     } else if (tile.kind == 2) {
@@ -237,11 +239,12 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
       const int warp = tid >> 5;
       const int team = tile.team;
       const int part = warp & (team - 1);
-      const int r = tile.r0 + warp / team;
+      const int rv = tile.r0 + warp / team;
+      const int r = rv < tile.r1 ? tile_row(ts, rv) : 0;
       ACC s[NV];
 #pragma unroll
       for (int v = 0; v < NV; ++v) s[v] = ACC(0);
-      if (r < tile.r1) {
+      if (rv < tile.r1) {
         const int b = ldg(ptr + r);
         const int e = ldg(ptr + r + 1);
         const int a0 = min(e, (b + 3) & ~3);
@@ -308,7 +311,7 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
           for (int v = 0; v < NV; ++v) partial[warp * NV + v] = s[v];
         }
         __syncthreads();
-        if (part == 0 && lane == 0 && r < tile.r1) {
+        if (part == 0 && lane == 0 && rv < tile.r1) {
           ACC tot[NV];
 #pragma unroll
           for (int v = 0; v < NV; ++v) {
@@ -370,7 +373,7 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
       block_reduce_acc<ACC, NV, MAXRED>(s, reinterpret_cast<ACC*>(red), tot);
       if (tile.nseg == 1) {
         // The whole row in one tile: no partials to combine.
-        if (tid == 0) epi.long_row(tile.lrow, tile.r0, tot);
+        if (tid == 0) epi.long_row(tile.lrow, tile_row(ts, tile.r0), tot);
         continue;
       }
       if (tid == 0) {
@@ -402,7 +405,7 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
 #pragma unroll
           for (int v = 0; v < NV; ++v) s[v] = static_cast<ACC>(sum[v]);
           ts.lcount[tile.lrow] = 0u;
-          epi.long_row(tile.lrow, tile.r0, s);
+          epi.long_row(tile.lrow, tile_row(ts, tile.r0), s);
         }
       }
       __syncthreads();

@@ -45,6 +45,7 @@ class PdlpOptions:
     autotune: bool = True
     tile_split: int = 0
     artificial_restart: float = 0.0
+    keep_inert_rows: bool = False
 
     def to_c(self) -> _native.Opts:
         o = _native.Opts()
@@ -60,6 +61,7 @@ class PdlpOptions:
         o.autotune = 1 if self.autotune else 0
         o.tile_split = int(self.tile_split)
         o.artificial_restart = float(self.artificial_restart)
+        o.keep_inert_rows = 1 if self.keep_inert_rows else 0
         return o
 
 
@@ -119,6 +121,32 @@ class PdlpSolver:
             _ptr(lp.cost, ctypes.c_double), _ptr(lp.lower, ctypes.c_double),
             _ptr(lp.upper, ctypes.c_double), ctypes.byref(o)), "sg_pdlp_create")
 
+    @classmethod
+    def from_model(cls, model, options: PdlpOptions | None = None):
+        """An engine for a model's LpProblem built on the GPU (sg_pdlp_create_model: scaling,
+        computational form and the row-major copy on the device). ``solve()`` answers in the
+        LpProblem's space; ``scaling`` holds the factors for ``problem.model_solution``."""
+        from .problem import Scaling
+        self = cls.__new__(cls)
+        self._lib = _native.load()
+        self.options = options or PdlpOptions()
+        self._h = ctypes.c_void_p()
+        m, n = int(model.m), int(model.n)
+        self.lp = LpProblem(m=m, n=n, colptr=np.zeros(n + 1, dtype=np.int64),
+                            rowidx=np.zeros(0, dtype=np.int32), vals=np.zeros(0),
+                            cost=np.zeros(0), lower=np.zeros(0), upper=np.zeros(0))
+        col, row = np.zeros(max(n, 1)), np.zeros(max(m, 1))
+        o = self.options.to_c()
+        D = ctypes.c_double
+        _native.check(self._lib.sg_pdlp_create_model(
+            ctypes.byref(self._h), m, n, _ptr(model.colptr, ctypes.c_int64),
+            _ptr(model.rowidx, ctypes.c_int32), _ptr(model.vals, D), _ptr(model.obj, D),
+            _ptr(model.col_lower, D), _ptr(model.col_upper, D), _ptr(model.row_lower, D),
+            _ptr(model.row_upper, D), 1 if model.maximize else 0, ctypes.byref(o),
+            _ptr(col, D), _ptr(row, D)), "sg_pdlp_create_model")
+        self.scaling = Scaling(col=col[:n].copy(), row=row[:m].copy())
+        return self
+
     def time_kernels(self, reps: int = 20):
         """Average device ms of one dual step, one primal step and one evaluation (CUDA events
         on the engine's stream); the next solve starts afresh."""
@@ -151,6 +179,14 @@ class PdlpSolver:
                           "sg_pdlp_tile_shape")
             out[name] = (v[0].value, v[1].value, v[2].value, v[3].value, v[4].value)
         return out
+
+    def step_rows(self) -> tuple[int, int]:
+        """(rows of A the dual steps run over, their tiles): m unless inert rows (empty, a
+        logical with no cost and 0 within its bounds) are left out."""
+        rows, tiles = ctypes.c_int(0), ctypes.c_int(0)
+        _native.check(self._lib.sg_pdlp_step_rows(self._h, ctypes.byref(rows),
+                                                  ctypes.byref(tiles)), "sg_pdlp_step_rows")
+        return rows.value, tiles.value
 
     def solve(self, x_out: np.ndarray | None = None, y_out: np.ndarray | None = None,
               download: bool = True) -> PdlpResult:

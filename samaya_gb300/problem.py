@@ -26,8 +26,9 @@ def _p(a, t):
     return a.ctypes.data_as(ctypes.POINTER(t))
 
 
-def make_problem(model: Model):
-    """Returns (LpProblem, Scaling)."""
+def make_problem(model: Model, device: bool = False):
+    """Returns (LpProblem, Scaling); ``device=True`` computes it on the GPU
+    (sg_scale_model_device, the same bits)."""
     lib = _native.load()
     m, n = model.m, model.n
     nnz = model.nnz
@@ -39,13 +40,14 @@ def make_problem(model: Model):
     row = np.zeros(max(m, 1))
     out_nnz = ctypes.c_int64(0)
     D, I64, I32 = ctypes.c_double, ctypes.c_int64, ctypes.c_int32
-    rc = lib.sg_scale_model(m, n, _p(model.colptr, I64), _p(model.rowidx, I32),
+    fn = lib.sg_scale_model_device if device else lib.sg_scale_model
+    rc = fn(m, n, _p(model.colptr, I64), _p(model.rowidx, I32),
                             _p(model.vals, D), _p(model.obj, D), _p(model.col_lower, D),
                             _p(model.col_upper, D), _p(model.row_lower, D),
                             _p(model.row_upper, D), 1 if model.maximize else 0, _p(colptr, I64),
                             _p(rowidx, I32), _p(vals, D), _p(cost, D), _p(lower, D),
                             _p(upper, D), _p(col, D), _p(row, D), ctypes.byref(out_nnz))
-    _native.check(rc, "sg_scale_model")
+    _native.check(rc, "sg_scale_model_device" if device else "sg_scale_model")
     k = out_nnz.value
     lp = LpProblem(m=m, n=n, colptr=colptr, rowidx=rowidx[:k].copy(), vals=vals[:k].copy(),
                    cost=cost, lower=lower, upper=upper)
