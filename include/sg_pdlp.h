@@ -78,6 +78,10 @@ typedef struct sg_pdlp_opts {
                                 and 0 within its bounds are left out of the solves' step
                                 launches (their dual and logical stay 0 in every iterate, so
                                 the answer is the same bits); 1: every row is stepped */
+  int row_groups;            /* dual steps over runs of rows whose k-th nonzeros lie in
+                                neighbouring columns (see sg_pdlp_step_rows): 0 (default) the
+                                tile tuner times them, 1 the built-in shape takes them, -1
+                                never */
 } sg_pdlp_opts;
 
 /* Algorithm variants. REFERENCE follows samaya's PDLP step for step (L2 Ruiz, fixed step
@@ -218,8 +222,10 @@ int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_ro
                        int* ntiles, int* variant, int* split);
 
 /* The rows of A the solves' dual steps run over (m, unless inert rows are left out: see
- * sg_pdlp_opts.keep_inert_rows) and the tiles over them. Diagnostics. */
-int sg_pdlp_step_rows(sg_pdlp* handle, int* rows, int* tiles);
+ * sg_pdlp_opts.keep_inert_rows), the tiles over them, and how many of those tiles are row
+ * groups (runs of up to 32 rows whose k-th nonzeros lie in neighbouring columns, staged so
+ * that one gather reads neighbouring entries; a tuned shape may choose them). Diagnostics. */
+int sg_pdlp_step_rows(sg_pdlp* handle, int* rows, int* tiles, int* group_tiles);
 
 /* The engine's partition of a CSR operator (row starts row_ptr, rows + 1) into tiles for a tile
  * shape (nonzeros per tile, rows per short-row tile, warp-per-row threshold, team split; the
@@ -230,6 +236,15 @@ int sg_pdlp_step_rows(sg_pdlp* handle, int* rows, int* tiles);
  * counterpart in the reference (its SpMV has no tiles); host only, no GPU needed. */
 int sg_build_tiles(int rows, const int32_t* row_ptr, int cap_nnz, int cap_rows, int warp_min,
                    int split, int32_t* tiles, int max_tiles, int* ntiles, int* nlong);
+
+/* The dual steps' partition with row groups: as sg_build_tiles, plus kind 3, a run of 8-32
+ * consecutive rows longer than warp_min, each a gather neighbour of the next (neighbours[r]
+ * nonzero: rows r and r + 1; `rows` entries), cut into segments of nonzero positions within
+ * the rows (for kind 3 the third and fourth fields are the first and end position, the ninth
+ * the group's counter when it has several segments, counted in *nlong). Host only. */
+int sg_build_group_tiles(int rows, const int32_t* row_ptr, const uint8_t* neighbours,
+                         int cap_nnz, int cap_rows, int warp_min, int split, int32_t* tiles,
+                         int max_tiles, int* ntiles, int* nlong);
 
 /* CSC -> CSR of an m x n matrix (the engine's row-major copy of A): row starts csr_ptr (m + 1),
  * column indices csr_idx and values csr_val (a_colptr[n] each), every row's columns in

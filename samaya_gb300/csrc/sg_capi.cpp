@@ -45,7 +45,51 @@ sg::Options to_options(const sg_pdlp_opts* o) {
   opt.artificial_restart =
       o->artificial_restart > 0 && o->artificial_restart < 1 ? o->artificial_restart : 0.0;
   opt.skip_inert_rows = o->keep_inert_rows == 0;
+  opt.row_groups = o->row_groups > 0 ? 1 : (o->row_groups < 0 ? -1 : 0);
   return opt;
+}
+
+// The tile partition as nine int32 per tile (sg_build_tiles, sg_build_group_tiles).
+int build_tiles_c(int rows, const int32_t* row_ptr, const uint8_t* neighbours, int cap_nnz,
+                  int cap_rows, int warp_min, int split, int32_t* tiles, int max_tiles,
+                  int* ntiles, int* nlong) {
+  if (rows < 0 || row_ptr == nullptr || ntiles == nullptr || nlong == nullptr ||
+      cap_nnz < 1 || cap_rows < 1 || warp_min < 0 || split < 0 || max_tiles < 0 ||
+      (max_tiles > 0 && tiles == nullptr)) {
+    return SG_ERR_INVALID_ARGUMENT;
+  }
+  try {
+    std::vector<int> ptr(row_ptr, row_ptr + rows + 1);
+    for (int r = 0; r < rows; ++r) {
+      if (ptr[r + 1] < ptr[r]) return SG_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<char> adj;
+    if (neighbours != nullptr) adj.assign(neighbours, neighbours + rows);
+    std::vector<sg::Tile> out;
+    int nl = 0;
+    sg::build_tiles(ptr, cap_nnz, cap_rows, warp_min, split, &out, &nl,
+                    neighbours != nullptr ? &adj : nullptr,
+                    neighbours != nullptr ? sg::group_positions(cap_nnz) : 0);
+    *ntiles = static_cast<int>(out.size());
+    *nlong = nl;
+    if (static_cast<int>(out.size()) > max_tiles) return SG_ERR_TOO_LARGE;
+    for (size_t i = 0; i < out.size(); ++i) {
+      const sg::Tile& t = out[i];
+      int32_t* o = tiles + 9 * i;
+      o[0] = t.r0;
+      o[1] = t.r1;
+      o[2] = t.k0;
+      o[3] = t.k1;
+      o[4] = t.kind;
+      o[5] = t.team;
+      o[6] = t.seg;
+      o[7] = t.nseg;
+      o[8] = t.lrow;
+    }
+    return SG_OK;
+  } catch (...) {
+    return SG_ERR_INTERNAL;
+  }
 }
 
 }  // namespace
@@ -338,46 +382,25 @@ int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_ro
   SG_SEAM(handle->engine->tile_shape(transpose, cap_nnz, cap_rows, ntiles, variant, split));
 }
 
-int sg_pdlp_step_rows(sg_pdlp* handle, int* rows, int* tiles) {
-  if (rows == nullptr || tiles == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "NULL output");
-  SG_SEAM(handle->engine->step_rows(rows, tiles));
+int sg_pdlp_step_rows(sg_pdlp* handle, int* rows, int* tiles, int* group_tiles) {
+  if (rows == nullptr || tiles == nullptr || group_tiles == nullptr) {
+    return fail(SG_ERR_INVALID_ARGUMENT, "NULL output");
+  }
+  SG_SEAM(handle->engine->step_rows(rows, tiles, group_tiles));
 }
 
 int sg_build_tiles(int rows, const int32_t* row_ptr, int cap_nnz, int cap_rows, int warp_min,
                    int split, int32_t* tiles, int max_tiles, int* ntiles, int* nlong) {
-  if (rows < 0 || row_ptr == nullptr || ntiles == nullptr || nlong == nullptr ||
-      cap_nnz < 1 || cap_rows < 1 || warp_min < 0 || split < 0 || max_tiles < 0 ||
-      (max_tiles > 0 && tiles == nullptr)) {
-    return SG_ERR_INVALID_ARGUMENT;
-  }
-  try {
-    std::vector<int> ptr(row_ptr, row_ptr + rows + 1);
-    for (int r = 0; r < rows; ++r) {
-      if (ptr[r + 1] < ptr[r]) return SG_ERR_INVALID_ARGUMENT;
-    }
-    std::vector<sg::Tile> out;
-    int nl = 0;
-    sg::build_tiles(ptr, cap_nnz, cap_rows, warp_min, split, &out, &nl);
-    *ntiles = static_cast<int>(out.size());
-    *nlong = nl;
-    if (static_cast<int>(out.size()) > max_tiles) return SG_ERR_TOO_LARGE;
-    for (size_t i = 0; i < out.size(); ++i) {
-      const sg::Tile& t = out[i];
-      int32_t* o = tiles + 9 * i;
-      o[0] = t.r0;
-      o[1] = t.r1;
-      o[2] = t.k0;
-      o[3] = t.k1;
-      o[4] = t.kind;
-      o[5] = t.team;
-      o[6] = t.seg;
-      o[7] = t.nseg;
-      o[8] = t.lrow;
-    }
-    return SG_OK;
-  } catch (...) {
-    return SG_ERR_INTERNAL;
-  }
+  return build_tiles_c(rows, row_ptr, nullptr, cap_nnz, cap_rows, warp_min, split, tiles,
+                       max_tiles, ntiles, nlong);
+}
+
+int sg_build_group_tiles(int rows, const int32_t* row_ptr, const uint8_t* neighbours,
+                         int cap_nnz, int cap_rows, int warp_min, int split, int32_t* tiles,
+                         int max_tiles, int* ntiles, int* nlong) {
+  if (neighbours == nullptr) return SG_ERR_INVALID_ARGUMENT;
+  return build_tiles_c(rows, row_ptr, neighbours, cap_nnz, cap_rows, warp_min, split, tiles,
+                       max_tiles, ntiles, nlong);
 }
 
 int sg_spmv(sg_pdlp* handle, int transpose, const double* x, double* y) {

@@ -27,7 +27,9 @@ constexpr int kCheckFrequency = 64;  // iterations between evaluations (pdlp.cpp
 // One CTA's share of an operator. kind 0: rows [r0, r1) whole, nonzeros [k0, k1);
 // kind 1: one segment [k0, k1) of long row r0 (r1 = r0 + 1), segment `seg` of `nseg`, long
 // row id `lrow` (its partials are combined by the last segment to finish); kind 2: rows
-// [r0, r1) of medium length, `team` warps each.
+// [r0, r1) of medium length, `team` warps each; kind 3 (dual step tile sets only): a group of
+// up to 32 consecutive rows [r0, r1) whose k-th nonzeros lie in neighbouring columns, nonzero
+// positions [k0, k1) within each row (segment `seg` of `nseg`; counter `lrow` when nseg > 1).
 struct Tile {
   int r0, r1;
   int k0, k1;
@@ -51,7 +53,12 @@ struct TileSet {
   // the rows (rows that are left out are empty, so every nonzero position is unchanged), and
   // a tile's row index v stands for rows[v].
   const int* rows;
+  int groups;         // kind-3 tiles in the set (0: none; only the dual step kernels take them)
+  double* grp_part;   // [ntiles * 32] partial sums of kind-3 segments (when groups > 0)
 };
+
+constexpr int kGroupRows = 32;  // rows of a kind-3 tile at most (a warp's lanes)
+constexpr int kGroupPos = 16;   // nonzero positions per row staged per warp and round
 
 __device__ __forceinline__ int tile_row(const TileSet& ts, int v) {
   return ts.rows != nullptr ? __ldg(ts.rows + v) : v;

@@ -55,10 +55,13 @@ std::vector<double> power_start(int m) {
 // tiles (kind 2); the other rows go consecutively into tiles of at most tile_nnz nonzeros and
 // tile_rows rows, a thread per row (kind 0).
 void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, int warp_min,
-                 int split, std::vector<Tile>* out, int* nlong) {
+                 int split, std::vector<Tile>* out, int* nlong, const std::vector<char>* adj,
+                 int group_pos) {
   out->clear();
   *nlong = 0;
   const int rows = static_cast<int>(ptr.size()) - 1;
+  const bool grouping = adj != nullptr && group_pos > 0 &&
+                        adj->size() >= static_cast<size_t>(std::max(rows, 0));
   // Rows longer than a tile are split into CTA segments (kind 1); rows of more than
   // warp_min nonzeros get a warp each, kWarpsPerTile rows per tile (kind 2) — or, with
   // split > 0, a team of the fewest warps (a power of two up to kWarpsPerTile) giving each at
@@ -71,9 +74,45 @@ void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, int w
     }
     return t;
   };
+  // The run of gather-neighbour rows from row q, each longer than warp_min (at most
+  // kGroupRows; 0 without grouping), and its longest row.
+  auto run_at = [&](int q, int* maxlen) {
+    if (!grouping || ptr[q + 1] - ptr[q] <= warp_min) return 0;
+    int g = 1;
+    *maxlen = ptr[q + 1] - ptr[q];
+    while (g < kGroupRows && q + g < rows && (*adj)[q + g - 1] &&
+           ptr[q + g + 1] - ptr[q + g] > warp_min) {
+      *maxlen = std::max(*maxlen, ptr[q + g + 1] - ptr[q + g]);
+      ++g;
+    }
+    return g;
+  };
   int r = 0;
   while (r < rows) {
     const int len = ptr[r + 1] - ptr[r];
+    if (grouping) {
+      int maxlen = 0;
+      const int g = run_at(r, &maxlen);
+      if (g >= 8) {
+        const int nseg = (maxlen + group_pos - 1) / group_pos;
+        const int lrow = nseg > 1 ? (*nlong)++ : -1;
+        for (int s = 0; s < nseg; ++s) {
+          Tile t{};
+          t.r0 = r;
+          t.r1 = r + g;
+          t.k0 = s * group_pos;
+          t.k1 = std::min(maxlen, (s + 1) * group_pos);
+          t.kind = 3;
+          t.team = 1;
+          t.seg = s;
+          t.nseg = nseg;
+          t.lrow = lrow;
+          out->push_back(t);
+        }
+        r += g;
+        continue;
+      }
+    }
     if (len > warp_min && len <= long_len) {
       Tile t{};
       t.r0 = r;
@@ -81,6 +120,8 @@ void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, int w
       while (r < rows && r - t.r0 < kWarpsPerTile / t.team) {
         const int l = ptr[r + 1] - ptr[r];
         if (l <= warp_min || l > long_len || team_of(l) != t.team) break;
+        int unused = 0;
+        if (r > t.r0 && run_at(r, &unused) >= 8) break;  // a row group starts here
         ++r;
       }
       t.r1 = r;
@@ -170,9 +211,10 @@ Engine::~Engine() {
     dfree(op->seg_part);
     dfree(op->lcount);
     dfree(op->act_rows);
-    dfree(op->act_tiles);
-    dfree(op->act_seg_part);
-    dfree(op->act_lcount);
+    dfree(op->st_tiles);
+    dfree(op->st_seg_part);
+    dfree(op->st_grp_part);
+    dfree(op->st_lcount);
   }
   for (double** p : {&it64_.V[0], &it64_.V[1], &it64_.Vbar, &it64_.Y[0], &it64_.Y[1],
                      &it64_.Verg, &it64_.Yerg, &it64_.Vrst, &it64_.Yrst, &it64_.cost,
@@ -347,6 +389,7 @@ int Engine::create(Engine** out, int m, int n, const int64_t* colptr, const int3
     }
     rc = e->set_active_rows(inert, &why);
   }
+  if (rc == kOk) rc = e->find_neighbours(&why);
   // Tiles of both operators (tuned or by the built-in rule), then the grids.
   if (rc == kOk) rc = e->tune_tiles(&why);
   if (rc != kOk) {
@@ -434,6 +477,7 @@ int Engine::create_from_device(Engine** out, const DeviceLp& d, const Options& o
     return code;
   }
   rc = e->set_active_rows(d.row_inert, &why);
+  if (rc == kOk) rc = e->find_neighbours(&why);
   if (rc == kOk) rc = e->tune_tiles(&why);
   if (rc != kOk) {
     if (err) *err = why;
@@ -453,9 +497,11 @@ struct ShapeKey {
   int max_len;
   long long over32, over128, over4096;
   int fp32;
+  int groups;  // the row-group option (0 tuned, 1 built-in, -1 never)
   bool operator<(const ShapeKey& o) const {
-    return std::tie(rows, nnz, max_len, over32, over128, over4096, fp32) <
-           std::tie(o.rows, o.nnz, o.max_len, o.over32, o.over128, o.over4096, o.fp32);
+    return std::tie(rows, nnz, max_len, over32, over128, over4096, fp32, groups) <
+           std::tie(o.rows, o.nnz, o.max_len, o.over32, o.over128, o.over4096, o.fp32,
+                    o.groups);
   }
 };
 
@@ -465,7 +511,7 @@ bool g_shape_file_read = false;
 
 // SG_TILE_CACHE names a text file that carries the tuner's choices across processes (so that a
 // profiler run, whose launches cannot be timed, uses the shapes a plain run picked): one line
-// per operator, the key's seven fields then the shape's five. Read once per process, appended
+// per operator, the key's eight fields then the shape's six. Read once per process, appended
 // after each tuning. Call with g_shape_mu held.
 void read_shape_file() {
   if (g_shape_file_read) return;
@@ -476,12 +522,13 @@ void read_shape_file() {
   if (f == nullptr) return;
   ShapeKey k{};
   TileShape sh;
-  while (std::fscanf(f, "%d %lld %d %lld %lld %lld %d %d %d %d %d %d", &k.rows, &k.nnz,
-                     &k.max_len, &k.over32, &k.over128, &k.over4096, &k.fp32, &sh.cap_nnz,
-                     &sh.cap_rows, &sh.warp_min, &sh.variant, &sh.split) == 12) {
+  while (std::fscanf(f, "%d %lld %d %lld %lld %lld %d %d %d %d %d %d %d %d", &k.rows, &k.nnz,
+                     &k.max_len, &k.over32, &k.over128, &k.over4096, &k.fp32, &k.groups,
+                     &sh.cap_nnz, &sh.cap_rows, &sh.warp_min, &sh.variant, &sh.split,
+                     &sh.groups) == 14) {
     if (sh.cap_nnz >= 256 && sh.cap_nnz <= 4 * kTileNnz && sh.cap_rows >= 1 &&
         sh.cap_rows <= kTileRows && sh.warp_min >= 32 && (sh.variant == 0 || sh.variant == 1) &&
-        sh.split >= 0) {
+        sh.split >= 0 && (sh.groups == 0 || sh.groups == 1)) {
       g_shape_cache[k] = sh;
     }
   }
@@ -493,16 +540,16 @@ void append_shape_file(const ShapeKey& k, const TileShape& sh) {
   if (path == nullptr || *path == '\0') return;
   FILE* f = std::fopen(path, "a");
   if (f == nullptr) return;
-  std::fprintf(f, "%d %lld %d %lld %lld %lld %d %d %d %d %d %d\n", k.rows, k.nnz, k.max_len,
-               k.over32, k.over128, k.over4096, k.fp32, sh.cap_nnz, sh.cap_rows, sh.warp_min,
-               sh.variant, sh.split);
+  std::fprintf(f, "%d %lld %d %lld %lld %lld %d %d %d %d %d %d %d %d\n", k.rows, k.nnz,
+               k.max_len, k.over32, k.over128, k.over4096, k.fp32, k.groups, sh.cap_nnz,
+               sh.cap_rows, sh.warp_min, sh.variant, sh.split, sh.groups);
   std::fclose(f);
 }
 
-ShapeKey shape_key(const DevOp& op, bool fp32) {
+ShapeKey shape_key(const DevOp& op, bool fp32, int groups) {
   // The rows the step kernel runs over (inert rows left out are empty).
   const int rows = op.act_rows != nullptr ? static_cast<int>(op.act_list.size()) : op.rows;
-  ShapeKey k{rows, op.nnz, 0, 0, 0, 0, fp32 ? 1 : 0};
+  ShapeKey k{rows, op.nnz, 0, 0, 0, 0, fp32 ? 1 : 0, groups};
   for (int r = 0; r < op.rows; ++r) {
     const int len = op.host_ptr[r + 1] - op.host_ptr[r];
     k.max_len = std::max(k.max_len, len);
@@ -534,6 +581,7 @@ TileShape Engine::default_shape(const DevOp& op) const {
   }
   sh.variant = 2 * in_long >= op.nnz && op.nnz > 0 ? 1 : 0;
   sh.split = opt_.tile_split;
+  sh.groups = opt_.row_groups > 0 ? 1 : 0;
   return sh;
 }
 
@@ -562,40 +610,93 @@ int Engine::set_active_rows(const std::vector<char>& inert, std::string* err) {
   return kOk;
 }
 
+// Positions per segment of a kind-3 row group: a multiple of the CTA's 8 x 16-position blocks
+// holding about a tile's nonzeros for 32 rows.
+int group_positions(int cap_nnz) {
+  const int step = (kBlock / 32) * kGroupPos;
+  return std::max(step, (cap_nnz / kGroupRows) / step * step);
+}
+
+// The gather neighbours among K's rows (row_neighbours_kernel), kept on the host for the tile
+// partition; none: host_adj stays empty.
+int Engine::find_neighbours(std::string* err) {
+  K_.host_adj.clear();
+  if (m_ < 2 || nnz_ == 0) return kOk;
+  unsigned char* d = nullptr;
+  SG_TRY(dalloc(&d, static_cast<size_t>(m_)));
+  launch_row_neighbours(m_, K_.ptr, K_.idx, d, stream_);
+  std::vector<char> adj(static_cast<size_t>(m_));
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    e = cudaMemcpyAsync(adj.data(), d, adj.size(), cudaMemcpyDeviceToHost, stream_);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+  dfree(d);
+  if (e != cudaSuccess) {
+    if (err) *err = std::string("row neighbours: ") + cudaGetErrorString(e);
+    return kErrCuda;
+  }
+  for (char a : adj) {
+    if (a) {
+      K_.host_adj = std::move(adj);
+      break;
+    }
+  }
+  return kOk;
+}
+
 // Builds an operator's tiles for a shape and uploads them (replacing earlier ones); with
-// active rows, also the tiles over those rows.
+// inert rows left out or row groups, also the dual steps' tile set.
 int Engine::set_tiles(DevOp* op, const TileShape& shape) {
   std::string* err = nullptr;
   std::vector<Tile> tiles;
   int nlong = 0;
   build_tiles(op->host_ptr, shape.cap_nnz, shape.cap_rows, shape.warp_min, shape.split, &tiles,
               &nlong);
-  std::vector<Tile> act_tiles;
-  int act_nlong = 0;
-  if (op->act_rows != nullptr) {
+  const bool grouped =
+      shape.groups != 0 && op == &K_ && !op->host_adj.empty() && opt_.row_groups >= 0;
+  const bool step_set = op->act_rows != nullptr || grouped;
+  std::vector<Tile> st_tiles;
+  int st_nlong = 0;
+  int st_groups = 0;
+  if (step_set) {
     // The active rows' starts: the rows left out are empty, so consecutive active rows are
-    // contiguous in the nonzeros and the tiles' nonzero ranges are the operator's own.
-    const std::vector<int>& a = op->act_list;
-    std::vector<int> vp(a.size() + 1, 0);
-    for (size_t v = 0; v < a.size(); ++v) {
-      vp[v] = op->host_ptr[a[v]];
-      vp[v + 1] = op->host_ptr[a[v] + 1];
+    // contiguous in the nonzeros and the tiles' nonzero ranges are the operator's own. Two
+    // active rows are gather neighbours when they are neighbouring rows of the operator.
+    const bool sub = op->act_rows != nullptr;
+    const size_t na = sub ? op->act_list.size() : static_cast<size_t>(op->rows);
+    std::vector<int> vp(na + 1, 0);
+    std::vector<char> vadj;
+    if (grouped) vadj.assign(na, 0);
+    for (size_t v = 0; v < na; ++v) {
+      const int r = sub ? op->act_list[v] : static_cast<int>(v);
+      vp[v] = op->host_ptr[r];
+      vp[v + 1] = op->host_ptr[r + 1];
+      if (grouped && v + 1 < na) {
+        const int rn = sub ? op->act_list[v + 1] : r + 1;
+        vadj[v] = rn == r + 1 && op->host_adj[r];
+      }
     }
-    build_tiles(vp, shape.cap_nnz, shape.cap_rows, shape.warp_min, shape.split, &act_tiles,
-                &act_nlong);
+    build_tiles(vp, shape.cap_nnz, shape.cap_rows, shape.warp_min, shape.split, &st_tiles,
+                &st_nlong, grouped ? &vadj : nullptr,
+                grouped ? group_positions(shape.cap_nnz) : 0);
+    for (const Tile& t : st_tiles) st_groups += t.kind == 3;
   }
   SG_TRY(cudaStreamSynchronize(stream_));
   dfree(op->tiles);
   dfree(op->seg_part);
   dfree(op->lcount);
-  dfree(op->act_tiles);
-  dfree(op->act_seg_part);
-  dfree(op->act_lcount);
+  dfree(op->st_tiles);
+  dfree(op->st_seg_part);
+  dfree(op->st_grp_part);
+  dfree(op->st_lcount);
+  op->step_set = false;
   op->cap_nnz = shape.cap_nnz;
   op->cap_rows = shape.cap_rows;
   op->warp_min = shape.warp_min;
   op->variant = shape.variant;
   op->split = shape.split;
+  op->groups = grouped ? 1 : 0;
   op->ntiles = static_cast<int>(tiles.size());
   op->nlong = nlong;
   SG_TRY(dalloc(&op->tiles, tiles.size()));
@@ -606,18 +707,21 @@ int Engine::set_tiles(DevOp* op, const TileShape& shape) {
   SG_TRY(dalloc(&op->seg_part, tiles.size() * kMaxVec));
   SG_TRY(dalloc(&op->lcount, std::max(nlong, 1)));
   SG_TRY(cudaMemsetAsync(op->lcount, 0, std::max(nlong, 1) * sizeof(unsigned), stream_));
-  if (op->act_rows != nullptr) {
-    op->act_ntiles = static_cast<int>(act_tiles.size());
-    op->act_nlong = act_nlong;
-    SG_TRY(dalloc(&op->act_tiles, act_tiles.size()));
-    if (!act_tiles.empty()) {
-      SG_TRY(cudaMemcpyAsync(op->act_tiles, act_tiles.data(), act_tiles.size() * sizeof(Tile),
+  if (step_set) {
+    op->st_ntiles = static_cast<int>(st_tiles.size());
+    op->st_nlong = st_nlong;
+    op->st_groups = st_groups;
+    SG_TRY(dalloc(&op->st_tiles, st_tiles.size()));
+    if (!st_tiles.empty()) {
+      SG_TRY(cudaMemcpyAsync(op->st_tiles, st_tiles.data(), st_tiles.size() * sizeof(Tile),
                              cudaMemcpyHostToDevice, stream_));
     }
-    SG_TRY(dalloc(&op->act_seg_part, act_tiles.size() * kMaxVec));
-    SG_TRY(dalloc(&op->act_lcount, std::max(act_nlong, 1)));
-    SG_TRY(cudaMemsetAsync(op->act_lcount, 0, std::max(act_nlong, 1) * sizeof(unsigned),
+    SG_TRY(dalloc(&op->st_seg_part, st_tiles.size() * kMaxVec));
+    SG_TRY(dalloc(&op->st_grp_part, st_groups > 0 ? st_tiles.size() * kGroupRows : 1));
+    SG_TRY(dalloc(&op->st_lcount, std::max(st_nlong, 1)));
+    SG_TRY(cudaMemsetAsync(op->st_lcount, 0, std::max(st_nlong, 1) * sizeof(unsigned),
                            stream_));
+    op->step_set = true;
   }
   SG_TRY(cudaStreamSynchronize(stream_));
   return kOk;
@@ -689,7 +793,7 @@ int Engine::tune_tiles(std::string* err) {
     ShapeKey key{};
     bool cached = false;
     if (tune) {
-      key = shape_key(*op, fp32_);
+      key = shape_key(*op, fp32_, opt_.row_groups);
       std::lock_guard<std::mutex> lock(g_shape_mu);
       read_shape_file();
       auto it = g_shape_cache.find(key);
@@ -733,6 +837,15 @@ int Engine::tune_tiles(std::string* err) {
       }
       constexpr double kTuneMargin = 0.97;
       double best_ms = -1.0;
+      // With gather-neighbour rows, every candidate also with row groups.
+      if (which == 0 && !op->host_adj.empty() && opt_.row_groups == 0) {
+        const size_t plain = cands.size();
+        for (size_t c = 0; c < plain; ++c) {
+          TileShape g = cands[c];
+          g.groups = 1;
+          cands.push_back(g);
+        }
+      }
       for (const TileShape& sh : cands) {
         const int rc = set_tiles(op, sh);
         if (rc != kOk) {
@@ -764,7 +877,7 @@ int Engine::tune_tiles(std::string* err) {
     }
   }
   dfree(long_terms_);
-  const int maxlong = std::max(std::max(std::max(K_.nlong, K_.act_nlong), Kt_.nlong), 1);
+  const int maxlong = std::max(std::max(std::max(K_.nlong, K_.st_nlong), Kt_.nlong), 1);
   if (dalloc(&long_terms_, static_cast<size_t>(maxlong) * kMaxSums) != cudaSuccess) {
     if (err) *err = "out of device memory";
     return kErrOutOfMemory;
@@ -1579,11 +1692,11 @@ int Engine::seam_step(double tau, double sigma, long long iter) {
   if (rc != kOk) return rc;
   if (seam_fp32_) {
     IterView<float> it = iter_view(it32_);
-    launch_dual_step(ctl_, K_.view32(), it, 0, grid_full_k_, stream_);
+    launch_dual_step(ctl_, seam_dual32(), it, 0, seam_grid_k(), stream_);
     launch_primal_step(ctl_, Kt_.view32(), it, 0, grid_step_t_, stream_);
   } else {
     IterView<double> it = iter_view(it64_);
-    launch_dual_step(ctl_, K_.view64(), it, 0, grid_full_k_, stream_);
+    launch_dual_step(ctl_, seam_dual64(), it, 0, seam_grid_k(), stream_);
     launch_primal_step(ctl_, Kt_.view64(), it, 0, grid_step_t_, stream_);
   }
   SG_TRY(cudaGetLastError());
@@ -1603,11 +1716,11 @@ int Engine::seam_halpern_step(double tau, double sigma, long long k) {
   if (seam_fp32_) {
     IterView<float> it = iter_view(it32_);
     launch_halpern_primal(ctl_, Kt_.view32(), it, 0, grid_step_t_, stream_);
-    launch_halpern_dual(ctl_, K_.view32(), it, 0, grid_full_k_, stream_);
+    launch_halpern_dual(ctl_, seam_dual32(), it, 0, seam_grid_k(), stream_);
   } else {
     IterView<double> it = iter_view(it64_);
     launch_halpern_primal(ctl_, Kt_.view64(), it, 0, grid_step_t_, stream_);
-    launch_halpern_dual(ctl_, K_.view64(), it, 0, grid_full_k_, stream_);
+    launch_halpern_dual(ctl_, seam_dual64(), it, 0, seam_grid_k(), stream_);
   }
   SG_TRY(cudaGetLastError());
   SG_TRY(cudaStreamSynchronize(stream_));

@@ -40,6 +40,7 @@ struct Options {
   int tile_split = 0;       // built-in rule's team split of medium rows (0: a warp per row)
   double artificial_restart = 0.0;  // forced-restart fraction (0: 0.36 reference, 0.1 others)
   bool skip_inert_rows = true;      // leave inert rows (see DevOp::act_rows) out of the solves
+  int row_groups = 0;               // kind-3 row groups: 0 tuner decides, 1 built-in, -1 never
 };
 
 // Tile shape of an operator: nonzeros per tile (and per long-row segment), rows per short-row
@@ -50,6 +51,7 @@ struct TileShape {
   int warp_min = kWarpRowMin;
   int variant = 0;          // step kernel variant (see sg_kernels.cu)
   int split = 0;            // kind-2 rows: nonzeros per warp of a team (0: a warp per row)
+  int groups = 0;           // dual steps: runs of gather-neighbour rows as kind-3 row groups
 };
 
 struct SolveInfo {
@@ -87,19 +89,28 @@ struct DevOp {
   int warp_min = kWarpRowMin;
   int variant = 0;
   int split = 0;
+  int groups = 0;
   std::vector<int> host_ptr;
   // The rows the solves iterate over, when some rows are inert: an empty row whose logical has
   // no cost and 0 within its bounds keeps y_i = r_i = 0 in every iterate (every iterate starts
   // at 0, and its step only ever adds 0), so the solves' launches leave it out. act_list
-  // (host, increasing) and act_rows (device) hold the other rows; act_* the tiles over them
-  // (their row index v stands for act_rows[v]); act_rows null: every row is in.
+  // (host, increasing) and act_rows (device) hold the other rows (a step-set tile's row index
+  // v stands for act_rows[v]); act_rows null: every row is in.
   std::vector<int> act_list;
   int* act_rows = nullptr;
-  Tile* act_tiles = nullptr;
-  int act_ntiles = 0;
-  int act_nlong = 0;
-  double* act_seg_part = nullptr;
-  unsigned* act_lcount = nullptr;
+  // host_adj[i]: rows i and i + 1 are gather neighbours (their k-th nonzeros lie 1-4 columns
+  // apart: sampled at 8 positions), the runs a shape with `groups` turns into kind-3 tiles.
+  std::vector<char> host_adj;
+  // The step set: the tiles the solves' dual steps run (over the active rows, with the row
+  // groups), when it differs from the full set (step_set).
+  bool step_set = false;
+  Tile* st_tiles = nullptr;
+  int st_ntiles = 0;
+  int st_nlong = 0;
+  int st_groups = 0;
+  double* st_seg_part = nullptr;
+  double* st_grp_part = nullptr;
+  unsigned* st_lcount = nullptr;
 
   TileSet tileset() const {
     TileSet t;
@@ -112,25 +123,29 @@ struct DevOp {
     t.cap_rows = cap_rows;
     t.variant = variant;
     t.rows = nullptr;
+    t.groups = 0;
+    t.grp_part = nullptr;
     return t;
   }
-  TileSet act_tileset() const {
-    if (act_rows == nullptr) return tileset();
+  TileSet step_tileset() const {
+    if (!step_set) return tileset();
     TileSet t = tileset();
-    t.tiles = act_tiles;
-    t.ntiles = act_ntiles;
-    t.nlong = act_nlong;
-    t.seg_part = act_seg_part;
-    t.lcount = act_lcount;
+    t.tiles = st_tiles;
+    t.ntiles = st_ntiles;
+    t.nlong = st_nlong;
+    t.seg_part = st_seg_part;
+    t.lcount = st_lcount;
     t.rows = act_rows;
+    t.groups = st_groups;
+    t.grp_part = st_grp_part;
     return t;
   }
-  int step_tiles() const { return act_rows == nullptr ? ntiles : act_ntiles; }
+  int step_tiles() const { return step_set ? st_ntiles : ntiles; }
   OpView<double> view64() const { return OpView<double>{ptr, idx, val, rows, tileset()}; }
   OpView<float> view32() const { return OpView<float>{ptr, idx, val32, rows, tileset()}; }
-  // The views of the solves' iteration launches (steps, evaluation, decisions, detection).
-  OpView<double> step64() const { return OpView<double>{ptr, idx, val, rows, act_tileset()}; }
-  OpView<float> step32() const { return OpView<float>{ptr, idx, val32, rows, act_tileset()}; }
+  // The views of the solves' dual steps (evaluation, detection and the rest take the full set).
+  OpView<double> step64() const { return OpView<double>{ptr, idx, val, rows, step_tileset()}; }
+  OpView<float> step32() const { return OpView<float>{ptr, idx, val32, rows, step_tileset()}; }
 };
 
 // Iterate storage of one precision.
@@ -213,10 +228,11 @@ class Engine {
   // Average device milliseconds of the step kernels and the evaluation (CUDA events).
   int time_kernels(int reps, double* ms_dual, double* ms_primal, double* ms_eval);
   int tile_capacity(int transpose) const { return transpose ? Kt_.cap_nnz : K_.cap_nnz; }
-  // The rows of A the solves' dual steps run over, and their tiles.
-  int step_rows(int* rows, int* tiles) const {
+  // The rows of A the solves' dual steps run over, their tiles, and the row-group tiles.
+  int step_rows(int* rows, int* tiles, int* group_tiles) const {
     *rows = K_.act_rows != nullptr ? static_cast<int>(K_.act_list.size()) : m_;
     *tiles = K_.step_tiles();
+    *group_tiles = K_.step_set ? K_.st_groups : 0;
     return kOk;
   }
   int tile_shape(int transpose, int* cap_nnz, int* cap_rows, int* ntiles, int* variant,
@@ -262,6 +278,13 @@ class Engine {
   TileShape default_shape(const DevOp& op) const;
   int set_tiles(DevOp* op, const TileShape& shape);
   int set_active_rows(const std::vector<char>& inert, std::string* err);
+  // The seam's dual steps: the solves' tiles (row groups included) unless inert rows are left
+  // out of them (a seam state may give those rows any value), else every row.
+  bool seam_step_set() const { return K_.step_set && K_.act_rows == nullptr; }
+  OpView<double> seam_dual64() const { return seam_step_set() ? K_.step64() : K_.view64(); }
+  OpView<float> seam_dual32() const { return seam_step_set() ? K_.step32() : K_.view32(); }
+  int seam_grid_k() const { return seam_step_set() ? grid_step_k_ : grid_full_k_; }
+  int find_neighbours(std::string* err);
   int tune_tiles(std::string* err);
   double time_step_kernel(bool dual, int reps);
 
@@ -331,8 +354,14 @@ class Engine {
 };
 
 // Builds the tile partition of a CSR operator (host). Exposed for the CPU tests.
+// With adj (adj[r]: rows r and r + 1 are gather neighbours) and group_pos > 0, runs of 8-32
+// neighbouring rows longer than warp_min become kind-3 row groups of group_pos positions per
+// segment.
 void build_tiles(const std::vector<int>& ptr, int tile_nnz, int tile_rows, int warp_min,
-                 int split, std::vector<Tile>* out, int* nlong);
+                 int split, std::vector<Tile>* out, int* nlong,
+                 const std::vector<char>* adj = nullptr, int group_pos = 0);
+// Positions per segment of a kind-3 row group for a tile capacity.
+int group_positions(int cap_nnz);
 
 // Device facts for sg_pdlp_available.
 int device_info(int* major, int* minor, char* name, size_t len);

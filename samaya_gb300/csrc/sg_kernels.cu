@@ -234,12 +234,14 @@ __device__ __forceinline__ StepScalars<ACC> step_scalars(const Ctl* __restrict__
 //      step took 108 us instead of 92);
 //   1: 128 registers, the warp-per-row and segment loops unrolled twice as deep (operators of
 //      long rows, whose few CTAs need more loads in flight each; at 3 CTAs per SM, 80
-//      registers, no faster on the transportation LP).
+//      registers, no faster on the transportation LP);
+//   2 (dual steps only): variant 0 plus the kind-3 row groups of a tile set that has them.
 // (Measured and not kept: a third variant loading a short row's first three pairs of
 // nonzeros together at 4 CTAs per SM; no faster on the transportation or power-law LPs.)
 template <typename T>
 constexpr int step_min_blocks(int variant, bool dual) {
   if (variant == 1) return 2;
+  if (variant == 2) return sizeof(T) == 8 ? 3 : 4;
   if (sizeof(T) == 8) return dual ? 4 : 5;
   return dual ? 5 : 6;
 }
@@ -272,7 +274,7 @@ __global__ void __launch_bounds__(kBlock, step_min_blocks<T>(VAR, true)) dual_st
   epi.alpha = sc.alpha;
   epi.beta = sc.beta;
   Gather1<T, ACC> g{it.Vbar};
-  run_tiles<T, ACC, 1, Gather1<T, ACC>, DualEpi<T, ACC>, false, VAR == 1>(
+  run_tiles<T, ACC, 1, Gather1<T, ACC>, DualEpi<T, ACC>, false, VAR == 1, VAR == 2>(
       K.ts, K.ptr, K.idx, K.val, g, epi);
 }
 
@@ -467,7 +469,7 @@ __global__ void __launch_bounds__(kBlock, step_min_blocks<T>(VAR, true)) halpern
   epi.w = sc.alpha;
   epi.hat = halpern_writes_hat(ctl, t, j);
   Gather1<T, ACC> g{it.Vbar};
-  run_tiles<T, ACC, 1, Gather1<T, ACC>, HalpernDualEpi<T, ACC>, false, VAR == 1>(
+  run_tiles<T, ACC, 1, Gather1<T, ACC>, HalpernDualEpi<T, ACC>, false, VAR == 1, VAR == 2>(
       K.ts, K.ptr, K.idx, K.val, g, epi);
 }
 
@@ -1576,6 +1578,16 @@ size_t tile_smem_bytes(const TileSet& ts, int nv, size_t acc_bytes) {
   return tile_smem_size(nv, acc_bytes, ts.cap_nnz, ts.cap_rows);
 }
 
+namespace {
+
+// The dual step launches: the kind-3 staging when the tile set has row groups.
+template <typename T>
+size_t dual_smem_bytes(const TileSet& ts) {
+  return ts.groups > 0 ? group_smem_size<T, Acc<T>>() : tile_smem_bytes(ts, 1, sizeof(T));
+}
+
+}  // namespace
+
 void configure_kernels() {
   // Opt in to large dynamic shared memory; the launch sizes themselves follow each operator's
   // tile capacity, so occupancy is set by the actual size.
@@ -1591,16 +1603,20 @@ void configure_kernels() {
   cudaFuncSetAttribute(dual_step_kernel<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(primal_step_kernel<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(dual_step_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(dual_step_kernel<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(primal_step_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(dual_step_kernel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(dual_step_kernel<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(primal_step_kernel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(halpern_dual_kernel<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(halpern_primal_kernel<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(halpern_dual_kernel<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(halpern_primal_kernel<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(halpern_dual_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(halpern_dual_kernel<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(halpern_primal_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(halpern_dual_kernel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(halpern_dual_kernel<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(halpern_primal_kernel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_farkas_cols_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_farkas_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
@@ -1616,8 +1632,10 @@ template <typename T>
 void launch_dual_step(const Ctl* ctl, const OpView<T>& K, const IterView<T>& it, int j, int grid,
                       cudaStream_t s) {
   if (K.ts.ntiles == 0) return;
-  const size_t sm = tile_smem_bytes(K.ts, 1, sizeof(T));
-  if (K.ts.variant == 1) {
+  const size_t sm = dual_smem_bytes<T>(K.ts);
+  if (K.ts.groups > 0) {
+    dual_step_kernel<T, 2><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
+  } else if (K.ts.variant == 1) {
     dual_step_kernel<T, 1><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
   } else {
     dual_step_kernel<T, 0><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
@@ -1652,8 +1670,10 @@ template <typename T>
 void launch_halpern_dual(const Ctl* ctl, const OpView<T>& K, const IterView<T>& it, int j,
                          int grid, cudaStream_t s) {
   if (K.ts.ntiles == 0) return;
-  const size_t sm = tile_smem_bytes(K.ts, 1, sizeof(T));
-  if (K.ts.variant == 1) {
+  const size_t sm = dual_smem_bytes<T>(K.ts);
+  if (K.ts.groups > 0) {
+    halpern_dual_kernel<T, 2><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
+  } else if (K.ts.variant == 1) {
     halpern_dual_kernel<T, 1><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
   } else {
     halpern_dual_kernel<T, 0><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
@@ -1734,6 +1754,38 @@ __global__ void reciprocal_kernel(const double* a, double* out, int count) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
     out[k] = 1.0 / a[k];
   }
+}
+
+// Gather neighbours: rows i and i + 1, each of more than 32 nonzeros, whose k-th nonzeros lie
+// 1 to 4 columns apart at 7 of 8 sampled positions k (the rows of a 2-D variable array x[k][j]
+// summed over k: the candidates of the kind-3 row groups).
+__global__ void row_neighbours_kernel(int m, const int* __restrict__ ptr,
+                                      const int* __restrict__ idx, unsigned char* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    unsigned char a = 0;
+    if (i + 1 < m) {
+      const int b0 = ptr[i];
+      const int b1 = ptr[i + 1];
+      const int len = min(b1 - b0, ptr[i + 2] - b1);
+      if (len > 32) {
+        int hits = 0;
+        for (int q = 0; q < 8; ++q) {
+          const int k = static_cast<int>(static_cast<long long>(q) * len / 8);
+          const int d = idx[b1 + k] - idx[b0 + k];
+          hits += d != 0 && d >= -4 && d <= 4;
+        }
+        a = hits >= 7;
+      }
+    }
+    out[i] = a;
+  }
+}
+
+void launch_row_neighbours(int m, const int* ptr, const int* idx, unsigned char* out,
+                           cudaStream_t s) {
+  if (m <= 0) return;
+  row_neighbours_kernel<<<vec_grid(m) < 1024 ? vec_grid(m) : 1024, kBlock, 0, s>>>(m, ptr, idx,
+                                                                                  out);
 }
 
 void launch_reciprocals(const double* a, double* out, int count, cudaStream_t s) {

@@ -98,6 +98,8 @@ void launch_setup_norms(Ctl* ctl, const OpView<double>& K, const OpView<double>&
                         cudaStream_t s);
 // out[k] = 1 / a[k] for k < count.
 void launch_reciprocals(const double* a, double* out, int count, cudaStream_t s);
+void launch_row_neighbours(int m, const int* ptr, const int* idx, unsigned char* out,
+                           cudaStream_t s);
 void launch_ruiz_pass(Ctl* ctl, const OpView<double>& K, const OpView<double>& Kt, double* rs,
                       double* cs, double* rn, double* cn, const RedView& red, int grid_k,
                       int grid_t, cudaStream_t s);

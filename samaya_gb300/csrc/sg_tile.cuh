@@ -12,6 +12,14 @@
 //   kind 1 (a segment of a row longer than the tile capacity): the CTA sums the segment
 //     (strided, then the fixed block tree) into TileSet::seg_part; the last segment to arrive
 //     (counter) adds the row's segments in tile order and runs epi.long_row.
+//   kind 3 (dual step kernels, GROUPS): up to 32 consecutive rows whose k-th nonzeros lie in
+//     neighbouring columns (the demand rows of a transportation LP: the k-th nonzero of row j
+//     is column k D + j). Each warp stages 16 nonzero positions of every row in shared memory
+//     (row-wise, coalesced loads) and then lane l sums row l's staged positions, so one
+//     gather instruction reads neighbouring entries of the gathered vector instead of 32
+//     separate sectors. The warps take alternate 16-position blocks; their sums are added in
+//     warp order, the segments of a group in segment order (TileSet::grp_part, counter), and
+//     lane l runs epi.row for row l.
 // Every sum is taken in a fixed order, so results do not depend on scheduling and a re-run is
 // bit-identical.
 #pragma once
@@ -27,6 +35,16 @@ constexpr int kRedDoubles = kMaxSums * (kBlock / 32);
 // Dynamic shared memory of a tile kernel: the block-reduction scratch only.
 __host__ __device__ constexpr size_t tile_smem_size(int, size_t, int, int) {
   return sizeof(double) * kRedDoubles;
+}
+
+// Kind-3 staging: per warp kGroupRows x (kGroupPos + 1) indices and values (the extra column
+// keeps lane l's reads of row l conflict-free), then the warps' row sums.
+constexpr int kGroupStride = kGroupPos + 1;
+template <typename T, typename ACC>
+__host__ __device__ constexpr size_t group_smem_size() {
+  return sizeof(double) * kRedDoubles +
+         (kBlock / 32) * (kGroupRows * kGroupStride * (sizeof(int) + sizeof(T)) +
+                          kGroupRows * sizeof(ACC));
 }
 
 __device__ __forceinline__ double* smem_red() {
@@ -151,6 +169,99 @@ __device__ __forceinline__ void short_row_sum(int b, int e, const int* __restric
   }
 }
 
+// A kind-3 tile (see the file comment). Barriers: uniform over the CTA (every thread of the CTA
+// runs the same tile).
+template <typename T, typename ACC, typename Prod, typename Epi>
+__device__ __forceinline__ void group_tile(const TileSet& ts, const Tile& tile, int ti,
+                                           const int* __restrict__ ptr,
+                                           const int* __restrict__ idx,
+                                           const T* __restrict__ val, const Prod& prod, Epi& epi,
+                                           double* red) {
+  constexpr int kWarps = kBlock / 32;
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const int nr = tile.r1 - tile.r0;  // 1..32 rows
+  // Lane l: row l's start and length.
+  int my_row = 0, my_b = 0, my_len = 0;
+  if (lane < nr) {
+    my_row = tile_row(ts, tile.r0 + lane);
+    my_b = ldg(ptr + my_row);
+    my_len = ldg(ptr + my_row + 1) - my_b;
+  }
+  unsigned char* base = reinterpret_cast<unsigned char*>(red + kRedDoubles);
+  int* sidx = reinterpret_cast<int*>(base) + warp * kGroupRows * kGroupStride;
+  T* sval = reinterpret_cast<T*>(base + kWarps * kGroupRows * kGroupStride * sizeof(int)) +
+            warp * kGroupRows * kGroupStride;
+  ACC* wsum = reinterpret_cast<ACC*>(base + kWarps * kGroupRows * kGroupStride *
+                                                (sizeof(int) + sizeof(T)));
+  const int half = lane >> 4;  // staging: lanes 0-15 take row i, lanes 16-31 row i + 1
+  const int col = lane & 15;
+  ACC s = ACC(0);
+  for (int pb = tile.k0 + warp * kGroupPos; pb < tile.k1; pb += kWarps * kGroupPos) {
+    const int pos = pb + col;
+#pragma unroll
+    for (int i2 = 0; i2 < kGroupRows; i2 += 2) {
+      const int i = i2 + half;
+      const int bi = __shfl_sync(0xffffffffu, my_b, i);
+      const int li = __shfl_sync(0xffffffffu, my_len, i);
+      int j = 0;
+      T a = T(0);
+      if (i < nr && pos < li && pos < tile.k1) {
+        j = ldg(idx + bi + pos);
+        a = ldg(val + bi + pos);
+      }
+      sidx[i * kGroupStride + col] = j;
+      sval[i * kGroupStride + col] = a;
+    }
+    __syncwarp();
+    if (lane < nr) {
+#pragma unroll
+      for (int t = 0; t < kGroupPos; ++t) {
+        if (pb + t < my_len && pb + t < tile.k1) {
+          const ACC p[1] = {prod(0, sval[lane * kGroupStride + t], sidx[lane * kGroupStride + t])};
+          s += p[0];
+        }
+      }
+    }
+    __syncwarp();
+  }
+  wsum[warp * kGroupRows + lane] = s;
+  __syncthreads();
+  ACC tot = ACC(0);
+  if (warp == 0) {
+    tot = wsum[lane];
+#pragma unroll
+    for (int w = 1; w < kWarps; ++w) tot += wsum[w * kGroupRows + lane];
+  }
+  __syncthreads();
+  if (warp != 0) return;
+  if (tile.nseg == 1) {
+    if (lane < nr) {
+      const ACC out[1] = {tot};
+      epi.row(my_row, out);
+    }
+    return;
+  }
+  ts.grp_part[ti * kGroupRows + lane] = static_cast<double>(tot);
+  __threadfence();
+  __syncwarp();
+  unsigned prev = 0;
+  if (lane == 0) prev = atomicAdd(ts.lcount + tile.lrow, 1u);
+  prev = __shfl_sync(0xffffffffu, prev, 0);
+  if (prev != static_cast<unsigned>(tile.nseg - 1)) return;
+  // The last segment to arrive adds the group's segments in order.
+  __threadfence();
+  const int first = ti - tile.seg;
+  double acc = 0.0;
+  for (int g = 0; g < tile.nseg; ++g) acc += __ldcg(ts.grp_part + (first + g) * kGroupRows + lane);
+  if (lane == 0) ts.lcount[tile.lrow] = 0u;
+  if (lane < nr) {
+    const ACC out[1] = {static_cast<ACC>(acc)};
+    epi.row(my_row, out);
+  }
+}
+
 // Prod: ACC operator()(int v, T val, int col) const — the v-th product of a nonzero.
 // Epi: void row(int r, const ACC (&s)[NV]) for rows of kind-0 tiles (lane 0 of the row's team),
 //      void long_row(int lrow, int r, const ACC (&s)[NV]) for a split row (thread 0 of the CTA
@@ -158,7 +269,7 @@ __device__ __forceinline__ void short_row_sum(int b, int e, const int* __restric
 // MAXRED: each row's products are combined by max instead of + (norm statistics).
 // WIDE: unroll the warp-per-row loop 8 deep (4 otherwise) and the segment loop 4 deep (2).
 template <typename T, typename ACC, int NV, typename Prod, typename Epi, bool MAXRED = false,
-          bool WIDE = false>
+          bool WIDE = false, bool GROUPS = false>
 __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restrict__ ptr,
                                           const int* __restrict__ idx,
                                           const T* __restrict__ val, const Prod& prod, Epi& epi) {
@@ -167,6 +278,13 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
   double* red = smem_red();
   for (int ti = blockIdx.x; ti < ts.ntiles; ti += gridDim.x) {
     const Tile tile = ts.tiles[ti];
+    if constexpr (GROUPS) {
+      static_assert(NV == 1 && !MAXRED, "kind-3 tiles carry one plain sum per row");
+      if (tile.kind == 3) {
+        group_tile<T, ACC>(ts, tile, ti, ptr, idx, val, prod, epi, red);
+        continue;
+      }
+    }
     if (tile.kind == 0) {
       // One thread per row; a row longer than a warp is taken over by its whole warp (ballot
       // queue), so skewed row lengths inside a tile cost no serial tail.

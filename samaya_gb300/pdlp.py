@@ -46,6 +46,7 @@ class PdlpOptions:
     tile_split: int = 0
     artificial_restart: float = 0.0
     keep_inert_rows: bool = False
+    row_groups: int = 0
 
     def to_c(self) -> _native.Opts:
         o = _native.Opts()
@@ -62,6 +63,7 @@ class PdlpOptions:
         o.tile_split = int(self.tile_split)
         o.artificial_restart = float(self.artificial_restart)
         o.keep_inert_rows = 1 if self.keep_inert_rows else 0
+        o.row_groups = int(self.row_groups)
         return o
 
 
@@ -180,13 +182,14 @@ class PdlpSolver:
             out[name] = (v[0].value, v[1].value, v[2].value, v[3].value, v[4].value)
         return out
 
-    def step_rows(self) -> tuple[int, int]:
-        """(rows of A the dual steps run over, their tiles): m unless inert rows (empty, a
-        logical with no cost and 0 within its bounds) are left out."""
-        rows, tiles = ctypes.c_int(0), ctypes.c_int(0)
-        _native.check(self._lib.sg_pdlp_step_rows(self._h, ctypes.byref(rows),
-                                                  ctypes.byref(tiles)), "sg_pdlp_step_rows")
-        return rows.value, tiles.value
+    def step_rows(self) -> tuple[int, int, int]:
+        """(rows of A the dual steps run over, their tiles, the row-group tiles among them):
+        m rows unless inert rows (empty, a logical with no cost and 0 within its bounds) are
+        left out."""
+        v = [ctypes.c_int(0) for _ in range(3)]
+        _native.check(self._lib.sg_pdlp_step_rows(self._h, *[ctypes.byref(x) for x in v]),
+                      "sg_pdlp_step_rows")
+        return v[0].value, v[1].value, v[2].value
 
     def solve(self, x_out: np.ndarray | None = None, y_out: np.ndarray | None = None,
               download: bool = True) -> PdlpResult:
@@ -290,6 +293,14 @@ class PdhgDevice:
         else:
             o = options.to_c()
             _native.check(self._lib.sg_pdlp_create(*args, ctypes.byref(o)), "sg_pdlp_create")
+
+    def step_rows(self) -> tuple[int, int, int]:
+        """As ``PdlpSolver.step_rows``: the rows, tiles and row-group tiles of the dual
+        steps."""
+        v = [ctypes.c_int(0) for _ in range(3)]
+        _native.check(self._lib.sg_pdlp_step_rows(self._h, *[ctypes.byref(x) for x in v]),
+                      "sg_pdlp_step_rows")
+        return v[0].value, v[1].value, v[2].value
 
     def set_original(self, col_scale, row_scale, cost, lower, upper):
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in

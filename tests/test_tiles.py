@@ -103,3 +103,113 @@ def test_build_tiles_argument_checks():
                               ctypes.byref(n), ctypes.byref(nl)) == -1
     assert lib.sg_build_tiles(2, ptr.ctypes.data_as(p32), 256, 256, 128, 0, None, 0,
                               ctypes.byref(n), ctypes.byref(nl)) == -5 and n.value == 1
+
+
+def _group_tiles(ptr, neighbours, cap, cap_rows, warp_min, split):
+    lib = _native.load(build_if_missing=True)
+    rows = len(ptr) - 1
+    ptr = np.ascontiguousarray(ptr, dtype=np.int32)
+    nb = np.ascontiguousarray(neighbours, dtype=np.uint8)
+    ntiles, nlong = ctypes.c_int(0), ctypes.c_int(0)
+    p32 = ctypes.POINTER(ctypes.c_int32)
+    p8 = ctypes.POINTER(ctypes.c_uint8)
+    rc = lib.sg_build_group_tiles(rows, ptr.ctypes.data_as(p32), nb.ctypes.data_as(p8), cap,
+                                  cap_rows, warp_min, split, None, 0, ctypes.byref(ntiles),
+                                  ctypes.byref(nlong))
+    assert rc in (0, -5)
+    out = np.zeros(max(ntiles.value, 1) * 9, dtype=np.int32)
+    rc = lib.sg_build_group_tiles(rows, ptr.ctypes.data_as(p32), nb.ctypes.data_as(p8), cap,
+                                  cap_rows, warp_min, split, out.ctypes.data_as(p32),
+                                  ntiles.value, ctypes.byref(ntiles), ctypes.byref(nlong))
+    assert rc == 0
+    return out[:ntiles.value * 9].reshape(-1, 9), nlong.value
+
+
+@pytest.mark.parametrize("cap", [2048, 4096, 8192])
+def test_row_groups_cover_runs_of_neighbour_rows(cap):
+    """sg_build_group_tiles (the dual steps' partition with row groups): every row once; a
+    kind-3 tile holds 8-32 consecutive rows longer than warp_min, each a neighbour of the next,
+    its segments cover positions [0, longest row) in steps of the group segment length; the
+    other rows are partitioned as sg_build_tiles would (kinds 0-2), and the counters of split
+    rows and multi-segment groups are numbered in order."""
+    rng = np.random.default_rng(cap)
+    rows = 4000
+    lengths = np.where(rng.random(rows) < 0.5, rng.integers(0, 100, size=rows),
+                       rng.integers(129, 3000, size=rows))
+    # Runs of neighbour rows of various lengths (some shorter than 8, some longer than 32).
+    neighbours = np.zeros(rows, dtype=np.uint8)
+    r = 0
+    while r < rows:
+        run = int(rng.integers(1, 70))
+        if rng.random() < 0.6:
+            end = min(rows, r + run)
+            neighbours[r:end - 1] = 1
+            # Mostly long rows inside a run, a few short ones breaking it.
+            lengths[r:end] = np.where(rng.random(end - r) < 0.95,
+                                      rng.integers(129, 3000, size=end - r), 50)
+        r += run
+    ptr = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    warp_min = 128
+    tiles, nlong = _group_tiles(ptr, neighbours, cap, 1024, warp_min, 0)
+    gp = max(128, (cap // 32) // 128 * 128)
+    long_len = max(cap, warp_min)
+    covered = np.zeros(int(ptr[-1]), dtype=np.int32)
+    rows_seen = np.zeros(rows, dtype=np.int32)
+    counters = []
+    groups = 0
+    i = 0
+    while i < len(tiles):
+        r0, r1, k0, k1, kind, team, seg, nseg, lrow = (int(v) for v in tiles[i])
+        if kind == 3:
+            g = r1 - r0
+            assert 8 <= g <= 32
+            assert np.all(lengths[r0:r1] > warp_min) and np.all(neighbours[r0:r1 - 1] == 1)
+            maxlen = int(lengths[r0:r1].max())
+            assert nseg == (maxlen + gp - 1) // gp
+            for s in range(nseg):
+                t = tiles[i + s]
+                assert t[4] == 3 and t[0] == r0 and t[1] == r1 and t[6] == s and t[7] == nseg
+                assert t[2] == s * gp and t[3] == min(maxlen, (s + 1) * gp)
+                for q in range(r0, r1):
+                    a, b = ptr[q] + t[2], min(ptr[q + 1], ptr[q] + t[3])
+                    if b > a:
+                        covered[a:b] += 1
+            if nseg > 1:
+                counters.append(lrow)
+            rows_seen[r0:r1] += 1
+            groups += 1
+            i += nseg
+        elif kind == 1:
+            assert lengths[r0] > long_len
+            for s in range(nseg):
+                t = tiles[i + s]
+                covered[t[2]:t[3]] += 1
+            counters.append(lrow)
+            rows_seen[r0] += 1
+            i += nseg
+        else:
+            assert kind in (0, 2) and k0 == ptr[r0] and k1 == ptr[r1]
+            if kind == 2:
+                # A row group would have started inside a kind-2 tile: never.
+                for q in range(r0 + 1, r1):
+                    run = 1
+                    while run < 32 and q + run < rows and neighbours[q + run - 1] and \
+                            lengths[q + run] > warp_min:
+                        run += 1
+                    assert run < 8 or lengths[q] <= warp_min
+            covered[k0:k1] += 1
+            rows_seen[r0:r1] += 1
+            i += 1
+    assert np.all(rows_seen == 1)
+    assert np.all(covered == 1)
+    assert counters == list(range(nlong))
+    assert groups > 10
+
+
+def test_group_tiles_need_the_neighbours():
+    lib = _native.load(build_if_missing=True)
+    ptr = np.array([0, 3, 5], dtype=np.int32)
+    n, nl = ctypes.c_int(0), ctypes.c_int(0)
+    p32 = ctypes.POINTER(ctypes.c_int32)
+    assert lib.sg_build_group_tiles(2, ptr.ctypes.data_as(p32), None, 256, 256, 128, 0, None, 0,
+                                    ctypes.byref(n), ctypes.byref(nl)) == -1
