@@ -321,8 +321,9 @@ def run_batch(args):
         cfg = {"workload": "256 facility-location node relaxations (100 x 400) sharing A",
                "instances": 256, "nnz": int(lp.nnz)}
     out = {}
-    algs = (("reference", sg.REFERENCE),) if args.algorithm == "reference" else (
-        ("enhanced", sg.ENHANCED),)
+    # The workload's algorithm and the Halpern iteration beside it.
+    names = {"reference": sg.REFERENCE, "enhanced": sg.ENHANCED, "halpern": sg.HALPERN}
+    algs = tuple((a, names[a]) for a in dict.fromkeys((args.algorithm, "halpern")))
     with Clocks(0) as clk:
         for name, prec in (("fp64", sg.FP64), ("fp32", sg.FP32_REFINED)):
             for alg_name, alg in algs:

@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(kBT) batch_setup_kernel(BatchView b) {
   }
   // Preconditioning.
   if (m > 0 && n > 0) {
-    if (b.algorithm == 1) {
+    if (b.algorithm >= 1) {
       for (int pass = 0; pass < 11; ++pass) {
         const bool ruiz = pass < 10;
         struct Abs {
@@ -411,7 +411,8 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
   bsums<3>(nrm, sh);
   const double c_norm = sqrt(nrm[0]);
   double omega = 1.0;
-  if (b.algorithm == 1) {
+  const bool halpern = b.algorithm == 2;
+  if (b.algorithm >= 1) {
     const double cn = sqrt(nrm[1]), bn = sqrt(nrm[2]);
     omega = (cn > 1e-10 && bn > 1e-10) ? cn / bn : 1.0;
   }
@@ -434,6 +435,55 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
     const double alpha = 1.0 / static_cast<double>(k_since + 1);
     const T ta = static_cast<T>(alpha), tb = static_cast<T>(1.0 - alpha);
     const T tsig = static_cast<T>(sigma), ttau = static_cast<T>(tau);
+    if (halpern) {
+      // The reflected Halpern iteration z+ = N + w (z0 - N), N = 2 T(z) - z, w = 1 / (k + 2)
+      // (k: iterations since the restart), T the PDHG map in primal-first order, as the
+      // single-LP engine's halpern_primal / halpern_dual kernels compute it; T(z) lands in
+      // Verg / Yerg (the point the evaluation, the restarts and the answer use).
+      const T tw = static_cast<T>(1.0 / static_cast<double>(k_since + 2));
+      {
+        struct G {
+          const T* y;
+          __device__ T operator()(T a, int i) const { return a * y[i]; }
+        } gy{Y(p)};
+        const T* x = V(p);
+        T* xn = V(p ^ 1);
+        auto f = [&](int j, T s) {
+          const T xo = x[j];
+          const T xh = fmin(fmax(xo - ttau * (ce[j] + s), le[j]), ue[j]);
+          const T refl = xh + (xh - xo);
+          Verg[j] = xh;
+          Vbar[j] = refl;
+          xn[j] = refl + tw * (Vrst[j] - refl);
+        };
+        block_rows<false>(n, tp, ti, tv, gy, f);
+      }
+      __syncthreads();
+      {
+        struct G {
+          const T* x;
+          __device__ T operator()(T a, int j) const { return a * x[j]; }
+        } gx{Vbar};
+        const T* yv = Y(p);
+        T* yn = Y(p ^ 1);
+        const T* vr = V(p) + n;
+        T* vrn = V(p ^ 1) + n;
+        auto f = [&](int i, T s) {
+          const T y = yv[i];
+          const T r = vr[i];
+          const T rh = fmin(fmax(r - ttau * (ce[n + i] - y), le[n + i]), ue[n + i]);
+          const T rrefl = rh + (rh - r);
+          const T yh = y + tsig * (s - rrefl);
+          Yerg[i] = yh;
+          Verg[n + i] = rh;
+          const T yrefl = yh + (yh - y);
+          yn[i] = yrefl + tw * (Yrst[i] - yrefl);
+          vrn[i] = rrefl + tw * (Vrst[n + i] - rrefl);
+        };
+        block_rows<false>(m, kp, ki, kv, gx, f);
+      }
+      __syncthreads();
+    } else {
     // Dual step (rows of A_eq) with the logicals' primal update.
     {
       // Products and sums in the storage type.
@@ -480,6 +530,7 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
       block_rows<false>(n, tp, ti, tv, gy, f);
     }
     __syncthreads();
+    }
     ++t;
     ++k_since;
     if (t % 64 != 0 && t != max_iter) continue;
@@ -537,7 +588,13 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
       block_rows<false>(n, tp, ti, tv, gy, fc);
     };
     double ec[9], ea[9];
-    eval_one(V(cur), Y(cur), ec);
+    // Halpern: only T(z) is measured (the Halpern iterate itself can leave the bounds).
+    if (halpern) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) ec[q] = 0.0;
+    } else {
+      eval_one(V(cur), Y(cur), ec);
+    }
     eval_one(Verg, Yerg, ea);
     // a: the current iterate's 7 sums, the average's 7, then the distances (v, y) of each.
     double a[18];
@@ -554,7 +611,7 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
     const Meas mc = finish7(a, mi.a_norm_max_col, mi.at_norm_max_row, c_norm, m);
     const Meas ma = finish7(a + 7, mi.a_norm_max_col, mi.at_norm_max_row, c_norm, m);
     const double tol = b.tol;
-    if (mc.rp < tol && mc.rd < tol && fabs(mc.rg) < tol) {
+    if (!halpern && mc.rp < tol && mc.rd < tol && fabs(mc.rg) < tol) {
       status = kOptimal;
       final_meas = mc;
       break;
@@ -565,14 +622,14 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
       final_meas = ma;
       break;
     }
-    final_meas = mc;
-    // Restart (pdlp.cpp:1069-1131).
+    final_meas = halpern ? ma : mc;
+    // Restart (pdlp.cpp:1069-1131); the Halpern iteration restarts to T(z).
     const double kc = kkt_w(omega, mc), ka = kkt_w(omega, ma);
-    const bool to_avg = ka < kc;
-    const double cand = fmin(kc, ka);
+    const bool to_avg = halpern || ka < kc;
+    const double cand = halpern ? ka : fmin(kc, ka);
     if (!(kar < INFINITY)) kar = cand;
     const bool restart = cand <= 0.2 * kar || (cand <= 0.8 * kar && cand > kprev) ||
-                         static_cast<double>(k_since) >= 0.36 * static_cast<double>(t);
+                         static_cast<double>(k_since) >= b.art_frac * static_cast<double>(t);
     kprev = cand;
     if (restart) {
       const double dx = sqrt(a[to_avg ? 16 : 14]);
@@ -613,7 +670,8 @@ __device__ void solve_instance(const BatchView& b, int inst, double* sh) {
       }
     }
   }
-  // Answer in the LpProblem's space.
+  // Answer in the LpProblem's space (Halpern: T(z), within the bounds).
+  if (halpern) result_avg = 1;
   const int cur = static_cast<int>(t & 1);
   const T* vv = result_avg ? Verg : V(cur);
   const T* yy = result_avg ? Yerg : Y(cur);

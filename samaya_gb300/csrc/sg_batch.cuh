@@ -71,8 +71,9 @@ struct BatchView {
   long long max_iter;
   double tol;
   const unsigned long long* deadline;  // device word: %globaltimer deadline, 0 = none
-  int algorithm;
+  int algorithm;     // 0 reference, 1 enhanced, 2 Halpern (enhanced preconditioning)
   int fp32;
+  double art_frac;   // forced restart once the iterations since the last reach this fraction
 };
 
 // Unrolled PDHG of every instance (the differentiable layer's forward and adjoint).

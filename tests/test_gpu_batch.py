@@ -119,3 +119,46 @@ def test_batch_shared_matrix_node_relaxations(engine, oracle):
         verified += int(ok)
         reports.append(rep)
     assert verified >= 0.8 * len(res), reports
+
+
+def test_batch_halpern_matches_the_oracle_and_the_node_optima(engine, oracle):
+    """The reflected Halpern iteration in the batched engine (T(z) measured, restarted to and
+    returned): uneven random LPs at 1e-7 against the oracle's objectives (1e-5 relative, FP64;
+    1e-3 in FP32 storage at 1e-4), the facility-location node relaxations at 1e-8 against their
+    HiGHS optima (1e-6 relative), and a re-run repeats every answer's bits."""
+    import dataclasses
+
+    from conftest import highs_objective
+    from samaya_gb300.batch import BatchSolver
+    from samaya_gb300.generators import (facility_location_lp, facility_node_bounds,
+                                         random_sparse_lp)
+    from samaya_gb300.problem import make_problem, model_solution
+    rng = np.random.default_rng(6)
+    probs = []
+    for k in range(6):
+        m = int(rng.integers(60, 300))
+        n = int(np.ceil(m * rng.uniform(2, 3)))
+        probs.append(make_problem(random_sparse_lp(m, n, seed=200 + k))[0])
+    refs = [_oracle_objective(lp, 1e-8) for lp in probs]
+    for prec, tol, bar in ((engine.FP64, 1e-7, 1e-5), (engine.FP32_REFINED, 1e-4, 1e-3)):
+        s = BatchSolver.from_problems(probs, engine.PdlpOptions(
+            tol=tol, algorithm=engine.HALPERN, precision=prec))
+        res = s.solve()
+        again = s.solve()
+        s.close()
+        for lp, r, r2, (st, ref) in zip(probs, res, again, refs):
+            assert st == oracle.OPTIMAL and r.status == engine.OPTIMAL
+            a = float(np.dot(lp.cost, r.x))
+            assert abs(a - ref) <= bar * (1 + abs(ref)), (prec, a, ref)
+            assert r.iterations == r2.iterations and np.array_equal(r.x, r2.x)
+    model = facility_location_lp(20, 60, seed=3)
+    lp, sc = make_problem(model)
+    node_bounds = facility_node_bounds(model, 20, 8, seed=4)
+    res = BatchSolver.shared(lp, _node_problems(lp, sc, model, node_bounds),
+                             engine.PdlpOptions(tol=1e-8, algorithm=engine.HALPERN)).solve()
+    for (mlo, mup), r in zip(node_bounds, res):
+        node_model = dataclasses.replace(model, col_lower=mlo, col_upper=mup)
+        st, ref = highs_objective(node_model)
+        assert st == 0 and r.status == engine.OPTIMAL, (st, r.status)
+        _, _, _, obj = model_solution(node_model, sc, r.x, r.y)
+        assert abs(obj - ref) <= 1e-6 * (1 + abs(ref)), (obj, ref)
