@@ -33,7 +33,10 @@ sys.path.insert(0, ROOT)
 METRIC = "PDLP time-to-1e-8 KKT (mixed vs FP64 GPU)"
 TOL = 1e-8
 CPU_CAP_S = 20.0
-SWITCH_TOL = 1e-6
+# The FP32 phase's tolerance: the latest switch that still leaves FP32 progressing on the
+# transportation LP (seeds 0-3: 97-110 ms at 3e-7 against 116-128 ms at 1e-6; at 1e-7 the FP32
+# phase reaches its precision floor and the stall test ends it late, 286 ms).
+SWITCH_TOL = 3e-7
 ALGORITHM_NAMES = {
     "enhanced": "enhanced (inf-norm Ruiz + Pock-Chambolle, primal weight |c|/|b|)",
     "halpern": "halpern (enhanced scaling, reflected Halpern PDHG)",

@@ -744,24 +744,36 @@ double Engine::time_step_kernel(bool dual, int reps) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  // The step kernels the solves run (classic or Halpern).
+  const bool halpern = opt_.algorithm == 2;
   auto launch = [&](int j) {
+    const int gk = std::max(1, std::min(K_.step_tiles(), 65535));
+    const int gt = std::max(1, std::min(Kt_.ntiles, 65535));
     if (fp32_) {
       IterView<float> it = iter_view(it32_);
       if (dual) {
-        launch_dual_step(c, K_.step32(), it, j, std::max(1, std::min(K_.step_tiles(), 65535)),
-                         stream_);
+        if (halpern) {
+          launch_halpern_dual(c, K_.step32(), it, j, gk, stream_);
+        } else {
+          launch_dual_step(c, K_.step32(), it, j, gk, stream_);
+        }
+      } else if (halpern) {
+        launch_halpern_primal(c, Kt_.view32(), it, j, gt, stream_);
       } else {
-        launch_primal_step(c, Kt_.view32(), it, j, std::max(1, std::min(Kt_.ntiles, 65535)),
-                           stream_);
+        launch_primal_step(c, Kt_.view32(), it, j, gt, stream_);
       }
     } else {
       IterView<double> it = iter_view(it64_);
       if (dual) {
-        launch_dual_step(c, K_.step64(), it, j, std::max(1, std::min(K_.step_tiles(), 65535)),
-                         stream_);
+        if (halpern) {
+          launch_halpern_dual(c, K_.step64(), it, j, gk, stream_);
+        } else {
+          launch_dual_step(c, K_.step64(), it, j, gk, stream_);
+        }
+      } else if (halpern) {
+        launch_halpern_primal(c, Kt_.view64(), it, j, gt, stream_);
       } else {
-        launch_primal_step(c, Kt_.view64(), it, j, std::max(1, std::min(Kt_.ntiles, 65535)),
-                           stream_);
+        launch_primal_step(c, Kt_.view64(), it, j, gt, stream_);
       }
     }
   };
@@ -1137,7 +1149,7 @@ int enqueue_chunk(Ctl* ctl, const OpView<T>& Ks, const OpView<T>& K, const OpVie
       launch_primal_step(ctl, Kt, it, j, gst, s);
     }
   }
-  launch_eval(ctl, K, Kt, it, ev, red, gk, gt, -1, s);
+  launch_eval(ctl, K, Kt, it, ev, red, gk, gt, -1, s, halpern);
   launch_decide_a(ctl, s);
   launch_detect(ctl, K, Kt, it, ev, red, scratch_n, nullptr, gk, gt, s);
   launch_decide_b(ctl, s);
@@ -1317,10 +1329,12 @@ int Engine::finish_fp64(SolveInfo* info, double t0, long long iterations_before,
   info->step_size = c.eta;
   info->operator_norm = c.op_norm;
   if (c.done == 0 || c.status == kTimeLimit || c.status == kIterationLimit) {
-    // The relative residuals of the last evaluation's current iterate.
-    info->rel_primal = c.meas[0][0];
-    info->rel_dual = c.meas[0][1];
-    info->rel_gap = c.meas[0][2];
+    // The relative residuals of the last evaluation's current iterate (Halpern: of T(z), the
+    // only point it measures and the answer).
+    const int slot = c.halpern ? 1 : 0;
+    info->rel_primal = c.meas[slot][0];
+    info->rel_dual = c.meas[slot][1];
+    info->rel_gap = c.meas[slot][2];
   }
   // Answer.
   IterView<double> it = iter_view(it64_);
@@ -1934,7 +1948,7 @@ int time_steps(Ctl* c, const OpView<T>& Ks, const OpView<T>& K, const OpView<T>&
   cudaEventRecord(e[1], s);
   for (int r = 0; r < reps; ++r) primal(r & 1);
   cudaEventRecord(e[2], s);
-  for (int r = 0; r < reps; ++r) launch_eval(c, K, Kt, it, ev, red, gk, gt, 0, s);
+  for (int r = 0; r < reps; ++r) launch_eval(c, K, Kt, it, ev, red, gk, gt, 0, s, halpern);
   cudaEventRecord(e[3], s);
   const cudaError_t err = cudaEventSynchronize(e[3]);
   float a = 0, b = 0, d = 0;

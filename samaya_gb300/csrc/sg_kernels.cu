@@ -476,9 +476,10 @@ __global__ void __launch_bounds__(kBlock, step_min_blocks<T>(VAR, true)) halpern
 // ------------------------------------------------------------------------------------------
 // Evaluation (pdhg_core.cu:102-144 / pdlp.cpp:411-488): the seven sums of the current and the
 // average iterate in the space before equilibration, plus the restart distances, from one
-// pass over each operator (both iterates share the matrix read).
+// pass over each operator (both iterates share the matrix read). W0 = 1 measures the second
+// slot alone (the Halpern solves decide on T(z) only; the current iterate's sums stay 0).
 
-template <typename T>
+template <typename T, int W0 = 0>
 struct EvalRowEpi {
   // rows of K: logicals r and duals y
   const T* vr[2];
@@ -489,7 +490,8 @@ struct EvalRowEpi {
   int n;
   double acc[kEvalSums];
   double* long_terms;
-  __device__ __forceinline__ void terms(int i, const double (&s)[2], double (&a)[kEvalSums]) {
+  __device__ __forceinline__ void terms(int i, const double (&s)[2 - W0],
+                                        double (&a)[kEvalSums]) {
     const double rs = ev.rs[i];
     const double irs = ev.inv_rs[i];
     const double c = ev.cost[n + i];
@@ -497,13 +499,13 @@ struct EvalRowEpi {
     const double up = ev.upper[n + i];
     const double q = ev.rhs != nullptr ? ev.rhs[i] : 0.0;
 #pragma unroll
-    for (int w = 0; w < 2; ++w) {
+    for (int w = W0; w < 2; ++w) {
       const double vrv = static_cast<double>(vr[w][i]);
       const double yv = static_cast<double>(y[w][i]);
       const double value = vrv * irs;
       const double yo = yv * rs;
       const double g = c - yo;
-      const double e = s[w] * irs - value - q;
+      const double e = s[w - W0] * irs - value - q;
       a[w * 7 + 0] += e * e;
       a[w * 7 + 5] += value * value;
       a[w * 7 + 6] += yo * yo;
@@ -520,8 +522,8 @@ struct EvalRowEpi {
       a[15 + 2 * w] += dy * dy;
     }
   }
-  __device__ __forceinline__ void row(int i, const double (&s)[2]) { terms(i, s, acc); }
-  __device__ __forceinline__ void long_row(int lrow, int i, const double (&s)[2]) {
+  __device__ __forceinline__ void row(int i, const double (&s)[2 - W0]) { terms(i, s, acc); }
+  __device__ __forceinline__ void long_row(int lrow, int i, const double (&s)[2 - W0]) {
     double a[kEvalSums];
 #pragma unroll
     for (int q = 0; q < kEvalSums; ++q) a[q] = 0.0;
@@ -531,7 +533,7 @@ struct EvalRowEpi {
   }
 };
 
-template <typename T>
+template <typename T, int W0 = 0>
 struct EvalColEpi {
   // rows of K': structurals x
   const T* x[2];
@@ -540,17 +542,18 @@ struct EvalColEpi {
   int m;
   double acc[kEvalSums];
   double* long_terms;
-  __device__ __forceinline__ void terms(int j, const double (&s)[2], double (&a)[kEvalSums]) {
+  __device__ __forceinline__ void terms(int j, const double (&s)[2 - W0],
+                                        double (&a)[kEvalSums]) {
     const double cs = ev.cs[j];
     const double ics = ev.inv_cs[j];
     const double c = ev.cost[j];
     const double lo = ev.lower[j];
     const double up = ev.upper[j];
 #pragma unroll
-    for (int w = 0; w < 2; ++w) {
+    for (int w = W0; w < 2; ++w) {
       const double xv = static_cast<double>(x[w][j]);
       const double value = xv * cs;
-      const double g = c + (m > 0 ? s[w] * ics : 0.0);
+      const double g = c + (m > 0 ? s[w - W0] * ics : 0.0);
       a[w * 7 + 4] += value * value;
       a[w * 7 + 2] += c * value;
       const double lam = bound_part(g, lo, up);
@@ -561,8 +564,8 @@ struct EvalColEpi {
       a[14 + 2 * w] += dv * dv;
     }
   }
-  __device__ __forceinline__ void row(int j, const double (&s)[2]) { terms(j, s, acc); }
-  __device__ __forceinline__ void long_row(int lrow, int j, const double (&s)[2]) {
+  __device__ __forceinline__ void row(int j, const double (&s)[2 - W0]) { terms(j, s, acc); }
+  __device__ __forceinline__ void long_row(int lrow, int j, const double (&s)[2 - W0]) {
     double a[kEvalSums];
 #pragma unroll
     for (int q = 0; q < kEvalSums; ++q) a[q] = 0.0;
@@ -587,13 +590,13 @@ __device__ __forceinline__ int eval_parity(const Ctl* ctl, int fixed_parity) {
   return static_cast<int>((ctl->t + steps) & 1);
 }
 
-template <typename T>
+template <typename T, int W0>
 __global__ void __launch_bounds__(kBlock) eval_rows_kernel(Ctl* ctl, OpView<T> K, IterView<T> it,
                                                            EvalView ev, RedView red,
                                                            int fixed_parity) {
   if (fixed_parity < 0 && ctl->done) return;
   const int cur = eval_parity(ctl, fixed_parity);
-  EvalRowEpi<T> epi;
+  EvalRowEpi<T, W0> epi;
   const int n = it.n;
   epi.vr[0] = it.v(cur) + n;
   epi.vr[1] = it.Verg + n;
@@ -606,20 +609,25 @@ __global__ void __launch_bounds__(kBlock) eval_rows_kernel(Ctl* ctl, OpView<T> K
   epi.long_terms = red.long_terms;
 #pragma unroll
   for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0;
-  Gather2<T> g{it.v(cur), it.Verg};
-  run_tiles<T, double, 2>(K.ts, K.ptr, K.idx, K.val, g, epi);
+  if constexpr (W0 == 0) {
+    Gather2<T> g{it.v(cur), it.Verg};
+    run_tiles<T, double, 2>(K.ts, K.ptr, K.idx, K.val, g, epi);
+  } else {
+    Gather1<T, double> g{it.Verg};
+    run_tiles<T, double, 1>(K.ts, K.ptr, K.idx, K.val, g, epi);
+  }
   EvalFin fin{ctl->eval_r};
   grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, smem_red(), fin, red.long_terms,
                          K.ts.nlong);
 }
 
-template <typename T>
+template <typename T, int W0>
 __global__ void __launch_bounds__(kBlock) eval_cols_kernel(Ctl* ctl, OpView<T> Kt, IterView<T> it,
                                                            EvalView ev, RedView red,
                                                            int fixed_parity) {
   if (fixed_parity < 0 && ctl->done) return;
   const int cur = eval_parity(ctl, fixed_parity);
-  EvalColEpi<T> epi;
+  EvalColEpi<T, W0> epi;
   epi.x[0] = it.v(cur);
   epi.x[1] = it.Verg;
   epi.x_rst = it.Vrst;
@@ -628,8 +636,13 @@ __global__ void __launch_bounds__(kBlock) eval_cols_kernel(Ctl* ctl, OpView<T> K
   epi.long_terms = red.long_terms;
 #pragma unroll
   for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0;
-  Gather2<T> g{it.y(cur), it.Yerg};
-  run_tiles<T, double, 2>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
+  if constexpr (W0 == 0) {
+    Gather2<T> g{it.y(cur), it.Yerg};
+    run_tiles<T, double, 2>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
+  } else {
+    Gather1<T, double> g{it.Yerg};
+    run_tiles<T, double, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
+  }
   EvalFin fin{ctl->eval_c};
   grid_reduce<kEvalSums>(epi.acc, red.partial, red.counter, smem_red(), fin, red.long_terms,
                          Kt.ts.nlong);
@@ -655,6 +668,7 @@ struct Gather2f {
   }
 };
 
+template <int W0 = 0>
 struct EvalRowEpi32 {
   const float* vr[2];
   const float* y[2];
@@ -666,17 +680,17 @@ struct EvalRowEpi32 {
   const float* q;
   float acc[kEvalSums];
   double* long_terms;
-  __device__ __forceinline__ void terms(int i, const float (&s)[2], float (&a)[kEvalSums]) {
+  __device__ __forceinline__ void terms(int i, const float (&s)[2 - W0], float (&a)[kEvalSums]) {
     const float c_i = c[i];
     const float lo = l[i];
     const float up = u[i];
     const float q_i = q != nullptr ? q[i] : 0.0f;
 #pragma unroll
-    for (int w = 0; w < 2; ++w) {
+    for (int w = W0; w < 2; ++w) {
       const float value = vr[w][i];
       const float yv = y[w][i];
       const float g = c_i - yv;
-      const float e = s[w] - value - q_i;
+      const float e = s[w - W0] - value - q_i;
       a[w * 7 + 0] += e * e;
       a[w * 7 + 5] += value * value;
       a[w * 7 + 6] += yv * yv;
@@ -692,8 +706,8 @@ struct EvalRowEpi32 {
       a[15 + 2 * w] += dy * dy;
     }
   }
-  __device__ __forceinline__ void row(int i, const float (&s)[2]) { terms(i, s, acc); }
-  __device__ __forceinline__ void long_row(int lrow, int i, const float (&s)[2]) {
+  __device__ __forceinline__ void row(int i, const float (&s)[2 - W0]) { terms(i, s, acc); }
+  __device__ __forceinline__ void long_row(int lrow, int i, const float (&s)[2 - W0]) {
     float a[kEvalSums];
 #pragma unroll
     for (int q2 = 0; q2 < kEvalSums; ++q2) a[q2] = 0.0f;
@@ -703,6 +717,7 @@ struct EvalRowEpi32 {
   }
 };
 
+template <int W0 = 0>
 struct EvalColEpi32 {
   const float* x[2];
   const float* x_rst;
@@ -712,14 +727,14 @@ struct EvalColEpi32 {
   int m;
   float acc[kEvalSums];
   double* long_terms;
-  __device__ __forceinline__ void terms(int j, const float (&s)[2], float (&a)[kEvalSums]) {
+  __device__ __forceinline__ void terms(int j, const float (&s)[2 - W0], float (&a)[kEvalSums]) {
     const float c_j = c[j];
     const float lo = l[j];
     const float up = u[j];
 #pragma unroll
-    for (int w = 0; w < 2; ++w) {
+    for (int w = W0; w < 2; ++w) {
       const float value = x[w][j];
-      const float g = c_j + (m > 0 ? s[w] : 0.0f);
+      const float g = c_j + (m > 0 ? s[w - W0] : 0.0f);
       a[w * 7 + 4] += value * value;
       a[w * 7 + 2] += c_j * value;
       const float lam = bound_part32(g, lo, up);
@@ -730,8 +745,8 @@ struct EvalColEpi32 {
       a[14 + 2 * w] += dv * dv;
     }
   }
-  __device__ __forceinline__ void row(int j, const float (&s)[2]) { terms(j, s, acc); }
-  __device__ __forceinline__ void long_row(int lrow, int j, const float (&s)[2]) {
+  __device__ __forceinline__ void row(int j, const float (&s)[2 - W0]) { terms(j, s, acc); }
+  __device__ __forceinline__ void long_row(int lrow, int j, const float (&s)[2 - W0]) {
     float a[kEvalSums];
 #pragma unroll
     for (int q2 = 0; q2 < kEvalSums; ++q2) a[q2] = 0.0f;
@@ -741,13 +756,14 @@ struct EvalColEpi32 {
   }
 };
 
+template <int W0>
 __global__ void __launch_bounds__(kBlock) eval_rows32_kernel(Ctl* ctl, OpView<float> K,
                                                              IterView<float> it, RedView red,
                                                              int fixed_parity) {
   if (fixed_parity < 0 && ctl->done) return;
   const int cur = eval_parity(ctl, fixed_parity);
   const int n = it.n;
-  EvalRowEpi32 epi;
+  EvalRowEpi32<W0> epi;
   epi.vr[0] = it.v(cur) + n;
   epi.vr[1] = it.Verg + n;
   epi.y[0] = it.y(cur);
@@ -761,8 +777,13 @@ __global__ void __launch_bounds__(kBlock) eval_rows32_kernel(Ctl* ctl, OpView<fl
   epi.long_terms = red.long_terms;
 #pragma unroll
   for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0f;
-  Gather2f g{it.v(cur), it.Verg};
-  run_tiles<float, float, 2>(K.ts, K.ptr, K.idx, K.val, g, epi);
+  if constexpr (W0 == 0) {
+    Gather2f g{it.v(cur), it.Verg};
+    run_tiles<float, float, 2>(K.ts, K.ptr, K.idx, K.val, g, epi);
+  } else {
+    Gather1<float, float> g{it.Verg};
+    run_tiles<float, float, 1>(K.ts, K.ptr, K.idx, K.val, g, epi);
+  }
   double acc[kEvalSums];
 #pragma unroll
   for (int q = 0; q < kEvalSums; ++q) acc[q] = epi.acc[q];
@@ -771,12 +792,13 @@ __global__ void __launch_bounds__(kBlock) eval_rows32_kernel(Ctl* ctl, OpView<fl
                          K.ts.nlong);
 }
 
+template <int W0>
 __global__ void __launch_bounds__(kBlock) eval_cols32_kernel(Ctl* ctl, OpView<float> Kt,
                                                              IterView<float> it, RedView red,
                                                              int fixed_parity) {
   if (fixed_parity < 0 && ctl->done) return;
   const int cur = eval_parity(ctl, fixed_parity);
-  EvalColEpi32 epi;
+  EvalColEpi32<W0> epi;
   epi.x[0] = it.v(cur);
   epi.x[1] = it.Verg;
   epi.x_rst = it.Vrst;
@@ -787,8 +809,13 @@ __global__ void __launch_bounds__(kBlock) eval_cols32_kernel(Ctl* ctl, OpView<fl
   epi.long_terms = red.long_terms;
 #pragma unroll
   for (int q = 0; q < kEvalSums; ++q) epi.acc[q] = 0.0f;
-  Gather2f g{it.y(cur), it.Yerg};
-  run_tiles<float, float, 2>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
+  if constexpr (W0 == 0) {
+    Gather2f g{it.y(cur), it.Yerg};
+    run_tiles<float, float, 2>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
+  } else {
+    Gather1<float, float> g{it.Yerg};
+    run_tiles<float, float, 1>(Kt.ts, Kt.ptr, Kt.idx, Kt.val, g, epi);
+  }
   double acc[kEvalSums];
 #pragma unroll
   for (int q = 0; q < kEvalSums; ++q) acc[q] = epi.acc[q];
@@ -1592,10 +1619,14 @@ void configure_kernels() {
   // Opt in to large dynamic shared memory; the launch sizes themselves follow each operator's
   // tile capacity, so occupancy is set by the actual size.
   const int big = 200 * 1024;
-  cudaFuncSetAttribute(eval_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(eval_cols_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(eval_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(eval_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(eval_rows_kernel<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(eval_rows_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(eval_cols_kernel<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(eval_cols_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(eval_rows_kernel<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(eval_rows_kernel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(eval_cols_kernel<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(eval_cols_kernel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_ray_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(det_ray_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(dual_step_kernel<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
@@ -1683,19 +1714,27 @@ void launch_halpern_dual(const Ctl* ctl, const OpView<T>& K, const IterView<T>& 
 template <typename T>
 void launch_eval(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
                  const EvalView& ev, const RedView& red, int grid_k, int grid_t,
-                 int fixed_parity, cudaStream_t s) {
+                 int fixed_parity, cudaStream_t s, bool second_only) {
+  const size_t smk = tile_smem_bytes(K.ts, 2, 8);
+  const size_t smt = tile_smem_bytes(Kt.ts, 2, 8);
   if constexpr (std::is_same<T, float>::value) {
     // FP32 operators carry their own (equilibrated) data: `ev` is not used.
     (void)ev;
-    eval_rows32_kernel<<<grid_k, kBlock, tile_smem_bytes(K.ts, 2, 8), s>>>(ctl, K, it, red,
-                                                                         fixed_parity);
-    eval_cols32_kernel<<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 2, 8), s>>>(ctl, Kt, it, red,
-                                                                           fixed_parity);
+    if (second_only) {
+      eval_rows32_kernel<1><<<grid_k, kBlock, smk, s>>>(ctl, K, it, red, fixed_parity);
+      eval_cols32_kernel<1><<<grid_t, kBlock, smt, s>>>(ctl, Kt, it, red, fixed_parity);
+    } else {
+      eval_rows32_kernel<0><<<grid_k, kBlock, smk, s>>>(ctl, K, it, red, fixed_parity);
+      eval_cols32_kernel<0><<<grid_t, kBlock, smt, s>>>(ctl, Kt, it, red, fixed_parity);
+    }
   } else {
-    eval_rows_kernel<T><<<grid_k, kBlock, tile_smem_bytes(K.ts, 2, 8), s>>>(ctl, K, it, ev, red,
-                                                                         fixed_parity);
-    eval_cols_kernel<T><<<grid_t, kBlock, tile_smem_bytes(Kt.ts, 2, 8), s>>>(ctl, Kt, it, ev,
-                                                                           red, fixed_parity);
+    if (second_only) {
+      eval_rows_kernel<T, 1><<<grid_k, kBlock, smk, s>>>(ctl, K, it, ev, red, fixed_parity);
+      eval_cols_kernel<T, 1><<<grid_t, kBlock, smt, s>>>(ctl, Kt, it, ev, red, fixed_parity);
+    } else {
+      eval_rows_kernel<T, 0><<<grid_k, kBlock, smk, s>>>(ctl, K, it, ev, red, fixed_parity);
+      eval_cols_kernel<T, 0><<<grid_t, kBlock, smt, s>>>(ctl, Kt, it, ev, red, fixed_parity);
+    }
   }
 }
 
@@ -1910,10 +1949,10 @@ template void launch_halpern_dual<float>(const Ctl*, const OpView<float>&,
                                          const IterView<float>&, int, int, cudaStream_t);
 template void launch_eval<double>(Ctl*, const OpView<double>&, const OpView<double>&,
                                   const IterView<double>&, const EvalView&, const RedView&, int,
-                                  int, int, cudaStream_t);
+                                  int, int, cudaStream_t, bool);
 template void launch_eval<float>(Ctl*, const OpView<float>&, const OpView<float>&,
                                  const IterView<float>&, const EvalView&, const RedView&, int, int,
-                                 int, cudaStream_t);
+                                 int, cudaStream_t, bool);
 template void launch_restart<double>(const Ctl*, const IterView<double>&, cudaStream_t);
 template void launch_restart<float>(const Ctl*, const IterView<float>&, cudaStream_t);
 template void launch_detect<double>(Ctl*, const OpView<double>&, const OpView<double>&,

@@ -77,9 +77,11 @@ template <typename T>
 void launch_halpern_dual(const Ctl* ctl, const OpView<T>& K, const IterView<T>& it, int j,
                          int grid, cudaStream_t s);
 template <typename T>
+// second_only: measure the second slot (Verg, Yerg) alone; the first slot's sums are 0 (the
+// Halpern solves decide on T(z) only).
 void launch_eval(Ctl* ctl, const OpView<T>& K, const OpView<T>& Kt, const IterView<T>& it,
                  const EvalView& ev, const RedView& red, int grid_k, int grid_t,
-                 int fixed_parity, cudaStream_t s);
+                 int fixed_parity, cudaStream_t s, bool second_only = false);
 void launch_decide_a(Ctl* ctl, cudaStream_t s);
 void launch_decide_b(Ctl* ctl, cudaStream_t s);
 template <typename T>
