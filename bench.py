@@ -226,16 +226,20 @@ def primal_step_bytes(lp, value_bytes, halpern=False):
     once, and the column epilogue: classic, 8 n-vectors (c, l, u, x, x_avg read; x_new, x_bar,
     x_avg written); Halpern, 7 (c, l, u, x, x0 read; x_new, x_bar written; x^ is written only by
     a chunk's last step, before an evaluation). When every column has the same bounds, each 0
-    or infinite (the transportation LP: x >= 0), the engine reads no bound vectors: 2 fewer."""
+    or infinite (the transportation LP: x >= 0), the engine reads no bound vectors: 2 fewer;
+    when every column has the same number of nonzeros (two in the transportation LP), no row
+    starts."""
     import numpy as np
     n, nnz = lp.n, lp.nnz
     m = int(np.count_nonzero(np.bincount(lp.rowidx[:nnz], minlength=lp.m)))
+    lens = np.diff(lp.colptr)
+    starts = 0 if n > 0 and np.all(lens == lens[0]) and lens[0] > 0 else (n + 1) * 4
     vecs = 7 if halpern else 8
     lo, up = lp.lower[:n], lp.upper[:n]
     if n > 0 and lo[0] in (0.0, -np.inf) and up[0] in (0.0, np.inf) and np.all(lo == lo[0]) \
             and np.all(up == up[0]):
         vecs -= 2
-    return nnz * (value_bytes + 4) + (n + 1) * 4 + m * value_bytes + vecs * n * value_bytes
+    return nnz * (value_bytes + 4) + starts + m * value_bytes + vecs * n * value_bytes
 
 
 def dual_step_bytes(lp, value_bytes, halpern=False, step_rows=None):

@@ -55,6 +55,10 @@ struct TileSet {
   const int* rows;
   int groups;         // kind-3 tiles in the set (0: none; only the dual step kernels take them)
   double* grp_part;   // [ntiles * 32] partial sums of kind-3 segments (when groups > 0)
+  // L > 0: every row of the operator has exactly L nonzeros (row r starts at r L), so the
+  // short-row tiles read no row starts (the columns of a transportation or network-flow LP:
+  // two nonzeros each); 0 otherwise.
+  int uniform_len;
 };
 
 constexpr int kGroupRows = 32;  // rows of a kind-3 tile at most (a warp's lanes)

@@ -618,8 +618,17 @@ int group_positions(int cap_nnz) {
 }
 
 // The gather neighbours among K's rows (row_neighbours_kernel), kept on the host for the tile
-// partition; none: host_adj stays empty.
+// partition; none: host_adj stays empty. Also marks operators whose rows all have the same
+// length (their short-row tiles need no row starts).
 int Engine::find_neighbours(std::string* err) {
+  for (DevOp* op : {&K_, &Kt_}) {
+    const std::vector<int>& p = op->host_ptr;
+    int len = op->rows > 0 ? p[1] - p[0] : 0;
+    for (int r = 1; len > 0 && r < op->rows; ++r) {
+      if (p[r + 1] - p[r] != len) len = 0;
+    }
+    op->uniform_len = len;
+  }
   K_.host_adj.clear();
   if (m_ < 2 || nnz_ == 0) return kOk;
   unsigned char* d = nullptr;

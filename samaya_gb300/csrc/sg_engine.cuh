@@ -90,6 +90,7 @@ struct DevOp {
   int variant = 0;
   int split = 0;
   int groups = 0;
+  int uniform_len = 0;  // every row of exactly this many nonzeros (0: not uniform)
   std::vector<int> host_ptr;
   // The rows the solves iterate over, when some rows are inert: an empty row whose logical has
   // no cost and 0 within its bounds keeps y_i = r_i = 0 in every iterate (every iterate starts
@@ -125,6 +126,7 @@ struct DevOp {
     t.rows = nullptr;
     t.groups = 0;
     t.grp_part = nullptr;
+    t.uniform_len = uniform_len;
     return t;
   }
   TileSet step_tileset() const {

@@ -297,8 +297,13 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
         int b = 0, e = 0, row = 0;
         if (valid) {
           row = tile_row(ts, tile.r0 + lr);
-          b = ldg(ptr + row);
-          e = ldg(ptr + row + 1);
+          if (ts.uniform_len > 0) {
+            b = row * ts.uniform_len;
+            e = b + ts.uniform_len;
+          } else {
+            b = ldg(ptr + row);
+            e = ldg(ptr + row + 1);
+          }
         }
         const bool shortrow = valid && e - b <= 32;
         if constexpr (has_pre<Epi>::value) {
