@@ -82,6 +82,14 @@ typedef struct sg_pdlp_opts {
                                 neighbouring columns (see sg_pdlp_step_rows): 0 (default) the
                                 tile tuner times them, 1 the built-in shape takes them, -1
                                 never */
+  int segment_staging;       /* 1: the dual steps stream the segments of rows longer than a
+                                tile through shared memory by bulk copies (two chunks of 2,048
+                                nonzeros in flight per CTA, completing on mbarriers); 0
+                                (default): the threads load them directly (measured faster on
+                                the power-law LP's long rows, which are bound by their
+                                scattered gathers, not by the nonzero stream) */
+  int tile_nnz;              /* built-in rule: nonzeros per tile (a power of two from 256 to
+                                16384); 0 (default): about 8 tiles per SM */
 } sg_pdlp_opts;
 
 /* Algorithm variants. REFERENCE follows samaya's PDLP step for step (L2 Ruiz, fixed step
@@ -222,10 +230,11 @@ int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_ro
                        int* ntiles, int* variant, int* split);
 
 /* The rows of A the solves' dual steps run over (m, unless inert rows are left out: see
- * sg_pdlp_opts.keep_inert_rows), the tiles over them, and how many of those tiles are row
- * groups (runs of up to 32 rows whose k-th nonzeros lie in neighbouring columns, staged so
- * that one gather reads neighbouring entries; a tuned shape may choose them). Diagnostics. */
-int sg_pdlp_step_rows(sg_pdlp* handle, int* rows, int* tiles, int* group_tiles);
+ * sg_pdlp_opts.keep_inert_rows), the tiles over them, how many of those tiles are row groups
+ * (runs of up to 32 rows whose k-th nonzeros lie in neighbouring columns, staged so that one
+ * gather reads neighbouring entries) and whether the long rows' segments are streamed through
+ * shared memory (1) or not (0); a tuned shape may choose either. Diagnostics. */
+int sg_pdlp_step_rows(sg_pdlp* handle, int* rows, int* tiles, int* group_tiles, int* staged);
 
 /* The engine's partition of a CSR operator (row starts row_ptr, rows + 1) into tiles for a tile
  * shape (nonzeros per tile, rows per short-row tile, warp-per-row threshold, team split; the

@@ -25,7 +25,8 @@ class Opts(ctypes.Structure):
                 ("verbose", ctypes.c_int), ("algorithm", ctypes.c_int),
                 ("autotune", ctypes.c_int),
                 ("tile_split", ctypes.c_int), ("artificial_restart", ctypes.c_double),
-                ("keep_inert_rows", ctypes.c_int), ("row_groups", ctypes.c_int)]
+                ("keep_inert_rows", ctypes.c_int), ("row_groups", ctypes.c_int),
+                ("segment_staging", ctypes.c_int), ("tile_nnz", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -111,7 +112,7 @@ def _declare(lib):
         "sg_spmv": (I, [P, I, c_double_p, c_double_p]),
         "sg_pdlp_time_kernels": (I, [P, I, c_double_p, c_double_p, c_double_p]),
         "sg_pdlp_tile_shape": (I, [P, I] + [ctypes.POINTER(ctypes.c_int)] * 5),
-        "sg_pdlp_step_rows": (I, [P] + [ctypes.POINTER(ctypes.c_int)] * 3),
+        "sg_pdlp_step_rows": (I, [P] + [ctypes.POINTER(ctypes.c_int)] * 4),
         "sg_build_tiles": (I, [I, c_int32_p, I, I, I, I, c_int32_p, I,
                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
         "sg_build_group_tiles": (I, [I, c_int32_p, ctypes.POINTER(ctypes.c_uint8), I, I, I, I,

@@ -46,6 +46,11 @@ sg::Options to_options(const sg_pdlp_opts* o) {
       o->artificial_restart > 0 && o->artificial_restart < 1 ? o->artificial_restart : 0.0;
   opt.skip_inert_rows = o->keep_inert_rows == 0;
   opt.row_groups = o->row_groups > 0 ? 1 : (o->row_groups < 0 ? -1 : 0);
+  opt.segment_staging = o->segment_staging > 0 ? 1 : -1;
+  opt.tile_nnz = 0;
+  for (int c = 256; c <= 4 * sg::kTileNnz; c *= 2) {
+    if (o->tile_nnz == c) opt.tile_nnz = c;
+  }
   return opt;
 }
 
@@ -382,11 +387,11 @@ int sg_pdlp_tile_shape(sg_pdlp* handle, int transpose, int* cap_nnz, int* cap_ro
   SG_SEAM(handle->engine->tile_shape(transpose, cap_nnz, cap_rows, ntiles, variant, split));
 }
 
-int sg_pdlp_step_rows(sg_pdlp* handle, int* rows, int* tiles, int* group_tiles) {
-  if (rows == nullptr || tiles == nullptr || group_tiles == nullptr) {
+int sg_pdlp_step_rows(sg_pdlp* handle, int* rows, int* tiles, int* group_tiles, int* staged) {
+  if (rows == nullptr || tiles == nullptr || group_tiles == nullptr || staged == nullptr) {
     return fail(SG_ERR_INVALID_ARGUMENT, "NULL output");
   }
-  SG_SEAM(handle->engine->step_rows(rows, tiles, group_tiles));
+  SG_SEAM(handle->engine->step_rows(rows, tiles, group_tiles, staged));
 }
 
 int sg_build_tiles(int rows, const int32_t* row_ptr, int cap_nnz, int cap_rows, int warp_min,

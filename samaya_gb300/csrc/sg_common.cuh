@@ -59,7 +59,14 @@ struct TileSet {
   // short-row tiles read no row starts (the columns of a transportation or network-flow LP:
   // two nonzeros each); 0 otherwise.
   int uniform_len;
+  // 1: the kind-1 segments are streamed through shared memory by bulk copies (dual step tile
+  // sets only; the operator's index and value arrays then carry kSegPad elements of padding).
+  int staged;
+  int* wait_error;  // set to 1 when a bounded wait for a bulk copy gave up (staged sets)
 };
+
+constexpr int kSegChunk = 2048;  // nonzeros per bulk-copied chunk of a staged segment
+constexpr int kSegPad = 4;       // padding elements after an operator's nonzeros
 
 constexpr int kGroupRows = 32;  // rows of a kind-3 tile at most (a warp's lanes)
 constexpr int kGroupPos = 16;   // nonzero positions per row staged per warp and round

@@ -216,6 +216,7 @@ Engine::~Engine() {
     dfree(op->st_grp_part);
     dfree(op->st_lcount);
   }
+  dfree(wait_error_);
   for (double** p : {&it64_.V[0], &it64_.V[1], &it64_.Vbar, &it64_.Y[0], &it64_.Y[1],
                      &it64_.Verg, &it64_.Yerg, &it64_.Vrst, &it64_.Yrst, &it64_.cost,
                      &it64_.lower, &it64_.upper, &it64_.rhs}) {
@@ -497,11 +498,12 @@ struct ShapeKey {
   int max_len;
   long long over32, over128, over4096;
   int fp32;
-  int groups;  // the row-group option (0 tuned, 1 built-in, -1 never)
+  int groups;   // the row-group option (0 tuned, 1 built-in, -1 never)
+  int staging;  // the segment-staging option (1 staged, -1 direct)
   bool operator<(const ShapeKey& o) const {
-    return std::tie(rows, nnz, max_len, over32, over128, over4096, fp32, groups) <
+    return std::tie(rows, nnz, max_len, over32, over128, over4096, fp32, groups, staging) <
            std::tie(o.rows, o.nnz, o.max_len, o.over32, o.over128, o.over4096, o.fp32,
-                    o.groups);
+                    o.groups, o.staging);
   }
 };
 
@@ -511,7 +513,7 @@ bool g_shape_file_read = false;
 
 // SG_TILE_CACHE names a text file that carries the tuner's choices across processes (so that a
 // profiler run, whose launches cannot be timed, uses the shapes a plain run picked): one line
-// per operator, the key's eight fields then the shape's six. Read once per process, appended
+// per operator, the key's nine fields then the shape's seven. Read once per process, appended
 // after each tuning. Call with g_shape_mu held.
 void read_shape_file() {
   if (g_shape_file_read) return;
@@ -522,13 +524,14 @@ void read_shape_file() {
   if (f == nullptr) return;
   ShapeKey k{};
   TileShape sh;
-  while (std::fscanf(f, "%d %lld %d %lld %lld %lld %d %d %d %d %d %d %d %d", &k.rows, &k.nnz,
-                     &k.max_len, &k.over32, &k.over128, &k.over4096, &k.fp32, &k.groups,
-                     &sh.cap_nnz, &sh.cap_rows, &sh.warp_min, &sh.variant, &sh.split,
-                     &sh.groups) == 14) {
+  while (std::fscanf(f, "%d %lld %d %lld %lld %lld %d %d %d %d %d %d %d %d %d %d", &k.rows,
+                     &k.nnz, &k.max_len, &k.over32, &k.over128, &k.over4096, &k.fp32,
+                     &k.groups, &k.staging, &sh.cap_nnz, &sh.cap_rows, &sh.warp_min,
+                     &sh.variant, &sh.split, &sh.groups, &sh.staged) == 16) {
     if (sh.cap_nnz >= 256 && sh.cap_nnz <= 4 * kTileNnz && sh.cap_rows >= 1 &&
         sh.cap_rows <= kTileRows && sh.warp_min >= 32 && (sh.variant == 0 || sh.variant == 1) &&
-        sh.split >= 0 && (sh.groups == 0 || sh.groups == 1)) {
+        sh.split >= 0 && (sh.groups == 0 || sh.groups == 1) &&
+        (sh.staged == 0 || sh.staged == 1)) {
       g_shape_cache[k] = sh;
     }
   }
@@ -540,16 +543,16 @@ void append_shape_file(const ShapeKey& k, const TileShape& sh) {
   if (path == nullptr || *path == '\0') return;
   FILE* f = std::fopen(path, "a");
   if (f == nullptr) return;
-  std::fprintf(f, "%d %lld %d %lld %lld %lld %d %d %d %d %d %d %d %d\n", k.rows, k.nnz,
-               k.max_len, k.over32, k.over128, k.over4096, k.fp32, k.groups, sh.cap_nnz,
-               sh.cap_rows, sh.warp_min, sh.variant, sh.split, sh.groups);
+  std::fprintf(f, "%d %lld %d %lld %lld %lld %d %d %d %d %d %d %d %d %d %d\n", k.rows, k.nnz,
+               k.max_len, k.over32, k.over128, k.over4096, k.fp32, k.groups, k.staging,
+               sh.cap_nnz, sh.cap_rows, sh.warp_min, sh.variant, sh.split, sh.groups, sh.staged);
   std::fclose(f);
 }
 
-ShapeKey shape_key(const DevOp& op, bool fp32, int groups) {
+ShapeKey shape_key(const DevOp& op, bool fp32, int groups, int staging) {
   // The rows the step kernel runs over (inert rows left out are empty).
   const int rows = op.act_rows != nullptr ? static_cast<int>(op.act_list.size()) : op.rows;
-  ShapeKey k{rows, op.nnz, 0, 0, 0, 0, fp32 ? 1 : 0, groups};
+  ShapeKey k{rows, op.nnz, 0, 0, 0, 0, fp32 ? 1 : 0, groups, staging};
   for (int r = 0; r < op.rows; ++r) {
     const int len = op.host_ptr[r + 1] - op.host_ptr[r];
     k.max_len = std::max(k.max_len, len);
@@ -570,6 +573,7 @@ TileShape Engine::default_shape(const DevOp& op) const {
   TileShape sh;
   int cap = 256;
   while (cap < kTileNnz && cap < target) cap *= 2;
+  if (opt_.tile_nnz > 0) cap = opt_.tile_nnz;
   sh.cap_nnz = cap;
   sh.cap_rows = std::min(kTileRows, std::max(256, cap / 2));
   sh.warp_min = kWarpRowMin;
@@ -582,6 +586,7 @@ TileShape Engine::default_shape(const DevOp& op) const {
   sh.variant = 2 * in_long >= op.nnz && op.nnz > 0 ? 1 : 0;
   sh.split = opt_.tile_split;
   sh.groups = opt_.row_groups > 0 ? 1 : 0;
+  sh.staged = opt_.segment_staging > 0 ? 1 : 0;
   return sh;
 }
 
@@ -664,10 +669,12 @@ int Engine::set_tiles(DevOp* op, const TileShape& shape) {
               &nlong);
   const bool grouped =
       shape.groups != 0 && op == &K_ && !op->host_adj.empty() && opt_.row_groups >= 0;
-  const bool step_set = op->act_rows != nullptr || grouped;
+  const bool staged = shape.staged != 0 && op == &K_ && opt_.segment_staging >= 0;
+  const bool step_set = op->act_rows != nullptr || grouped || staged;
   std::vector<Tile> st_tiles;
   int st_nlong = 0;
   int st_groups = 0;
+  int st_staged = 0;
   if (step_set) {
     // The active rows' starts: the rows left out are empty, so consecutive active rows are
     // contiguous in the nonzeros and the tiles' nonzero ranges are the operator's own. Two
@@ -689,7 +696,10 @@ int Engine::set_tiles(DevOp* op, const TileShape& shape) {
     build_tiles(vp, shape.cap_nnz, shape.cap_rows, shape.warp_min, shape.split, &st_tiles,
                 &st_nlong, grouped ? &vadj : nullptr,
                 grouped ? group_positions(shape.cap_nnz) : 0);
-    for (const Tile& t : st_tiles) st_groups += t.kind == 3;
+    for (const Tile& t : st_tiles) {
+      st_groups += t.kind == 3;
+      st_staged |= staged && t.kind == 1 ? 1 : 0;
+    }
   }
   SG_TRY(cudaStreamSynchronize(stream_));
   dfree(op->tiles);
@@ -706,6 +716,7 @@ int Engine::set_tiles(DevOp* op, const TileShape& shape) {
   op->variant = shape.variant;
   op->split = shape.split;
   op->groups = grouped ? 1 : 0;
+  op->staged = st_staged;
   op->ntiles = static_cast<int>(tiles.size());
   op->nlong = nlong;
   SG_TRY(dalloc(&op->tiles, tiles.size()));
@@ -720,6 +731,7 @@ int Engine::set_tiles(DevOp* op, const TileShape& shape) {
     op->st_ntiles = static_cast<int>(st_tiles.size());
     op->st_nlong = st_nlong;
     op->st_groups = st_groups;
+    op->st_staged = st_staged;
     SG_TRY(dalloc(&op->st_tiles, st_tiles.size()));
     if (!st_tiles.empty()) {
       SG_TRY(cudaMemcpyAsync(op->st_tiles, st_tiles.data(), st_tiles.size() * sizeof(Tile),
@@ -814,7 +826,7 @@ int Engine::tune_tiles(std::string* err) {
     ShapeKey key{};
     bool cached = false;
     if (tune) {
-      key = shape_key(*op, fp32_, opt_.row_groups);
+      key = shape_key(*op, fp32_, opt_.row_groups, opt_.segment_staging);
       std::lock_guard<std::mutex> lock(g_shape_mu);
       read_shape_file();
       auto it = g_shape_cache.find(key);
@@ -858,7 +870,9 @@ int Engine::tune_tiles(std::string* err) {
       }
       constexpr double kTuneMargin = 0.97;
       double best_ms = -1.0;
-      // With gather-neighbour rows, every candidate also with row groups.
+      // With gather-neighbour rows, every candidate also with row groups. (Staged segments
+      // are not a candidate: on the power-law LP's long rows they measured slower than the
+      // direct loads at every capacity, 57.9 against 50.3 us in FP64.)
       if (which == 0 && !op->host_adj.empty() && opt_.row_groups == 0) {
         const size_t plain = cands.size();
         for (size_t c = 0; c < plain; ++c) {
@@ -920,13 +934,25 @@ int Engine::alloc_all(std::string* err) {
   const size_t nb = static_cast<size_t>(nnz_);
   SG_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   for (auto& ev : ev_) SG_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  // The nonzero arrays carry kSegPad zeroed elements after the last nonzero: a staged segment's
+  // bulk copies end at the 4-aligned position above it.
   for (DevOp* op : {&K_, &Kt_}) {
     SG_TRY(dalloc(&op->ptr, static_cast<size_t>(op->rows) + 1));
-    SG_TRY(dalloc(&op->idx, nb));
-    SG_TRY(dalloc(&op->val, nb));
-    SG_TRY(dalloc(&op->val_orig, nb));
-    if (fp32_) SG_TRY(dalloc(&op->val32, nb));
+    SG_TRY(dalloc(&op->idx, nb + kSegPad));
+    SG_TRY(dalloc(&op->val, nb + kSegPad));
+    SG_TRY(dalloc(&op->val_orig, nb + kSegPad));
+    SG_TRY(cudaMemsetAsync(op->idx + nb, 0, kSegPad * sizeof(int), stream_));
+    SG_TRY(cudaMemsetAsync(op->val + nb, 0, kSegPad * sizeof(double), stream_));
+    SG_TRY(cudaMemsetAsync(op->val_orig + nb, 0, kSegPad * sizeof(double), stream_));
+    if (fp32_) {
+      SG_TRY(dalloc(&op->val32, nb + kSegPad));
+      SG_TRY(cudaMemsetAsync(op->val32 + nb, 0, kSegPad * sizeof(float), stream_));
+    }
   }
+  SG_TRY(dalloc(&wait_error_, 1));
+  SG_TRY(cudaMemsetAsync(wait_error_, 0, sizeof(int), stream_));
+  K_.wait_error = wait_error_;
+  Kt_.wait_error = wait_error_;
   for (double** p : {&it64_.V[0], &it64_.V[1], &it64_.Vbar, &it64_.Verg, &it64_.Vrst,
                      &it64_.cost, &it64_.lower, &it64_.upper}) {
     SG_TRY(dalloc(p, nt));
@@ -1273,6 +1299,20 @@ int Engine::run_loop(double deadline_s, SolveInfo* info, cudaGraphExec_t exec, C
   return kOk;
 }
 
+// A staged segment's bulk copy that never completed (its bounded wait gave up) makes the
+// launch's sums unusable: the call reports it (and the flag is cleared).
+int Engine::check_wait_error(std::string* err) {
+  int flag = 0;
+  if (cudaMemcpy(&flag, wait_error_, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    if (err) *err = "reading the wait flag failed";
+    return kErrCuda;
+  }
+  if (flag == 0) return kOk;
+  cudaMemset(wait_error_, 0, sizeof(int));
+  if (err) *err = "a bulk copy into shared memory did not complete";
+  return kErrCuda;
+}
+
 int Engine::solve(SolveInfo* info, double* x, double* y, double* dual_ray, double* primal_ray,
                   std::string* err) {
   *info = SolveInfo();
@@ -1292,8 +1332,11 @@ int Engine::solve(SolveInfo* info, double* x, double* y, double* dual_ray, doubl
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (rc != kOk && err) *err = std::string("solve failed: ") + cudaGetErrorString(cudaGetLastError());
-  return rc;
+  if (rc != kOk) {
+    if (err) *err = std::string("solve failed: ") + cudaGetErrorString(cudaGetLastError());
+    return rc;
+  }
+  return check_wait_error(err);
 }
 
 int Engine::solve_fp64(SolveInfo* info, double* x, double* y, double* dual_ray,

@@ -41,6 +41,8 @@ struct Options {
   double artificial_restart = 0.0;  // forced-restart fraction (0: 0.36 reference, 0.1 others)
   bool skip_inert_rows = true;      // leave inert rows (see DevOp::act_rows) out of the solves
   int row_groups = 0;               // kind-3 row groups: 0 tuner decides, 1 built-in, -1 never
+  int segment_staging = 0;          // staged kind-1 segments: 1 always, otherwise never
+  int tile_nnz = 0;                 // built-in rule's nonzeros per tile (0: ~8 tiles per SM)
 };
 
 // Tile shape of an operator: nonzeros per tile (and per long-row segment), rows per short-row
@@ -52,6 +54,7 @@ struct TileShape {
   int variant = 0;          // step kernel variant (see sg_kernels.cu)
   int split = 0;            // kind-2 rows: nonzeros per warp of a team (0: a warp per row)
   int groups = 0;           // dual steps: runs of gather-neighbour rows as kind-3 row groups
+  int staged = 0;           // dual steps: kind-1 segments streamed through shared memory
 };
 
 struct SolveInfo {
@@ -90,7 +93,9 @@ struct DevOp {
   int variant = 0;
   int split = 0;
   int groups = 0;
+  int staged = 0;
   int uniform_len = 0;  // every row of exactly this many nonzeros (0: not uniform)
+  int* wait_error = nullptr;  // the engine's bounded-wait flag (staged step sets)
   std::vector<int> host_ptr;
   // The rows the solves iterate over, when some rows are inert: an empty row whose logical has
   // no cost and 0 within its bounds keeps y_i = r_i = 0 in every iterate (every iterate starts
@@ -109,6 +114,7 @@ struct DevOp {
   int st_ntiles = 0;
   int st_nlong = 0;
   int st_groups = 0;
+  int st_staged = 0;
   double* st_seg_part = nullptr;
   double* st_grp_part = nullptr;
   unsigned* st_lcount = nullptr;
@@ -127,6 +133,8 @@ struct DevOp {
     t.groups = 0;
     t.grp_part = nullptr;
     t.uniform_len = uniform_len;
+    t.staged = 0;
+    t.wait_error = wait_error;
     return t;
   }
   TileSet step_tileset() const {
@@ -140,6 +148,7 @@ struct DevOp {
     t.rows = act_rows;
     t.groups = st_groups;
     t.grp_part = st_grp_part;
+    t.staged = st_staged;
     return t;
   }
   int step_tiles() const { return step_set ? st_ntiles : ntiles; }
@@ -231,10 +240,11 @@ class Engine {
   int time_kernels(int reps, double* ms_dual, double* ms_primal, double* ms_eval);
   int tile_capacity(int transpose) const { return transpose ? Kt_.cap_nnz : K_.cap_nnz; }
   // The rows of A the solves' dual steps run over, their tiles, and the row-group tiles.
-  int step_rows(int* rows, int* tiles, int* group_tiles) const {
+  int step_rows(int* rows, int* tiles, int* group_tiles, int* staged) const {
     *rows = K_.act_rows != nullptr ? static_cast<int>(K_.act_list.size()) : m_;
     *tiles = K_.step_tiles();
     *group_tiles = K_.step_set ? K_.st_groups : 0;
+    *staged = K_.step_set ? K_.st_staged : 0;
     return kOk;
   }
   int tile_shape(int transpose, int* cap_nnz, int* cap_rows, int* ntiles, int* variant,
@@ -293,6 +303,8 @@ class Engine {
   int m_ = 0, n_ = 0;
   long long nnz_ = 0;
   Options opt_;
+  int* wait_error_ = nullptr;  // device: a staged segment's bounded wait gave up
+  int check_wait_error(std::string* err);
   // grid_step_k_: the dual steps of the solves (active rows); grid_full_k_: every row.
   int grid_k_ = 1, grid_t_ = 1, grid_step_k_ = 1, grid_step_t_ = 1, grid_full_k_ = 1;
   int sm_count_ = 148;

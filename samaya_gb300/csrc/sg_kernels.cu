@@ -235,7 +235,8 @@ __device__ __forceinline__ StepScalars<ACC> step_scalars(const Ctl* __restrict__
 //   1: 128 registers, the warp-per-row and segment loops unrolled twice as deep (operators of
 //      long rows, whose few CTAs need more loads in flight each; at 3 CTAs per SM, 80
 //      registers, no faster on the transportation LP);
-//   2 (dual steps only): variant 0 plus the kind-3 row groups of a tile set that has them.
+//   2 (dual steps only): variant 0 plus the kind-3 row groups and the staged kind-1 segments
+//      of a tile set that has them.
 // (Measured and not kept: a third variant loading a short row's first three pairs of
 // nonzeros together at 4 CTAs per SM; no faster on the transportation or power-law LPs.)
 template <typename T>
@@ -1607,10 +1608,18 @@ size_t tile_smem_bytes(const TileSet& ts, int nv, size_t acc_bytes) {
 
 namespace {
 
-// The dual step launches: the kind-3 staging when the tile set has row groups.
+// The dual step launches: the kind-3 staging or the staged segments' chunk buffers when the
+// tile set has them (both in the variant-2 kernels).
+template <typename T>
+bool dual_variant2(const TileSet& ts) {
+  return ts.groups > 0 || ts.staged;
+}
 template <typename T>
 size_t dual_smem_bytes(const TileSet& ts) {
-  return ts.groups > 0 ? group_smem_size<T, Acc<T>>() : tile_smem_bytes(ts, 1, sizeof(T));
+  if (!dual_variant2<T>(ts)) return tile_smem_bytes(ts, 1, sizeof(T));
+  const size_t g = group_smem_size<T, Acc<T>>();
+  const size_t c = staged_smem_size<T>();
+  return g > c ? g : c;
 }
 
 }  // namespace
@@ -1664,7 +1673,7 @@ void launch_dual_step(const Ctl* ctl, const OpView<T>& K, const IterView<T>& it,
                       cudaStream_t s) {
   if (K.ts.ntiles == 0) return;
   const size_t sm = dual_smem_bytes<T>(K.ts);
-  if (K.ts.groups > 0) {
+  if (dual_variant2<T>(K.ts)) {
     dual_step_kernel<T, 2><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
   } else if (K.ts.variant == 1) {
     dual_step_kernel<T, 1><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
@@ -1702,7 +1711,7 @@ void launch_halpern_dual(const Ctl* ctl, const OpView<T>& K, const IterView<T>& 
                          int grid, cudaStream_t s) {
   if (K.ts.ntiles == 0) return;
   const size_t sm = dual_smem_bytes<T>(K.ts);
-  if (K.ts.groups > 0) {
+  if (dual_variant2<T>(K.ts)) {
     halpern_dual_kernel<T, 2><<<grid, kBlock, sm, s>>>(ctl, K, it, j);
   } else if (K.ts.variant == 1) {
     halpern_dual_kernel<T, 1><<<grid, kBlock, sm, s>>>(ctl, K, it, j);

@@ -37,6 +37,52 @@ __host__ __device__ constexpr size_t tile_smem_size(int, size_t, int, int) {
   return sizeof(double) * kRedDoubles;
 }
 
+// Staged kind-1 segments: two chunks of kSegChunk indices and values (double buffer).
+template <typename T>
+__host__ __device__ constexpr size_t staged_smem_size() {
+  return sizeof(double) * kRedDoubles + 2 * kSegChunk * (sizeof(int) + sizeof(T));
+}
+
+// mbarrier and bulk-copy primitives (PTX ISA: mbarrier, cp.async.bulk).
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes,
+                                              unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// A bounded wait: gives up after kWaitTries polls (each poll may suspend the thread for a
+// while), far beyond any copy's completion time.
+constexpr int kWaitTries = 1 << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  for (int k = 0; k < kWaitTries; ++k) {
+    if (mbar_try_wait(bar, parity)) return true;
+  }
+  return false;
+}
+
 // Kind-3 staging: per warp kGroupRows x (kGroupPos + 1) indices and values (the extra column
 // keeps lane l's reads of row l conflict-free), then the warps' row sums.
 constexpr int kGroupStride = kGroupPos + 1;
@@ -276,6 +322,22 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
   const int tid = threadIdx.x;
   __shared__ bool last_seg;
   double* red = smem_red();
+  // Staged segments (GROUPS kernels of a set with ts.staged): two chunk buffers after the
+  // reduction scratch, their completion barriers and expected parities (uniform over the CTA).
+  __shared__ __align__(8) unsigned long long seg_bar[2];
+  __shared__ int seg_fail;
+  unsigned seg_parity = 0u;
+  if constexpr (GROUPS) {
+    if (ts.staged) {
+      if (tid == 0) {
+        mbar_init(&seg_bar[0], 1);
+        mbar_init(&seg_bar[1], 1);
+        seg_fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      }
+      __syncthreads();
+    }
+  }
   for (int ti = blockIdx.x; ti < ts.ntiles; ti += gridDim.x) {
     const Tile tile = ts.tiles[ti];
     if constexpr (GROUPS) {
@@ -452,7 +514,75 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
       ACC s[NV];
 #pragma unroll
       for (int v = 0; v < NV; ++v) s[v] = ACC(0);
-      {
+      bool staged_done = false;
+      if constexpr (GROUPS) {
+        if (ts.staged) {
+          // The segment [k0, k1) streamed through shared memory: chunks of kSegChunk nonzeros
+          // from the 4-aligned position below k0 to the one above k1 (16-byte aligned copies
+          // of a multiple of 16 bytes; the arrays carry kSegPad elements of padding), two in
+          // flight, completing on an mbarrier each. Thread t sums the in-segment elements at
+          // 4 t .. 4 t + 3 and 4 t + 1024 .. of every chunk, in chunk order.
+          int* cidx = reinterpret_cast<int*>(red + kRedDoubles);
+          T* cval = reinterpret_cast<T*>(cidx + 2 * kSegChunk);
+          const int k0 = tile.k0;
+          const int k1 = tile.k1;
+          const int base = k0 & ~3;
+          const int end = (k1 + 3) & ~3;
+          const int nch = (end - base + kSegChunk - 1) / kSegChunk;
+          auto issue = [&](int c) {
+            const int st = c & 1;
+            const int from = base + c * kSegChunk;
+            const int len = min(kSegChunk, end - from);
+            const unsigned bi = static_cast<unsigned>(len) * sizeof(int);
+            const unsigned bv = static_cast<unsigned>(len) * sizeof(T);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(&seg_bar[st], bi + bv);
+            bulk_copy_g2s(cidx + st * kSegChunk, idx + from, bi, &seg_bar[st]);
+            bulk_copy_g2s(cval + st * kSegChunk, val + from, bv, &seg_bar[st]);
+          };
+          auto wait = [&](int c) {
+            const int st = c & 1;
+            if (!mbar_wait_bounded(&seg_bar[st], (seg_parity >> st) & 1u)) seg_fail = 1;
+            seg_parity ^= 1u << st;
+          };
+          if (tid == 0) {
+            issue(0);
+            if (nch > 1) issue(1);
+          }
+          wait(0);
+          __syncthreads();
+          for (int c = 0; c < nch && !seg_fail; ++c) {
+            const int st = c & 1;
+            const int from = base + c * kSegChunk;
+#pragma unroll
+            for (int u = 0; u < kSegChunk / (4 * kBlock); ++u) {
+              const int e = 4 * tid + u * 4 * kBlock;
+              const int4 j = *reinterpret_cast<const int4*>(cidx + st * kSegChunk + e);
+              const T* vp = cval + st * kSegChunk + e;
+              const int p = from + e;
+              const int jj[4] = {j.x, j.y, j.z, j.w};
+#pragma unroll
+              for (int w = 0; w < 4; ++w) {
+                if (p + w >= k0 && p + w < k1) {
+#pragma unroll
+                  for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, vp[w], jj[w]));
+                }
+              }
+            }
+            if (c + 1 < nch) wait(c + 1);
+            __syncthreads();
+            if (tid == 0 && c + 2 < nch && !seg_fail) issue(c + 2);
+          }
+          if (seg_fail) {
+            // A copy never completed: report it and leave the tile loop (the solve then fails
+            // on the flag; the sums of this launch are not used).
+            if (tid == 0) atomicExch(ts.wait_error, 1);
+            return;
+          }
+          staged_done = true;
+        }
+      }
+      if (!staged_done) {
         // Head up to a 4-aligned position, then 16-byte loads of four nonzeros per thread,
         // then the tail (scalar).
         const int k0 = tile.k0;

@@ -47,6 +47,8 @@ class PdlpOptions:
     artificial_restart: float = 0.0
     keep_inert_rows: bool = False
     row_groups: int = 0
+    segment_staging: int = 0
+    tile_nnz: int = 0
 
     def to_c(self) -> _native.Opts:
         o = _native.Opts()
@@ -64,6 +66,8 @@ class PdlpOptions:
         o.artificial_restart = float(self.artificial_restart)
         o.keep_inert_rows = 1 if self.keep_inert_rows else 0
         o.row_groups = int(self.row_groups)
+        o.segment_staging = int(self.segment_staging)
+        o.tile_nnz = int(self.tile_nnz)
         return o
 
 
@@ -182,14 +186,14 @@ class PdlpSolver:
             out[name] = (v[0].value, v[1].value, v[2].value, v[3].value, v[4].value)
         return out
 
-    def step_rows(self) -> tuple[int, int, int]:
-        """(rows of A the dual steps run over, their tiles, the row-group tiles among them):
-        m rows unless inert rows (empty, a logical with no cost and 0 within its bounds) are
-        left out."""
-        v = [ctypes.c_int(0) for _ in range(3)]
+    def step_rows(self) -> tuple[int, int, int, int]:
+        """(rows of A the dual steps run over, their tiles, the row-group tiles among them,
+        1 if the long rows' segments are staged through shared memory): m rows unless inert
+        rows (empty, a logical with no cost and 0 within its bounds) are left out."""
+        v = [ctypes.c_int(0) for _ in range(4)]
         _native.check(self._lib.sg_pdlp_step_rows(self._h, *[ctypes.byref(x) for x in v]),
                       "sg_pdlp_step_rows")
-        return v[0].value, v[1].value, v[2].value
+        return v[0].value, v[1].value, v[2].value, v[3].value
 
     def solve(self, x_out: np.ndarray | None = None, y_out: np.ndarray | None = None,
               download: bool = True) -> PdlpResult:
@@ -294,13 +298,13 @@ class PdhgDevice:
             o = options.to_c()
             _native.check(self._lib.sg_pdlp_create(*args, ctypes.byref(o)), "sg_pdlp_create")
 
-    def step_rows(self) -> tuple[int, int, int]:
-        """As ``PdlpSolver.step_rows``: the rows, tiles and row-group tiles of the dual
-        steps."""
-        v = [ctypes.c_int(0) for _ in range(3)]
+    def step_rows(self) -> tuple[int, int, int, int]:
+        """As ``PdlpSolver.step_rows``: the rows, tiles, row-group tiles and segment staging of
+        the dual steps."""
+        v = [ctypes.c_int(0) for _ in range(4)]
         _native.check(self._lib.sg_pdlp_step_rows(self._h, *[ctypes.byref(x) for x in v]),
                       "sg_pdlp_step_rows")
-        return v[0].value, v[1].value, v[2].value
+        return v[0].value, v[1].value, v[2].value, v[3].value
 
     def set_original(self, col_scale, row_scale, cost, lower, upper):
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in

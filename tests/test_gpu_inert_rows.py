@@ -73,7 +73,7 @@ def test_leaving_inert_rows_out_changes_no_bit(engine, models, name, algorithm, 
                                   autotune=False, keep_inert_rows=keep,
                                   max_iterations=MAX_ITERATIONS)
         with engine.PdlpSolver(lp, opts) as s:
-            rows, tiles, _ = s.step_rows()
+            rows, tiles, _, _ = s.step_rows()
             assert rows == (lp.m if keep else lp.m - inert)
             assert tiles > 0
             out.append(s.solve())
@@ -115,7 +115,7 @@ def test_an_empty_row_that_excludes_zero_is_stepped(engine):
         opts = engine.PdlpOptions(tol=1e-6, autotune=False, keep_inert_rows=keep,
                                   max_iterations=100000)
         with engine.PdlpSolver(lp, opts) as s:
-            rows, _, _ = s.step_rows()
+            rows, _, _, _ = s.step_rows()
             assert rows == (lp.m if keep else lp.m - _inert(model))
             out.append(s.solve())
     a, b = out

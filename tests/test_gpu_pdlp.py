@@ -287,7 +287,7 @@ def test_tile_cache_file_carries_the_tuned_shapes(tmp_path):
                            text=True, timeout=600)
     assert first.returncode == 0, first.stderr
     lines = path.read_text().splitlines()
-    assert len(lines) == 2 and all(len(x.split()) == 14 for x in lines), lines
+    assert len(lines) == 2 and all(len(x.split()) == 16 for x in lines), lines
     second = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True,
                             text=True, timeout=600)
     assert second.returncode == 0, second.stderr

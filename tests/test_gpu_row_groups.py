@@ -33,7 +33,7 @@ def test_group_halpern_steps_match_the_oracle(engine, oracle, precision):
         opts = engine.PdlpOptions(precision=precision, autotune=False, row_groups=1)
         dev = engine.PdhgDevice(e["m"], e["n"], e["colptr"], e["rowidx"], e["vals"], e["cost"],
                                 e["lower"], e["upper"], options=opts)
-        rows, tiles, groups = dev.step_rows()
+        rows, tiles, groups, _ = dev.step_rows()
         assert rows == lp.m and groups >= 2
         dev.set_original(e["cs"], e["rs"], lp.cost, lp.lower, lp.upper)
         dev.set_state(v, y, v0, y0, precision=0 if precision == 0 else 1)
