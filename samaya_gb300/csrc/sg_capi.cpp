@@ -140,8 +140,8 @@ int sg_pdlp_create(sg_pdlp** handle, int m, int n, const int64_t* a_colptr,
   try {
     std::string why;
     sg::Engine* e = nullptr;
-    const int rc = sg::Engine::create(&e, m, n, a_colptr, a_rowidx, a_val, cost, lower, upper,
-                                      to_options(opts), &why);
+    const int rc = sg::create_engine_from_lp(&e, m, n, a_colptr, a_rowidx, a_val, cost, lower,
+                                             upper, to_options(opts), &why);
     if (rc != sg::kOk) return fail(rc, why);
     *handle = new sg_pdlp{e};
     return SG_OK;

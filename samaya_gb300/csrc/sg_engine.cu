@@ -201,12 +201,11 @@ Engine::~Engine() {
   if (stream_) cudaStreamSynchronize(stream_);
   if (chunk_exec_) cudaGraphExecDestroy(chunk_exec_);
   if (chunk_graph_) cudaGraphDestroy(chunk_graph_);
+  if (chunk32_exec_) cudaGraphExecDestroy(chunk32_exec_);
+  if (chunk32_graph_) cudaGraphDestroy(chunk32_graph_);
+  // The buffers sized by the problem live in the arena; the tile sets and the rest are their
+  // own allocations.
   for (DevOp* op : {&K_, &Kt_}) {
-    dfree(op->ptr);
-    dfree(op->idx);
-    dfree(op->val);
-    dfree(op->val_orig);
-    dfree(op->val32);
     dfree(op->tiles);
     dfree(op->seg_part);
     dfree(op->lcount);
@@ -216,32 +215,8 @@ Engine::~Engine() {
     dfree(op->st_grp_part);
     dfree(op->st_lcount);
   }
-  dfree(wait_error_);
-  for (double** p : {&it64_.V[0], &it64_.V[1], &it64_.Vbar, &it64_.Y[0], &it64_.Y[1],
-                     &it64_.Verg, &it64_.Yerg, &it64_.Vrst, &it64_.Yrst, &it64_.cost,
-                     &it64_.lower, &it64_.upper, &it64_.rhs}) {
-    dfree(*p);
-  }
-  for (float** p : {&it32_.V[0], &it32_.V[1], &it32_.Vbar, &it32_.Y[0], &it32_.Y[1],
-                    &it32_.Verg, &it32_.Yerg, &it32_.Vrst, &it32_.Yrst, &it32_.cost,
-                    &it32_.lower, &it32_.upper, &it32_.rhs}) {
-    dfree(*p);
-  }
-  for (double** p : {&cost_orig_, &lower_orig_, &upper_orig_, &cost_ev_, &lower_ev_, &upper_ev_,
-                     &rhs_ev_, &cs_, &rs_, &inv_cs_, &inv_rs_, &cn_, &rn_, &pu_, &pv_, &u0_,
-                     &scratch_n_, &x_out_,
-                     &y_out_, &ray_out_, &partial_, &long_terms_}) {
-    dfree(*p);
-  }
-  for (double** p : {&ones_n_, &ones_m_, &cost_in_, &lower_in_, &upper_in_, &rhs_in_, &bh_,
-                     &dvec_}) {
-    dfree(*p);
-  }
-  if (chunk32_exec_) cudaGraphExecDestroy(chunk32_exec_);
-  if (chunk32_graph_) cudaGraphDestroy(chunk32_graph_);
-  dfree(ctl32_);
-  dfree(counter_);
-  dfree(ctl_);
+  dfree(long_terms_);
+  dfree(arena_);
   if (ctl_host_) cudaFreeHost(ctl_host_);
   for (auto& e : ev_) {
     if (e) cudaEventDestroy(e);
@@ -263,144 +238,6 @@ int Engine::check(cudaError_t e, const char* what) {
       return e_ == cudaErrorMemoryAllocation ? kErrOutOfMemory : kErrCuda; \
     }                                       \
   } while (0)
-
-int Engine::create(Engine** out, int m, int n, const int64_t* colptr, const int32_t* rowidx,
-                   const double* val, const double* cost, const double* lower,
-                   const double* upper, const Options& opt, std::string* err) {
-  *out = nullptr;
-  if (m < 0 || n < 0 || colptr == nullptr || cost == nullptr || lower == nullptr ||
-      upper == nullptr) {
-    if (err) *err = "invalid argument";
-    return kErrInvalidArgument;
-  }
-  const long long nnz = colptr[n];
-  if (nnz < 0 || colptr[0] != 0) {
-    if (err) *err = "column starts must begin at 0";
-    return kErrInvalidArgument;
-  }
-  if (nnz >= static_cast<long long>(std::numeric_limits<int>::max()) ||
-      static_cast<long long>(n) + m >= std::numeric_limits<int>::max()) {
-    if (err) *err = "matrix too large for 32-bit offsets";
-    return kErrTooLarge;
-  }
-  if (nnz > 0 && (rowidx == nullptr || val == nullptr)) {
-    if (err) *err = "null matrix arrays";
-    return kErrInvalidArgument;
-  }
-  for (int j = 0; j < n; ++j) {
-    if (colptr[j + 1] < colptr[j]) {
-      if (err) *err = "column starts must not decrease";
-      return kErrInvalidArgument;
-    }
-  }
-  // K = A by rows (checking every row index and value on the way); K' = A^T by rows is the CSC
-  // of A.
-  std::vector<int> kptr(static_cast<size_t>(m) + 1, 0);
-  std::vector<int> kidx(static_cast<size_t>(std::max<long long>(nnz, 1)));
-  std::vector<double> kval(static_cast<size_t>(std::max<long long>(nnz, 1)));
-  {
-    const char* why = nullptr;
-    if (csc_to_csr(m, n, colptr, rowidx, val, kptr.data(), kidx.data(), kval.data(), 16,
-                   &why) != 0) {
-      if (err) *err = why;
-      return kErrInvalidArgument;
-    }
-  }
-  for (long long k = 0; k < static_cast<long long>(n) + m; ++k) {
-    if (!std::isfinite(cost[k]) || std::isnan(lower[k]) || std::isnan(upper[k])) {
-      if (err) *err = "cost or bound not valid";
-      return kErrInvalidArgument;
-    }
-  }
-  int dev_major = 0, dev_minor = 0;
-  if (device_info(&dev_major, &dev_minor, nullptr, 0) != kOk) {
-    if (err) *err = "no sm_103 GPU";
-    return kErrNoDevice;
-  }
-  Engine* e = new Engine();
-  e->m_ = m;
-  e->n_ = n;
-  e->nnz_ = nnz;
-  e->opt_ = opt;
-  e->fp32_ = opt.precision == 1 || opt.precision == 2;
-  e->switch_ = opt.precision == 2;
-  // Every structural column with the same bounds, each 0 or infinite (equilibration divides
-  // them by a positive factor, so they stay shared): the primal steps skip the bound vectors.
-  if (n > 0) {
-    const double lo = lower[0], hi = upper[0];
-    bool uniform = (lo == 0.0 || lo == -INFINITY) && (hi == 0.0 || hi == INFINITY);
-    for (int j = 1; uniform && j < n; ++j) uniform = lower[j] == lo && upper[j] == hi;
-    e->x_bounds_uniform_ = uniform;
-    e->x_lo_ = lo;
-    e->x_hi_ = hi;
-  }
-  std::vector<int> tptr(static_cast<size_t>(n) + 1);
-  for (int j = 0; j <= n; ++j) tptr[j] = static_cast<int>(colptr[j]);
-  e->K_.rows = m;
-  e->K_.cols = n;
-  e->K_.nnz = nnz;
-  e->K_.host_ptr = kptr;
-  e->Kt_.rows = n;
-  e->Kt_.cols = m;
-  e->Kt_.nnz = nnz;
-  e->Kt_.host_ptr = tptr;
-  std::string why;
-  int rc = e->alloc_all(&why);
-  if (rc != kOk) {
-    if (err) *err = why;
-    delete e;
-    return rc;
-  }
-  cudaStream_t s = e->stream_;
-  const size_t nb = static_cast<size_t>(nnz);
-  const size_t nt = static_cast<size_t>(n) + m;
-  auto up = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
-    if (bytes == 0) return cudaSuccess;
-    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
-  };
-  cudaError_t ce = cudaSuccess;
-  ce = up(e->K_.ptr, kptr.data(), kptr.size() * sizeof(int));
-  if (ce == cudaSuccess) ce = up(e->K_.idx, kidx.data(), nb * sizeof(int));
-  if (ce == cudaSuccess) ce = up(e->K_.val_orig, kval.data(), nb * sizeof(double));
-  if (ce == cudaSuccess) ce = up(e->Kt_.ptr, tptr.data(), tptr.size() * sizeof(int));
-  if (ce == cudaSuccess) ce = up(e->Kt_.idx, rowidx, nb * sizeof(int));
-  if (ce == cudaSuccess) ce = up(e->Kt_.val_orig, val, nb * sizeof(double));
-  if (ce == cudaSuccess) ce = up(e->cost_orig_, cost, nt * sizeof(double));
-  if (ce == cudaSuccess) ce = up(e->lower_orig_, lower, nt * sizeof(double));
-  if (ce == cudaSuccess) ce = up(e->upper_orig_, upper, nt * sizeof(double));
-  std::vector<double> u0 = power_start(m);
-  if (ce == cudaSuccess) ce = up(e->u0_, u0.data(), u0.size() * sizeof(double));
-  {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&e->sm_count_, cudaDevAttrMultiProcessorCount, dev);
-  }
-  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
-  if (ce != cudaSuccess) {
-    if (err) *err = std::string("upload: ") + cudaGetErrorString(ce);
-    const int code = ce == cudaErrorMemoryAllocation ? kErrOutOfMemory : kErrCuda;
-    delete e;
-    return code;
-  }
-  {
-    std::vector<char> inert(static_cast<size_t>(m));
-    for (int i = 0; i < m; ++i) {
-      inert[i] = kptr[i + 1] == kptr[i] && cost[n + i] == 0.0 && lower[n + i] <= 0.0 &&
-                 upper[n + i] >= 0.0;
-    }
-    rc = e->set_active_rows(inert, &why);
-  }
-  if (rc == kOk) rc = e->find_neighbours(&why);
-  // Tiles of both operators (tuned or by the built-in rule), then the grids.
-  if (rc == kOk) rc = e->tune_tiles(&why);
-  if (rc != kOk) {
-    if (err) *err = why;
-    delete e;
-    return rc;
-  }
-  *out = e;
-  return kOk;
-}
 
 int Engine::create_from_device(Engine** out, const DeviceLp& d, const Options& opt,
                                std::string* err) {
@@ -937,6 +774,23 @@ int Engine::tune_tiles(std::string* err) {
   return kOk;
 }
 
+namespace {
+
+// Lays buffers out in one allocation (256-byte aligned): a first pass with no base only sums
+// the sizes, a second assigns the pointers in the same order.
+struct Carver {
+  char* base = nullptr;
+  size_t used = 0;
+  template <typename T>
+  void take(T** p, size_t count) {
+    used = (used + 255) & ~static_cast<size_t>(255);
+    *p = base != nullptr ? reinterpret_cast<T*>(base + used) : nullptr;
+    used += std::max<size_t>(count, 1) * sizeof(T);
+  }
+};
+
+}  // namespace
+
 int Engine::alloc_all(std::string* err) {
   const size_t nt = static_cast<size_t>(n_) + m_;
   const size_t m = static_cast<size_t>(m_);
@@ -945,62 +799,73 @@ int Engine::alloc_all(std::string* err) {
   for (auto& ev : ev_) SG_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   // The nonzero arrays carry kSegPad zeroed elements after the last nonzero: a staged segment's
   // bulk copies end at the 4-aligned position above it.
+  auto layout = [&](Carver& c) {
+    for (DevOp* op : {&K_, &Kt_}) {
+      c.take(&op->ptr, static_cast<size_t>(op->rows) + 1);
+      c.take(&op->idx, nb + kSegPad);
+      c.take(&op->val, nb + kSegPad);
+      c.take(&op->val_orig, nb + kSegPad);
+      if (fp32_) c.take(&op->val32, nb + kSegPad);
+    }
+    c.take(&wait_error_, 1);
+    for (double** p : {&it64_.V[0], &it64_.V[1], &it64_.Vbar, &it64_.Verg, &it64_.Vrst,
+                       &it64_.cost, &it64_.lower, &it64_.upper}) {
+      c.take(p, nt);
+    }
+    for (double** p : {&it64_.Y[0], &it64_.Y[1], &it64_.Yerg, &it64_.Yrst, &it64_.rhs}) {
+      c.take(p, m);
+    }
+    if (fp32_) {
+      for (float** p : {&it32_.V[0], &it32_.V[1], &it32_.Vbar, &it32_.Verg, &it32_.Vrst,
+                        &it32_.cost, &it32_.lower, &it32_.upper}) {
+        c.take(p, nt);
+      }
+      for (float** p : {&it32_.Y[0], &it32_.Y[1], &it32_.Yerg, &it32_.Yrst, &it32_.rhs}) {
+        c.take(p, m);
+      }
+      for (double** p : {&cost_in_, &lower_in_, &upper_in_, &dvec_}) c.take(p, nt);
+      for (double** p : {&rhs_in_, &bh_, &ones_m_}) c.take(p, m);
+      c.take(&ones_n_, static_cast<size_t>(n_));
+      c.take(&ctl32_, 1);
+    }
+    for (double** p : {&cost_orig_, &lower_orig_, &upper_orig_, &cost_ev_, &lower_ev_,
+                       &upper_ev_, &x_out_, &scratch_n_}) {
+      c.take(p, nt);
+    }
+    for (double** p : {&rhs_ev_, &rs_, &rn_, &pu_, &u0_, &y_out_, &ray_out_}) c.take(p, m);
+    for (double** p : {&cs_, &cn_, &pv_, &inv_cs_}) c.take(p, static_cast<size_t>(n_));
+    c.take(&inv_rs_, m);
+    c.take(&partial_, static_cast<size_t>(4096) * kMaxSums);
+    c.take(&counter_, 8);
+    c.take(&ctl_, 1);
+  };
+  {
+    Carver sizing;
+    layout(sizing);
+    SG_TRY(cudaMalloc(reinterpret_cast<void**>(&arena_), sizing.used));
+    arena_bytes_ = sizing.used;
+    Carver carve;
+    carve.base = arena_;
+    layout(carve);
+  }
   for (DevOp* op : {&K_, &Kt_}) {
-    SG_TRY(dalloc(&op->ptr, static_cast<size_t>(op->rows) + 1));
-    SG_TRY(dalloc(&op->idx, nb + kSegPad));
-    SG_TRY(dalloc(&op->val, nb + kSegPad));
-    SG_TRY(dalloc(&op->val_orig, nb + kSegPad));
     SG_TRY(cudaMemsetAsync(op->idx + nb, 0, kSegPad * sizeof(int), stream_));
     SG_TRY(cudaMemsetAsync(op->val + nb, 0, kSegPad * sizeof(double), stream_));
     SG_TRY(cudaMemsetAsync(op->val_orig + nb, 0, kSegPad * sizeof(double), stream_));
-    if (fp32_) {
-      SG_TRY(dalloc(&op->val32, nb + kSegPad));
-      SG_TRY(cudaMemsetAsync(op->val32 + nb, 0, kSegPad * sizeof(float), stream_));
-    }
+    if (fp32_) SG_TRY(cudaMemsetAsync(op->val32 + nb, 0, kSegPad * sizeof(float), stream_));
   }
-  SG_TRY(dalloc(&wait_error_, 1));
   SG_TRY(cudaMemsetAsync(wait_error_, 0, sizeof(int), stream_));
   K_.wait_error = wait_error_;
   Kt_.wait_error = wait_error_;
-  for (double** p : {&it64_.V[0], &it64_.V[1], &it64_.Vbar, &it64_.Verg, &it64_.Vrst,
-                     &it64_.cost, &it64_.lower, &it64_.upper}) {
-    SG_TRY(dalloc(p, nt));
-  }
-  for (double** p : {&it64_.Y[0], &it64_.Y[1], &it64_.Yerg, &it64_.Yrst, &it64_.rhs}) {
-    SG_TRY(dalloc(p, m));
-  }
   if (fp32_) {
-    for (float** p : {&it32_.V[0], &it32_.V[1], &it32_.Vbar, &it32_.Verg, &it32_.Vrst,
-                      &it32_.cost, &it32_.lower, &it32_.upper}) {
-      SG_TRY(dalloc(p, nt));
-    }
-    for (float** p : {&it32_.Y[0], &it32_.Y[1], &it32_.Yerg, &it32_.Yrst, &it32_.rhs}) {
-      SG_TRY(dalloc(p, m));
-    }
-    for (double** p : {&cost_in_, &lower_in_, &upper_in_, &dvec_}) SG_TRY(dalloc(p, nt));
-    for (double** p : {&rhs_in_, &bh_, &ones_m_}) SG_TRY(dalloc(p, m));
-    SG_TRY(dalloc(&ones_n_, static_cast<size_t>(n_)));
-    {
-      std::vector<double> ones(std::max<size_t>(std::max<size_t>(m, n_), 1), 1.0);
-      SG_TRY(cudaMemcpy(ones_n_, ones.data(), static_cast<size_t>(n_) * sizeof(double),
-                        cudaMemcpyHostToDevice));
-      SG_TRY(cudaMemcpy(ones_m_, ones.data(), m * sizeof(double), cudaMemcpyHostToDevice));
-    }
-    SG_TRY(dalloc(&ctl32_, 1));
+    std::vector<double> ones(std::max<size_t>(std::max<size_t>(m, n_), 1), 1.0);
+    SG_TRY(cudaMemcpy(ones_n_, ones.data(), static_cast<size_t>(n_) * sizeof(double),
+                      cudaMemcpyHostToDevice));
+    SG_TRY(cudaMemcpy(ones_m_, ones.data(), m * sizeof(double), cudaMemcpyHostToDevice));
     SG_TRY(cudaMemsetAsync(ctl32_, 0, sizeof(Ctl), stream_));
     configure_refine_kernels();
   }
-  for (double** p : {&cost_orig_, &lower_orig_, &upper_orig_, &cost_ev_, &lower_ev_, &upper_ev_,
-                     &x_out_, &scratch_n_}) {
-    SG_TRY(dalloc(p, nt));
-  }
-  for (double** p : {&rhs_ev_, &rs_, &rn_, &pu_, &u0_, &y_out_, &ray_out_}) SG_TRY(dalloc(p, m));
-  for (double** p : {&cs_, &cn_, &pv_, &inv_cs_}) SG_TRY(dalloc(p, static_cast<size_t>(n_)));
-  SG_TRY(dalloc(&inv_rs_, m));
-  SG_TRY(dalloc(&partial_, static_cast<size_t>(4096) * kMaxSums));
-  SG_TRY(dalloc(&counter_, 8));
   SG_TRY(cudaMemsetAsync(counter_, 0, 8 * sizeof(unsigned), stream_));
-  SG_TRY(dalloc(&ctl_, 1));
   SG_TRY(cudaMemsetAsync(ctl_, 0, sizeof(Ctl), stream_));
   SG_TRY(cudaHostAlloc(reinterpret_cast<void**>(&ctl_host_), sizeof(Ctl), cudaHostAllocDefault));
   memset(ctl_host_, 0, sizeof(Ctl));

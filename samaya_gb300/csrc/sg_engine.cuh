@@ -200,12 +200,9 @@ class Engine {
  public:
   ~Engine();
 
-  // Uploads the LpProblem (A as CSC m x n, cost/lower/upper n + m) and builds both operators.
-  static int create(Engine** out, int m, int n, const int64_t* colptr, const int32_t* rowidx,
-                    const double* val, const double* cost, const double* lower,
-                    const double* upper, const Options& opt, std::string* err);
-  // The same from an LpProblem built in device memory (copied device to device; the caller
-  // keeps its buffers).
+  // Builds both operators from an LpProblem in device memory (A by columns and by rows,
+  // cost/lower/upper n + m; copied device to device, the caller keeps its buffers). The host
+  // entry points (create_engine_from_lp, create_engine_from_model) build that problem.
   static int create_from_device(Engine** out, const DeviceLp& lp, const Options& opt,
                                 std::string* err);
 
@@ -340,6 +337,10 @@ class Engine {
   unsigned* counter_ = nullptr;
   double* long_terms_ = nullptr;
   Ctl* ctl_ = nullptr;
+  // One device allocation holding every buffer whose size the problem fixes (operators,
+  // iterates, problem vectors, control blocks): one cudaMalloc and one cudaFree per engine.
+  char* arena_ = nullptr;
+  size_t arena_bytes_ = 0;
   Ctl* ctl_host_ = nullptr;       // pinned
   cudaStream_t stream_ = nullptr;
   cudaGraphExec_t chunk_exec_ = nullptr;

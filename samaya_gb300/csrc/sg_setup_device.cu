@@ -23,6 +23,7 @@
 #include <cub/device/device_scan.cuh>
 
 #include "../../include/sg_pdlp.h"
+#include "sg_transpose.h"
 
 namespace sg {
 
@@ -45,9 +46,10 @@ __device__ __forceinline__ double clamp_scale(double v) {
 }
 
 // The column of every nonzero (thread per column).
-__global__ void column_of_kernel(int n, const int64_t* __restrict__ cp, int32_t* __restrict__ col) {
+template <typename P>
+__global__ void column_of_kernel(int n, const P* __restrict__ cp, int32_t* __restrict__ col) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-    for (int64_t p = cp[j]; p < cp[j + 1]; ++p) col[p] = j;
+    for (P p = cp[j]; p < cp[j + 1]; ++p) col[p] = j;
   }
 }
 
@@ -735,6 +737,177 @@ int create_engine_from_model(Engine** out, const ModelView& mv, const Options& o
         }
         rc = Engine::create_from_device(out, lp, opt, err);
       }
+    }
+  }
+  cudaStreamDestroy(s);
+  return rc;
+}
+
+// An engine for an LpProblem on the host (sg_pdlp_create's arguments) with the row-major copy
+// of A built on the device: the input is checked on the host (row indices and values by up to 16
+// threads), the column starts (as int32), row indices, values and vectors are uploaded once, and
+// the nonzeros are sorted by row with CUB's stable radix sort. The same CSR as the host's counting sort (stable in both), so the
+// same bits in every solve; the host keeps only O(m + n) work.
+int create_engine_from_lp(Engine** out, int m, int n, const int64_t* colptr,
+                          const int32_t* rowidx, const double* val, const double* cost,
+                          const double* lower, const double* upper, const Options& opt,
+                          std::string* err) {
+  *out = nullptr;
+  if (m < 0 || n < 0 || colptr == nullptr || cost == nullptr || lower == nullptr ||
+      upper == nullptr) {
+    if (err) *err = "invalid argument";
+    return kErrInvalidArgument;
+  }
+  const long long nnz = colptr[n];
+  if (nnz < 0 || colptr[0] != 0) {
+    if (err) *err = "column starts must begin at 0";
+    return kErrInvalidArgument;
+  }
+  if (nnz >= static_cast<long long>(std::numeric_limits<int>::max()) ||
+      static_cast<long long>(n) + m >= std::numeric_limits<int>::max()) {
+    if (err) *err = "matrix too large for 32-bit offsets";
+    return kErrTooLarge;
+  }
+  if (nnz > 0 && (rowidx == nullptr || val == nullptr)) {
+    if (err) *err = "null matrix arrays";
+    return kErrInvalidArgument;
+  }
+  DeviceLp lp;
+  lp.m = m;
+  lp.n = n;
+  lp.nnz = nnz;
+  lp.tptr_host.resize(static_cast<size_t>(n) + 1);
+  for (int j = 0; j < n; ++j) {
+    if (colptr[j + 1] < colptr[j]) {
+      if (err) *err = "column starts must not decrease";
+      return kErrInvalidArgument;
+    }
+    lp.tptr_host[j] = static_cast<int>(colptr[j]);
+  }
+  lp.tptr_host[n] = static_cast<int>(nnz);
+  const long long nt = static_cast<long long>(n) + m;
+  for (long long k = 0; k < nt; ++k) {
+    if (!std::isfinite(cost[k]) || std::isnan(lower[k]) || std::isnan(upper[k])) {
+      if (err) *err = "cost or bound not valid";
+      return kErrInvalidArgument;
+    }
+  }
+  if (nnz > 0) {
+    const char* why = nullptr;
+    if (check_nonzeros(m, nnz, rowidx, val, 16, &why) != 0) {
+      if (err) *err = why;
+      return kErrInvalidArgument;
+    }
+  }
+  if (device_info(nullptr, nullptr, nullptr, 0) != kOk) {
+    if (err) *err = "no sm_103 GPU";
+    return kErrNoDevice;
+  }
+  cudaStream_t s = nullptr;
+  SG_DEV(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  int rc = kOk;
+  {
+    Buffers t;
+    int* tptr = nullptr;
+    int32_t* row = nullptr;
+    double* v = nullptr;
+    double* c = nullptr;
+    double* lo = nullptr;
+    double* up = nullptr;
+    int* col = nullptr;
+    int* keys = nullptr;
+    int* perm_in = nullptr;
+    int* perm = nullptr;
+    int* kptr = nullptr;
+    int* kidx = nullptr;
+    double* kval = nullptr;
+    cudaError_t e = cudaSuccess;
+    auto step = [&](cudaError_t x) {
+      if (e == cudaSuccess) e = x;
+    };
+    const size_t nb = static_cast<size_t>(nnz);
+    step(t.get(&tptr, static_cast<size_t>(n) + 1));
+    step(t.get(&row, nb));
+    step(t.get(&v, nb));
+    step(t.get(&c, static_cast<size_t>(nt)));
+    step(t.get(&lo, static_cast<size_t>(nt)));
+    step(t.get(&up, static_cast<size_t>(nt)));
+    step(t.get(&col, nb));
+    step(t.get(&keys, nb));
+    step(t.get(&perm_in, nb));
+    step(t.get(&perm, nb));
+    step(t.get(&kptr, static_cast<size_t>(m) + 1));
+    step(t.get(&kidx, nb));
+    step(t.get(&kval, nb));
+    if (e == cudaSuccess) {
+      step(cudaMemcpyAsync(tptr, lp.tptr_host.data(), (static_cast<size_t>(n) + 1) * sizeof(int),
+                           cudaMemcpyHostToDevice, s));
+      if (nb > 0) {
+        step(cudaMemcpyAsync(row, rowidx, nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        step(cudaMemcpyAsync(v, val, nb * sizeof(double), cudaMemcpyHostToDevice, s));
+      }
+      if (nt > 0) {
+        step(cudaMemcpyAsync(c, cost, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+        step(cudaMemcpyAsync(lo, lower, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+        step(cudaMemcpyAsync(up, upper, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+      }
+    }
+    // The row-major copy: a stable sort of the nonzeros by row.
+    if (e == cudaSuccess && rc == kOk && nnz > 0) {
+      if (n > 0) column_of_kernel<<<grid_for(n), kT, 0, s>>>(n, tptr, col);
+      iota_kernel<<<grid_for(nnz), kT, 0, s>>>(static_cast<int>(nnz), perm_in);
+      int bits = 1;
+      while (bits < 31 && (1LL << bits) <= m) ++bits;
+      size_t temp = 0;
+      step(cub::DeviceRadixSort::SortPairs(nullptr, temp, row, keys, perm_in, perm,
+                                           static_cast<int>(nnz), 0, bits, s));
+      char* tmp = nullptr;
+      step(t.get(&tmp, temp));
+      step(cub::DeviceRadixSort::SortPairs(tmp, temp, row, keys, perm_in, perm,
+                                           static_cast<int>(nnz), 0, bits, s));
+      gather_rows_kernel<<<grid_for(nnz), kT, 0, s>>>(static_cast<int>(nnz), perm, col, v, kidx,
+                                                      kval);
+      step(cudaGetLastError());
+    }
+    if (e == cudaSuccess && rc == kOk) {
+      row_starts_kernel<<<grid_for(static_cast<long long>(m) + 1), kT, 0, s>>>(
+          m, static_cast<int>(nnz), keys, kptr);
+      step(cudaGetLastError());
+      lp.kptr_host.resize(static_cast<size_t>(m) + 1);
+      step(cudaMemcpyAsync(lp.kptr_host.data(), kptr, lp.kptr_host.size() * sizeof(int),
+                           cudaMemcpyDeviceToHost, s));
+      step(cudaStreamSynchronize(s));
+    }
+    if (e != cudaSuccess) {
+      if (err) *err = std::string("device setup: ") + cudaGetErrorString(e);
+      rc = e == cudaErrorMemoryAllocation ? kErrOutOfMemory : kErrCuda;
+    }
+    if (rc == kOk) {
+      // Inert rows and shared column bounds from the host's vectors (as Engine::create_from_device
+      // expects them).
+      lp.row_inert.resize(static_cast<size_t>(m));
+      for (int i = 0; i < m; ++i) {
+        lp.row_inert[i] = lp.kptr_host[i + 1] == lp.kptr_host[i] && cost[n + i] == 0.0 &&
+                          lower[n + i] <= 0.0 && upper[n + i] >= 0.0;
+      }
+      if (n > 0) {
+        const double l0 = lower[0], u0 = upper[0];
+        bool uniform = (l0 == 0.0 || l0 == -INFINITY) && (u0 == 0.0 || u0 == INFINITY);
+        for (int j = 1; uniform && j < n; ++j) uniform = lower[j] == l0 && upper[j] == u0;
+        lp.x_uniform = uniform;
+        lp.x_lo = l0;
+        lp.x_hi = u0;
+      }
+      lp.kptr = kptr;
+      lp.kidx = kidx;
+      lp.kval = kval;
+      lp.tptr = tptr;
+      lp.tidx = row;
+      lp.tval = v;
+      lp.cost = c;
+      lp.lower = lo;
+      lp.upper = up;
+      rc = Engine::create_from_device(out, lp, opt, err);
     }
   }
   cudaStreamDestroy(s);

@@ -32,6 +32,13 @@ int scale_model_device(const ModelView& mv, int64_t* lp_colptr, int32_t* lp_rowi
                        double* lp_val, double* cost, double* lower, double* upper,
                        double* col_scale, double* row_scale, int64_t* lp_nnz, std::string* err);
 
+// An engine for an LpProblem on the host (the arguments of sg_pdlp_create), the row-major copy
+// of A built on the device.
+int create_engine_from_lp(Engine** out, int m, int n, const int64_t* colptr,
+                          const int32_t* rowidx, const double* val, const double* cost,
+                          const double* lower, const double* upper, const Options& opt,
+                          std::string* err);
+
 // An engine for the model's LpProblem, built on the device without a host round trip of the
 // scaled matrix or a host transpose; the scale factors are copied out (either may be null).
 int create_engine_from_model(Engine** out, const ModelView& mv, const Options& opt,

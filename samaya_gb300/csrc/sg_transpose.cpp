@@ -115,6 +115,36 @@ int csc_to_csr(int m, int n, const int64_t* colptr, const int32_t* rowidx, const
   return 0;
 }
 
+int check_nonzeros(int m, long long nnz, const int32_t* rowidx, const double* val,
+                   int max_threads, const char** why) {
+  int threads = static_cast<int>(std::min<long long>(nnz / (1LL << 19) + 1, 16));
+  threads = std::min(threads, std::max(1, max_threads));
+  const unsigned hw = std::thread::hardware_concurrency();
+  if (hw > 0) threads = std::min(threads, static_cast<int>(hw));
+  threads = std::max(threads, 1);
+  std::atomic<int> bad_row{0}, bad_val{0};
+  parallel_for(threads, [&](int t) {
+    const long long p0 = nnz * t / threads;
+    const long long p1 = nnz * (t + 1) / threads;
+    int br = 0, bv = 0;
+    for (long long p = p0; p < p1; ++p) {
+      br |= rowidx[p] < 0 || rowidx[p] >= m;
+      bv |= !std::isfinite(val[p]);
+    }
+    if (br) bad_row.store(1);
+    if (bv) bad_val.store(1);
+  });
+  if (bad_row.load()) {
+    *why = "row index out of range";
+    return 1;
+  }
+  if (bad_val.load()) {
+    *why = "matrix value not finite";
+    return 1;
+  }
+  return 0;
+}
+
 }  // namespace sg
 
 extern "C" {

@@ -12,4 +12,9 @@ namespace sg {
 int csc_to_csr(int m, int n, const int64_t* colptr, const int32_t* rowidx, const double* val,
                int* kptr, int* kidx, double* kval, int max_threads, const char** why);
 
+// Every row index in [0, m) and every value finite: returns 0, or 1 with `why` set. Uses up to
+// max_threads host threads.
+int check_nonzeros(int m, long long nnz, const int32_t* rowidx, const double* val,
+                   int max_threads, const char** why);
+
 }  // namespace sg

@@ -211,10 +211,12 @@ class PdlpSolver:
                               setup_seconds=r.setup_seconds, solve_seconds=r.solve_seconds,
                               step_size=r.step_size, primal_weight=r.primal_weight,
                               kernel_launches=r.kernel_launches, device_ms=r.device_ms)
-        x = x_out if x_out is not None else np.zeros(lp.n + lp.m)
-        y = y_out if y_out is not None else np.zeros(max(lp.m, 1))
-        dr = np.zeros(max(lp.m, 1))
-        pr = np.zeros(max(lp.n, 1))
+        # The engine writes every entry of x and y; a ray only with its flag set (copied out
+        # below), so none of these needs zeroing.
+        x = x_out if x_out is not None else np.empty(lp.n + lp.m)
+        y = y_out if y_out is not None else np.empty(max(lp.m, 1))
+        dr = np.empty(max(lp.m, 1))
+        pr = np.empty(max(lp.n, 1))
         r = _native.Result()
         _native.check(self._lib.sg_pdlp_solve(self._h, ctypes.byref(r), _ptr(x, ctypes.c_double),
                                               _ptr(y, ctypes.c_double), _ptr(dr, ctypes.c_double),
