@@ -37,11 +37,7 @@ struct Tile {
   int team;  // kind 2: warps per row (1, 2, 4 or 8); 1 otherwise
   int seg, nseg;
   int lrow;
-  // kind 1: 1 when the row holds at least a quarter of the columns, so that consecutive
-  // nonzeros gather neighbouring entries: the CTA's threads then take consecutive nonzeros
-  // (thread t: k0 + t + 256 i) and a warp's gather reads a few sectors instead of 32.
-  int dense;
-  int pad[2];
+  int pad[3];
 };
 
 struct TileSet {

@@ -504,14 +504,6 @@ int Engine::set_tiles(DevOp* op, const TileShape& shape) {
   int nlong = 0;
   build_tiles(op->host_ptr, shape.cap_nnz, shape.cap_rows, shape.warp_min, shape.split, &tiles,
               &nlong);
-  // Segments of rows holding at least a quarter of the columns take the dense layout.
-  auto mark_dense = [op](std::vector<Tile>* ts, const std::vector<int>& p) {
-    for (Tile& t : *ts) {
-      const long long len = p[t.r0 + 1] - p[t.r0];
-      t.dense = t.kind == 1 && 4 * len >= op->cols ? 1 : 0;
-    }
-  };
-  mark_dense(&tiles, op->host_ptr);
   const bool grouped =
       shape.groups != 0 && op == &K_ && !op->host_adj.empty() && opt_.row_groups >= 0;
   const bool staged = shape.staged != 0 && op == &K_ && opt_.segment_staging >= 0;
@@ -541,7 +533,6 @@ int Engine::set_tiles(DevOp* op, const TileShape& shape) {
     build_tiles(vp, shape.cap_nnz, shape.cap_rows, shape.warp_min, shape.split, &st_tiles,
                 &st_nlong, grouped ? &vadj : nullptr,
                 grouped ? group_positions(shape.cap_nnz) : 0);
-    mark_dense(&st_tiles, vp);
     for (const Tile& t : st_tiles) {
       st_groups += t.kind == 3;
       st_staged |= staged && t.kind == 1 ? 1 : 0;

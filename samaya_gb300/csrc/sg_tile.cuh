@@ -582,18 +582,6 @@ __device__ __forceinline__ void run_tiles(const TileSet& ts, const int* __restri
           staged_done = true;
         }
       }
-      if (!staged_done && tile.dense) {
-        // A dense row: thread t takes nonzeros k0 + t, k0 + t + 256, ... (a warp's loads and
-        // gathers cover 32 consecutive nonzeros, neighbouring columns), 8 in flight.
-#pragma unroll 8
-        for (int q = tile.k0 + tid; q < tile.k1; q += kBlock) {
-          const T a = ldg(val + q);
-          const int j = ldg(idx + q);
-#pragma unroll
-          for (int v = 0; v < NV; ++v) s[v] = combine<MAXRED>(s[v], prod(v, a, j));
-        }
-        staged_done = true;
-      }
       if (!staged_done) {
         // Head up to a 4-aligned position, then 16-byte loads of four nonzeros per thread,
         // then the tail (scalar).
