@@ -777,18 +777,13 @@ int create_engine_from_lp(Engine** out, int m, int n, const int64_t* colptr,
   lp.n = n;
   lp.nnz = nnz;
   lp.tptr_host.resize(static_cast<size_t>(n) + 1);
-  for (int j = 0; j < n; ++j) {
-    if (colptr[j + 1] < colptr[j]) {
-      if (err) *err = "column starts must not decrease";
-      return kErrInvalidArgument;
-    }
-    lp.tptr_host[j] = static_cast<int>(colptr[j]);
-  }
-  lp.tptr_host[n] = static_cast<int>(nnz);
   const long long nt = static_cast<long long>(n) + m;
-  for (long long k = 0; k < nt; ++k) {
-    if (!std::isfinite(cost[k]) || std::isnan(lower[k]) || std::isnan(upper[k])) {
-      if (err) *err = "cost or bound not valid";
+  bool shared_bounds = false;
+  {
+    const char* why = nullptr;
+    if (check_columns(m, n, colptr, cost, lower, upper, lp.tptr_host.data(), &shared_bounds, 16,
+                      &why) != 0) {
+      if (err) *err = why;
       return kErrInvalidArgument;
     }
   }
@@ -892,9 +887,8 @@ int create_engine_from_lp(Engine** out, int m, int n, const int64_t* colptr,
       }
       if (n > 0) {
         const double l0 = lower[0], u0 = upper[0];
-        bool uniform = (l0 == 0.0 || l0 == -INFINITY) && (u0 == 0.0 || u0 == INFINITY);
-        for (int j = 1; uniform && j < n; ++j) uniform = lower[j] == l0 && upper[j] == u0;
-        lp.x_uniform = uniform;
+        lp.x_uniform = shared_bounds && (l0 == 0.0 || l0 == -INFINITY) &&
+                       (u0 == 0.0 || u0 == INFINITY);
         lp.x_lo = l0;
         lp.x_hi = u0;
       }

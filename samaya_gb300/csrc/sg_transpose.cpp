@@ -145,6 +145,47 @@ int check_nonzeros(int m, long long nnz, const int32_t* rowidx, const double* va
   return 0;
 }
 
+int check_columns(int m, int n, const int64_t* colptr, const double* cost, const double* lower,
+                  const double* upper, int* tptr, bool* shared, int max_threads,
+                  const char** why) {
+  const long long nt = static_cast<long long>(n) + m;
+  int threads = static_cast<int>(std::min<long long>(nt / (1LL << 18) + 1, 16));
+  threads = std::min(threads, std::max(1, max_threads));
+  const unsigned hw = std::thread::hardware_concurrency();
+  if (hw > 0) threads = std::min(threads, static_cast<int>(hw));
+  threads = std::max(threads, 1);
+  std::atomic<int> bad_start{0}, bad_vec{0}, differ{0};
+  const double l0 = n > 0 ? lower[0] : 0.0;
+  const double u0 = n > 0 ? upper[0] : 0.0;
+  parallel_for(threads, [&](int t) {
+    const long long k0 = nt * t / threads;
+    const long long k1 = nt * (t + 1) / threads;
+    int bs = 0, bv = 0, df = 0;
+    for (long long k = k0; k < k1; ++k) {
+      if (k < n) {
+        bs |= colptr[k + 1] < colptr[k];
+        tptr[k] = static_cast<int>(colptr[k]);
+        df |= !(lower[k] == l0 && upper[k] == u0);
+      }
+      bv |= !std::isfinite(cost[k]) || std::isnan(lower[k]) || std::isnan(upper[k]);
+    }
+    if (bs) bad_start.store(1);
+    if (bv) bad_vec.store(1);
+    if (df) differ.store(1);
+  });
+  tptr[n] = static_cast<int>(colptr[n]);
+  *shared = n > 0 && differ.load() == 0;
+  if (bad_start.load()) {
+    *why = "column starts must not decrease";
+    return 1;
+  }
+  if (bad_vec.load()) {
+    *why = "cost or bound not valid";
+    return 1;
+  }
+  return 0;
+}
+
 }  // namespace sg
 
 extern "C" {

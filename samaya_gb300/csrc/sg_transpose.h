@@ -12,6 +12,13 @@ namespace sg {
 int csc_to_csr(int m, int n, const int64_t* colptr, const int32_t* rowidx, const double* val,
                int* kptr, int* kidx, double* kval, int max_threads, const char** why);
 
+// Column starts non-decreasing (and copied to int32 `tptr`, n + 1), every cost finite and no
+// bound NaN (n + m entries): returns 0, or 1 with `why` set; *shared is set when every
+// structural column has the first column's bounds. Uses up to max_threads host threads.
+int check_columns(int m, int n, const int64_t* colptr, const double* cost, const double* lower,
+                  const double* upper, int* tptr, bool* shared, int max_threads,
+                  const char** why);
+
 // Every row index in [0, m) and every value finite: returns 0, or 1 with `why` set. Uses up to
 // max_threads host threads.
 int check_nonzeros(int m, long long nnz, const int32_t* rowidx, const double* val,
