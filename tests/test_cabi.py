@@ -63,6 +63,32 @@ def test_invalid_problems_are_rejected_before_any_device_work():
                             _p(v, ctypes.c_double), _p(v, ctypes.c_double),
                             _p(v, ctypes.c_double), None)
     assert rc == -1
+    assert b"column starts" in lib.sg_pdlp_last_error()
+    # A cost that is not finite, a bound that is NaN (structural or logical).
+    for arr, k, value in (("cost", 1, np.inf), ("lower", 3, np.nan), ("upper", 0, np.nan)):
+        vecs = {"cost": np.zeros(4), "lower": np.zeros(4), "upper": np.zeros(4)}
+        vecs[arr][k] = value
+        rc = lib.sg_pdlp_create(ctypes.byref(h), 2, 2, _p(colptr, ctypes.c_int64),
+                                _p(rowidx, ctypes.c_int32), _p(vals, ctypes.c_double),
+                                _p(vecs["cost"], ctypes.c_double),
+                                _p(vecs["lower"], ctypes.c_double),
+                                _p(vecs["upper"], ctypes.c_double), None)
+        assert rc == -1 and not h.value
+        assert b"cost or bound" in lib.sg_pdlp_last_error()
+    # The row-index and value checks run on several host threads: a bad entry near the end of
+    # a large matrix is found too.
+    nnz = 3_000_000
+    big_ptr = np.arange(0, nnz + 1, 3, dtype=np.int64)
+    big_rows = np.tile(np.array([0, 1, 2], dtype=np.int32), nnz // 3)
+    big_vals = np.ones(nnz)
+    big_rows[-2] = 7
+    nb = len(big_ptr) - 1
+    zero = np.zeros(nb + 3)
+    rc = lib.sg_pdlp_create(ctypes.byref(h), 3, nb, _p(big_ptr, ctypes.c_int64),
+                            _p(big_rows, ctypes.c_int32), _p(big_vals, ctypes.c_double),
+                            _p(zero, ctypes.c_double), _p(zero, ctypes.c_double),
+                            _p(zero, ctypes.c_double), None)
+    assert rc == -1 and b"row index" in lib.sg_pdlp_last_error()
     assert lib.sg_pdlp_solve(None, None, None, None, None, None) == -1
     lib.sg_pdlp_destroy(None)
 
