@@ -138,7 +138,10 @@ int sg_pdlp_available(int* cc_major, int* cc_minor, char* name, size_t name_len)
 
 /* Uploads an LpProblem and prepares the engine. Replaces gpu::PdhgDevice::create (reference
  * src/gpu/pdhg_core.cu:242-273) for the solve_pdlp path: the matrix given here is the
- * LpProblem's A before PDLP's own equilibration, which the engine performs on the device.
+ * LpProblem's A before PDLP's own equilibration, which the engine performs on the device. The
+ * input is checked on the host first (SG_ERR_INVALID_ARGUMENT for decreasing column starts, a
+ * row index out of range, a value or cost that is not finite, a NaN bound); the row-major
+ * copy of A is then built on the device (a stable sort by row: the CSR sg_csc_to_csr gives).
  * Matrices with 2^31 - 1 or more nonzeros are refused (SG_ERR_TOO_LARGE), as the reference
  * refuses them (pdhg_core.cu:176-178). */
 int sg_pdlp_create(sg_pdlp** handle, int m, int n, const int64_t* a_colptr,
