@@ -718,11 +718,23 @@ int Engine::tune_tiles(std::string* err) {
           cands.push_back(g);
         }
       }
+      // Candidates that differ from the tiles in place only in the kernel variant reuse them
+      // (the partition does not depend on the variant).
+      bool built = false;
+      TileShape in_place;
       for (const TileShape& sh : cands) {
-        const int rc = set_tiles(op, sh);
-        if (rc != kOk) {
-          if (err) *err = "autotune: tile upload failed";
-          return rc;
+        if (built && sh.cap_nnz == in_place.cap_nnz && sh.cap_rows == in_place.cap_rows &&
+            sh.warp_min == in_place.warp_min && sh.split == in_place.split &&
+            sh.groups == in_place.groups && sh.staged == in_place.staged) {
+          op->variant = sh.variant;
+        } else {
+          const int rc = set_tiles(op, sh);
+          if (rc != kOk) {
+            if (err) *err = "autotune: tile upload failed";
+            return rc;
+          }
+          built = true;
+          in_place = sh;
         }
         double ms = -1.0;
         for (int round = 0; round < 3; ++round) {
