@@ -12,6 +12,7 @@ reference's CPU PDLP (the oracle port, 1 core) on a bounded run of the same LP.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
     python bench.py --workload powerlaw|random|batchA|batchB|diff   (the other configurations)
+    python bench.py --workload mps      (the MPS reader on the transportation LP's 93 MB file)
 
 With N > 1 (torchrun) every rank solves its own replica (replicas only; no collective on the
 data path); the time is the max over ranks.
@@ -71,10 +72,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="transport",
-                    choices=["transport", "powerlaw", "random", "batchA", "batchB", "diff"],
+                    choices=["transport", "powerlaw", "random", "batchA", "batchB", "diff", "mps"],
                     help="transport (the headline), powerlaw, random (2000 x 5000): one LP to "
                          "1e-8; batchA / batchB: LPs/s of the batched engine against sequential "
-                         "solves; diff: the differentiable layer's forward and backward")
+                         "solves; diff: the differentiable layer's forward and backward; mps: "
+                         "the fast MPS reader on the transportation LP's file")
     ap.add_argument("--precision", default="auto",
                     choices=["auto", "mixed", "refined", "fp64"],
                     help="mixed: FP32 PDLP then FP64 PDLP from its answer; refined: FP32 "
@@ -416,10 +418,125 @@ def run_diff(args):
     return _device_clock_line(line, clk)
 
 
+MPS_WORKLOAD = ("transportation LP 1000 supplies x 2000 demands as a free-MPS file (3,000 rows, "
+                "2,000,000 columns, 4,000,000 entries, two entries to a line)")
+
+
+def mps_file():
+    """The transportation LP written as free MPS into a temporary directory (and read once, so
+    that the timed reads come from the page cache). Returns (path, bytes, directory)."""
+    import tempfile
+    from samaya_gb300 import generators as g
+    from samaya_gb300.mps import write_mps
+    tmp = tempfile.mkdtemp(prefix="sg_mps_")
+    path = os.path.join(tmp, "transport.mps")
+    write_mps(g.transportation_lp(1000, 2000, seed=0), path)
+    with open(path, "rb") as f:
+        while f.read(1 << 24):
+            pass
+    return path, os.path.getsize(path), tmp
+
+
+def run_mps(args):
+    """The fast MPS reader (include/sg_mps.h): seconds per read of the transportation LP's file
+    through the C ABI (value; the model stays in the engine library's handle) and through the
+    Python API (e2e: the arrays copied out into numpy); where a GPU is present also file to
+    answer (read, create on the device, solve to 1e-8) against the same solve from the model in
+    memory; samaya's own reader (oracle/_ref) beside it where it was built."""
+    import ctypes
+    import shutil
+    from samaya_gb300 import _native
+    from samaya_gb300 import mps
+    path, size, tmp = mps_file()
+    lib = _native.load()
+    mps._declare(lib)
+    try:
+        def c_read():
+            h = ctypes.c_void_p()
+            t0 = time.perf_counter()
+            rc = lib.sg_mps_read(os.fsencode(path), 0, ctypes.byref(h))
+            dt = time.perf_counter() - t0
+            if rc != 0:
+                raise RuntimeError(lib.sg_pdlp_last_error().decode())
+            lib.sg_mps_free(h)
+            return dt
+        c_times, py_times = [], []
+        for i in range(args.warmup + args.steps):
+            dt = c_read()
+            t0 = time.perf_counter()
+            f = mps.read_mps(path)
+            dp = time.perf_counter() - t0
+            if i >= args.warmup:
+                c_times.append(dt)
+                py_times.append(dp)
+        value = sum(c_times) / len(c_times)
+        e2e = sum(py_times) / len(py_times)
+        line = {"metric": "MPS read time (fast reader)", "value": value, "unit": "s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": MPS_WORKLOAD, "file_bytes": size,
+                           "threads": "automatic (one per MiB of a section, at most "
+                                      "the hardware's)"},
+                "mb_per_s": size / value / 1e6, "host_cores": os.cpu_count(),
+                "gpu_launches": 0,
+                "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0,
+                        "what": "samaya_gb300.mps.read_mps: the C read plus the copy of the "
+                                "model's arrays and names into numpy"},
+                "nnz": f.model.nnz}
+        try:
+            from oracle import ref
+            if ref.available() and ref.build():
+                t = [ref.mps_read_file(path)["seconds"] for _ in range(2)]
+                line["cpu_baseline"] = {"value": min(t), "unit": "s", "cores": 1,
+                                        "kind": "reference",
+                                        "sample": "samaya::read_mps on the same file (the "
+                                                  "reference's reader, compiled by "
+                                                  "oracle/Makefile.ref)"}
+        except Exception as e:  # the reference build is optional test infrastructure
+            line["cpu_baseline"] = {"unavailable": str(e)}
+        if _native_gpu():
+            line["from_file"] = mps_to_answer(path, args)
+        print(json.dumps(line), flush=True)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return 0
+
+
+def _native_gpu():
+    import samaya_gb300 as sg
+    return sg.gpu_info()["gpu"] is not None
+
+
+def mps_to_answer(path, args):
+    """Seconds from the MPS file to the answer (fast read, device setup from the model, mixed
+    precision solve to 1e-8), and the same solve from the model already in memory."""
+    import samaya_gb300 as sg
+    from samaya_gb300 import mps
+    opts = solver_options(args, "mixed")
+    model = mps.read_mps(path).model
+
+    def solve(md):
+        with sg.PdlpSolver.from_model(md, opts) as s:
+            return s.solve()
+    file_s, mem_s = [], []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        r = solve(mps.read_mps(path).model)
+        file_s.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        solve(model)
+        mem_s.append(time.perf_counter() - t0)
+    return {"file_s": min(file_s), "memory_s": min(mem_s), "status": r.status_name}
+
+
 def run_reference(args):
     world, rank, _ = dist()
     if rank != 0:
         return 0
+    if args.workload == "mps":
+        return run_reference_mps(args)
     if args.workload not in ("transport", "powerlaw", "random"):
         print(json.dumps({"impl": "reference", "unavailable": "the reference solves one LP at "
                           "a time and has no adjoint: no counterpart of this workload"}))
@@ -450,6 +567,41 @@ def run_reference(args):
     return 0
 
 
+def run_reference_mps(args):
+    """samaya::read_mps on the same file, where the reference's reader was compiled
+    (oracle/_ref: built from the reference checkout, which only the build machine has)."""
+    import shutil
+    try:
+        from oracle import ref
+        if not (ref.available() and ref.build()):
+            raise RuntimeError("samaya's compiled reader (oracle/_ref) is not on this machine")
+    except Exception as e:
+        print(json.dumps({"impl": "reference", "unavailable": str(e)}))
+        return 0
+    path, size, tmp = mps_file()
+    try:
+        times = []
+        for i in range(args.warmup + args.steps):
+            dt = ref.mps_read_file(path)["seconds"]
+            if i >= args.warmup:
+                times.append(dt)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    value = sum(times) / len(times)
+    sample = "samaya::read_mps (src/io/mps_reader.cpp:530) on the same file, 1 thread"
+    print(json.dumps({"metric": "MPS read time (fast reader)", "value": value, "unit": "s",
+                      "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": MPS_WORKLOAD, "file_bytes": size},
+                      "impl": "reference",
+                      "cpu_baseline": {"value": value, "unit": "s", "cores": 1,
+                                       "kind": "reference", "sample": sample},
+                      "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -460,6 +612,8 @@ def main():
         return run_batch(args)
     if args.workload == "diff":
         return run_diff(args)
+    if args.workload == "mps":
+        return run_mps(args)
     world, rank, local = dist()
     import numpy as np
     import samaya_gb300 as sg

@@ -41,7 +41,10 @@ enum {
   SG_ERR_OUT_OF_MEMORY = -4,
   SG_ERR_TOO_LARGE = -5,
   SG_ERR_INTERNAL = -6,
-  SG_ERR_NOT_READY = -7
+  SG_ERR_NOT_READY = -7,
+  SG_ERR_PARSE = -8,       /* MPS text that free MPS rejects (sg_mps.h) */
+  SG_ERR_UNSUPPORTED = -9, /* valid MPS outside what the fast reader reads (sg_mps.h) */
+  SG_ERR_IO = -10          /* a file that cannot be opened or read */
 };
 
 /* Precision of the iterations. */

@@ -29,11 +29,10 @@ def available() -> bool:
 
 
 def build() -> str | None:
-    """Builds the reference's CPU sources in place (only where the checkout exists)."""
-    if os.path.exists(_LIB):
-        return _LIB
+    """Builds the reference's CPU sources in place (only where the checkout exists; make
+    rebuilds what changed, ref_driver.cpp included)."""
     if not os.path.isdir(os.path.join(REFERENCE_ROOT, "src")):
-        return None
+        return _LIB if os.path.exists(_LIB) else None
     subprocess.check_call(["make", "-s", "-f", "Makefile.ref", f"REF={REFERENCE_ROOT}",
                            f"-j{os.cpu_count() or 4}"], cwd=_HERE)
     return _LIB
@@ -181,3 +180,69 @@ def solver_pdlp(model):
                ctypes.byref(pi))
     return dict(status=status, objective=obj.value, verified=bool(ver.value),
                 simplex_iterations=si.value, pdlp_iterations=pi.value)
+
+
+class RefMpsError(RuntimeError):
+    """samaya's reader raised: ``parse`` is True for a samaya::ParseError."""
+
+    def __init__(self, parse: bool, message: str):
+        super().__init__(message)
+        self.parse = parse
+
+
+def _mps_take(h):
+    L = lib()
+    info = np.zeros(10, dtype=np.int64)
+    off = ctypes.c_double(0)
+    secs = ctypes.c_double(0)
+    L.ref_mps_info(h, _p(info, I64), ctypes.byref(off), ctypes.byref(secs))
+    m, n, nnz = int(info[0]), int(info[1]), int(info[2])
+    colptr = np.zeros(n + 1, dtype=np.int64)
+    rowidx = np.zeros(max(nnz, 1), dtype=np.int32)
+    vals = np.zeros(max(nnz, 1))
+    obj, cl, cu = np.zeros(max(n, 1)), np.zeros(max(n, 1)), np.zeros(max(n, 1))
+    integer = np.zeros(max(n, 1), dtype=np.uint8)
+    rl, ru = np.zeros(max(m, 1)), np.zeros(max(m, 1))
+    L.ref_mps_get(h, _p(colptr, I64), _p(rowidx, I32), _p(vals, D), _p(obj, D), _p(cl, D),
+                  _p(cu, D), integer.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), _p(rl, D),
+                  _p(ru, D))
+    name = ctypes.create_string_buffer(int(info[5]) + 1)
+    rn = ctypes.create_string_buffer(int(info[6]) + 1)
+    cn = ctypes.create_string_buffer(int(info[7]) + 1)
+    rs = np.zeros(m + 1, dtype=np.int64)
+    cs = np.zeros(n + 1, dtype=np.int64)
+    L.ref_mps_names(h, name, rn, _p(rs, I64), cn, _p(cs, I64))
+    return dict(m=m, n=n, colptr=colptr, rowidx=rowidx[:nnz], vals=vals[:nnz], obj=obj[:n],
+                col_lower=cl[:n], col_upper=cu[:n], col_integer=integer[:n], row_lower=rl[:m],
+                row_upper=ru[:m], maximize=bool(info[3]), obj_offset=off.value,
+                name=name.raw[:int(info[5])], row_names=rn.raw[:int(info[6])], row_starts=rs,
+                col_names=cn.raw[:int(info[7])], col_starts=cs, q_nnz=int(info[8]),
+                quadratic_rows=int(info[9]), seconds=secs.value)
+
+
+def _mps_call(fn, *args):
+    L = lib()
+    f = getattr(L, fn)
+    f.restype = ctypes.c_int
+    L.ref_mps_free.argtypes = [ctypes.c_void_p]
+    h = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(4096)
+    rc = f(*args, ctypes.byref(h), err, ctypes.c_size_t(len(err)))
+    if rc != 0:
+        raise RefMpsError(rc == 1, err.value.decode(errors="replace"))
+    try:
+        return _mps_take(h)
+    finally:
+        L.ref_mps_free(h)
+
+
+def mps_read_text(text):
+    """samaya::read_mps_from_string (src/io/mps_reader.cpp:517): the Model as arrays, names as
+    bytes with starts; raises RefMpsError where samaya raises."""
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    return _mps_call("ref_mps_read", ctypes.c_char_p(data), ctypes.c_size_t(len(data)))
+
+
+def mps_read_file(path):
+    """samaya::read_mps (src/io/mps_reader.cpp:530); ``seconds`` is its wall time."""
+    return _mps_call("ref_mps_read_file", ctypes.c_char_p(os.fsencode(path)))

@@ -12,11 +12,17 @@
 //   ref_random_lp       -> samaya::test::random_lp         (tests/lp_generators.hpp:32)
 //   ref_reference_lp    -> samaya::test::ReferenceLp       (tests/reference_lp.hpp:20)
 //   ref_solver_pdlp     -> Solver::solve with LpMethod::kPdlp (src/core/solver.cpp:705)
+//   ref_mps_read        -> samaya::read_mps_from_string     (src/io/mps_reader.cpp:517)
+//   ref_mps_read_file   -> samaya::read_mps                 (src/io/mps_reader.cpp:530)
 
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <exception>
 #include <random>
+#include <string>
+#include <string_view>
 #include <vector>
 
 #include "core/log.hpp"
@@ -25,6 +31,7 @@
 #include "lp/pdlp.hpp"
 #include "lp_generators.hpp"
 #include "reference_lp.hpp"
+#include "samaya/io.hpp"
 #include "samaya/model.hpp"
 #include "samaya/solver.hpp"
 #include "samaya/verify.hpp"
@@ -234,5 +241,117 @@ int ref_solver_pdlp(int m, int n, const int64_t* colptr, const int32_t* rowidx,
   *pdlp_iterations = r.barrier_iterations;
   return static_cast<int>(r.status);
 }
+
+// ---- MPS: a model read by samaya's own reader, held until ref_mps_free ----
+
+struct RefMps {
+  samaya::Model model;
+  double seconds = 0.0;
+};
+
+static int ref_mps_finish(RefMps* r, void** out, char* err, size_t errlen, int code,
+                          const char* what) {
+  if (code == 0) {
+    *out = r;
+    return 0;
+  }
+  delete r;
+  if (err != nullptr && errlen > 0) {
+    std::strncpy(err, what, errlen - 1);
+    err[errlen - 1] = '\0';
+  }
+  return code;
+}
+
+// 0: read; 1: samaya::ParseError (message in err); 2: another exception.
+int ref_mps_read(const char* text, size_t len, void** out, char* err, size_t errlen) {
+  RefMps* r = new RefMps;
+  try {
+    const auto t0 = std::chrono::steady_clock::now();
+    r->model = samaya::read_mps_from_string(std::string_view(text, len));
+    r->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return ref_mps_finish(r, out, err, errlen, 0, "");
+  } catch (const samaya::ParseError& e) {
+    return ref_mps_finish(r, out, err, errlen, 1, e.what());
+  } catch (const std::exception& e) {
+    return ref_mps_finish(r, out, err, errlen, 2, e.what());
+  }
+}
+
+int ref_mps_read_file(const char* path, void** out, char* err, size_t errlen) {
+  RefMps* r = new RefMps;
+  try {
+    const auto t0 = std::chrono::steady_clock::now();
+    r->model = samaya::read_mps(path);
+    r->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return ref_mps_finish(r, out, err, errlen, 0, "");
+  } catch (const samaya::ParseError& e) {
+    return ref_mps_finish(r, out, err, errlen, 1, e.what());
+  } catch (const std::exception& e) {
+    return ref_mps_finish(r, out, err, errlen, 2, e.what());
+  }
+}
+
+// info: m, n, nnz, maximize, integers, name bytes, row name bytes, column name bytes, Q entries,
+// quadratic row terms; *obj_offset; *seconds (the read's wall time).
+void ref_mps_info(void* h, int64_t* info, double* obj_offset, double* seconds) {
+  const RefMps& r = *static_cast<RefMps*>(h);
+  const samaya::Model& md = r.model;
+  int64_t rn = 0, cn = 0;
+  for (const auto& s : md.row_names) rn += static_cast<int64_t>(s.size());
+  for (const auto& s : md.col_names) cn += static_cast<int64_t>(s.size());
+  info[0] = md.num_rows();
+  info[1] = md.num_cols();
+  info[2] = md.A.nnz();
+  info[3] = md.sense == samaya::ObjSense::kMaximize ? 1 : 0;
+  info[4] = md.num_integers();
+  info[5] = static_cast<int64_t>(md.name.size());
+  info[6] = rn;
+  info[7] = cn;
+  info[8] = md.Q.nnz();
+  info[9] = static_cast<int64_t>(md.row_quadratic.size());
+  *obj_offset = md.obj_offset;
+  *seconds = r.seconds;
+}
+
+void ref_mps_get(void* h, int64_t* colptr, int32_t* rowidx, double* vals, double* obj,
+                 double* col_lower, double* col_upper, uint8_t* col_integer, double* row_lower,
+                 double* row_upper) {
+  const samaya::Model& md = static_cast<RefMps*>(h)->model;
+  copy_csc(md.A, colptr, rowidx, vals);
+  const std::size_t n = md.obj.size(), m = md.row_lower.size();
+  for (std::size_t j = 0; j < n; ++j) {
+    obj[j] = md.obj[j];
+    col_lower[j] = md.col_lower[j];
+    col_upper[j] = md.col_upper[j];
+    col_integer[j] = md.col_type[j] == samaya::VarType::kInteger ? 1 : 0;
+  }
+  for (std::size_t i = 0; i < m; ++i) {
+    row_lower[i] = md.row_lower[i];
+    row_upper[i] = md.row_upper[i];
+  }
+}
+
+void ref_mps_names(void* h, char* name, char* row_names, int64_t* row_starts, char* col_names,
+                   int64_t* col_starts) {
+  const samaya::Model& md = static_cast<RefMps*>(h)->model;
+  std::memcpy(name, md.name.data(), md.name.size());
+  int64_t p = 0;
+  row_starts[0] = 0;
+  for (std::size_t i = 0; i < md.row_names.size(); ++i) {
+    std::memcpy(row_names + p, md.row_names[i].data(), md.row_names[i].size());
+    p += static_cast<int64_t>(md.row_names[i].size());
+    row_starts[i + 1] = p;
+  }
+  p = 0;
+  col_starts[0] = 0;
+  for (std::size_t j = 0; j < md.col_names.size(); ++j) {
+    std::memcpy(col_names + p, md.col_names[j].data(), md.col_names[j].size());
+    p += static_cast<int64_t>(md.col_names[j].size());
+    col_starts[j + 1] = p;
+  }
+}
+
+void ref_mps_free(void* h) { delete static_cast<RefMps*>(h); }
 
 }  // extern "C"

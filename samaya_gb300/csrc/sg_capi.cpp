@@ -8,12 +8,18 @@
 #include <string>
 #include <vector>
 
+#include "../../include/sg_mps.h"
 #include "../../include/sg_pdlp.h"
 #include "sg_engine.cuh"
+#include "sg_mps.h"
 #include "sg_setup_device.cuh"
 
 struct sg_pdlp {
   sg::Engine* engine = nullptr;
+};
+
+struct sg_mps {
+  sg::MpsModel model;
 };
 
 namespace {
@@ -23,6 +29,30 @@ thread_local std::string g_last_error;
 int fail(int code, const std::string& message) {
   g_last_error = message;
   return code;
+}
+
+// The C status of a read; the handle goes to *out on success and is freed otherwise.
+int mps_result(sg::MpsStatus st, const sg::MpsError& e, sg_mps* h, sg_mps** out) {
+  if (st == sg::MpsStatus::kOk) {
+    *out = h;
+    return SG_OK;
+  }
+  delete h;
+  const std::string msg = e.line > 0 ? "line " + std::to_string(e.line) + ": " + e.message
+                                     : e.message;
+  switch (st) {
+    case sg::MpsStatus::kParseError: return fail(SG_ERR_PARSE, msg);
+    case sg::MpsStatus::kUnsupported: return fail(SG_ERR_UNSUPPORTED, msg);
+    case sg::MpsStatus::kIoError: return fail(SG_ERR_IO, msg);
+    case sg::MpsStatus::kTooLarge: return fail(SG_ERR_TOO_LARGE, msg);
+    case sg::MpsStatus::kOutOfMemory: return fail(SG_ERR_OUT_OF_MEMORY, msg);
+    default: return fail(SG_ERR_INTERNAL, msg);
+  }
+}
+
+template <class V, class T>
+void copy_out(const V& v, T* dst) {
+  if (dst != nullptr && !v.empty()) memcpy(dst, v.data(), v.size() * sizeof(T));
 }
 
 sg::Options to_options(const sg_pdlp_opts* o) {
@@ -282,6 +312,9 @@ const char* sg_pdlp_error_string(int code) {
     case SG_ERR_TOO_LARGE: return "problem too large for 32-bit offsets";
     case SG_ERR_INTERNAL: return "internal error";
     case SG_ERR_NOT_READY: return "handle not ready for this call";
+    case SG_ERR_PARSE: return "not valid free MPS";
+    case SG_ERR_UNSUPPORTED: return "outside what the fast MPS reader reads";
+    case SG_ERR_IO: return "file cannot be read";
     default: return "unknown error";
   }
 }
@@ -412,5 +445,75 @@ int sg_spmv(sg_pdlp* handle, int transpose, const double* x, double* y) {
   if (x == nullptr || y == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "NULL vector");
   SG_SEAM(handle->engine->spmv(transpose, x, y));
 }
+
+// ---- the fast MPS reader (include/sg_mps.h) ----
+
+int sg_mps_read(const char* path, int threads, sg_mps** out) {
+  if (out == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "NULL output");
+  *out = nullptr;
+  if (path == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "path is NULL");
+  sg_mps* h = new (std::nothrow) sg_mps;
+  if (h == nullptr) return fail(SG_ERR_OUT_OF_MEMORY, "out of host memory");
+  sg::MpsError e;
+  return mps_result(sg::read_mps_file(path, threads, &h->model, &e), e, h, out);
+}
+
+int sg_mps_read_text(const char* text, size_t len, int threads, sg_mps** out) {
+  if (out == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "NULL output");
+  *out = nullptr;
+  if (text == nullptr && len > 0) return fail(SG_ERR_INVALID_ARGUMENT, "text is NULL");
+  sg_mps* h = new (std::nothrow) sg_mps;
+  if (h == nullptr) return fail(SG_ERR_OUT_OF_MEMORY, "out of host memory");
+  sg::MpsError e;
+  return mps_result(sg::read_mps_text(text, len, threads, &h->model, &e), e, h, out);
+}
+
+int sg_mps_get_info(const sg_mps* h, sg_mps_info* info) {
+  if (h == nullptr || info == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "NULL argument");
+  const sg::MpsModel& md = h->model;
+  info->m = md.m;
+  info->n = md.n;
+  info->nnz = static_cast<int64_t>(md.vals.size());
+  info->maximize = md.maximize ? 1 : 0;
+  int32_t k = 0;
+  for (const uint8_t v : md.col_integer) k += v ? 1 : 0;
+  info->num_integers = k;
+  info->obj_offset = md.obj_offset;
+  info->name_bytes = static_cast<int64_t>(md.name.size());
+  info->row_name_bytes = static_cast<int64_t>(md.row_names.size());
+  info->col_name_bytes = static_cast<int64_t>(md.col_names.size());
+  return SG_OK;
+}
+
+int sg_mps_get_model(const sg_mps* h, int64_t* colptr, int32_t* rowidx, double* vals,
+                     double* obj, double* col_lower, double* col_upper, uint8_t* col_integer,
+                     double* row_lower, double* row_upper) {
+  if (h == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "NULL handle");
+  const sg::MpsModel& md = h->model;
+  copy_out(md.colptr, colptr);
+  copy_out(md.rowidx, rowidx);
+  copy_out(md.vals, vals);
+  copy_out(md.obj, obj);
+  copy_out(md.col_lower, col_lower);
+  copy_out(md.col_upper, col_upper);
+  copy_out(md.col_integer, col_integer);
+  copy_out(md.row_lower, row_lower);
+  copy_out(md.row_upper, row_upper);
+  return SG_OK;
+}
+
+int sg_mps_get_names(const sg_mps* h, char* name, char* row_names, int64_t* row_starts,
+                     char* col_names, int64_t* col_starts) {
+  if (h == nullptr) return fail(SG_ERR_INVALID_ARGUMENT, "NULL handle");
+  const sg::MpsModel& md = h->model;
+  if (name != nullptr && !md.name.empty()) memcpy(name, md.name.data(), md.name.size());
+  copy_out(md.row_names, row_names);
+  copy_out(md.row_name_start, row_starts);
+  copy_out(md.col_names, col_names);
+  copy_out(md.col_name_start, col_starts);
+  return SG_OK;
+}
+
+void sg_mps_free(sg_mps* h) { delete h; }
 
 }  // extern "C"

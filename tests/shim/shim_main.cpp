@@ -22,8 +22,14 @@
 // place of a solve, so that samaya's crossover can be measured from the engine's point on a
 // machine without a GPU. With `dual`: the dual simplex from its own start instead (no PDLP, no
 // crossover), the work the crossover saves.
+//
+//   shim_main --read <model.mps>
+// reads the file with the fast reader's binding (samaya_gb300/shim/read_mps_fast.cpp) and with
+// samaya::read_mps, compares every field of the two Models bit for bit and prints: same
+// fast_reads samaya_reads binding_seconds samaya_seconds.
 #include <dlfcn.h>
 
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -33,6 +39,7 @@
 
 #include "samaya/io.hpp"
 #include "samaya/solver.hpp"
+#include "read_mps_fast.hpp"
 #include "samaya_c_pdlp.h"
 #include "solve_pdlp_gpu.hpp"
 
@@ -85,6 +92,50 @@ int crossover_mode(const char* mps, bool dual_simplex) {
   return 0;
 }
 
+template <class T>
+bool same_bits(const std::vector<T>& a, const std::vector<T>& b) {
+  return a.size() == b.size() && (a.empty() || std::memcmp(a.data(), b.data(), a.size() * sizeof(T)) == 0);
+}
+
+template <class S>
+bool same_span(S a, S b) {
+  return a.size() == b.size() && (a.empty() || std::memcmp(a.data(), b.data(), a.size_bytes()) == 0);
+}
+
+bool same_matrix(const samaya::SparseMatrix& a, const samaya::SparseMatrix& b) {
+  return a.rows() == b.rows() && a.cols() == b.cols() && same_span(a.col_start(), b.col_start()) &&
+         same_span(a.row_index(), b.row_index()) && same_span(a.values(), b.values());
+}
+
+bool same_model(const samaya::Model& a, const samaya::Model& b) {
+  bool q = a.row_quadratic.size() == b.row_quadratic.size();
+  for (size_t k = 0; q && k < a.row_quadratic.size(); ++k) {
+    const auto &x = a.row_quadratic[k], &y = b.row_quadratic[k];
+    q = x.row == y.row && x.col1 == y.col1 && x.col2 == y.col2 &&
+        std::memcmp(&x.value, &y.value, sizeof(double)) == 0;
+  }
+  return q && a.name == b.name && a.sense == b.sense &&
+         std::memcmp(&a.obj_offset, &b.obj_offset, sizeof(double)) == 0 && same_bits(a.obj, b.obj) &&
+         same_bits(a.col_lower, b.col_lower) && same_bits(a.col_upper, b.col_upper) &&
+         a.col_type == b.col_type && a.col_names == b.col_names &&
+         same_bits(a.row_lower, b.row_lower) && same_bits(a.row_upper, b.row_upper) &&
+         a.row_names == b.row_names && same_matrix(a.A, b.A) && same_matrix(a.Q, b.Q);
+}
+
+int read_mode(const char* path) {
+  using clock = std::chrono::steady_clock;
+  const auto t0 = clock::now();
+  const samaya::Model fast = samaya_gb300::read_mps(path);
+  const auto t1 = clock::now();
+  const samaya::Model own = samaya::read_mps(path);
+  const auto t2 = clock::now();
+  const samaya_gb300::ReadCounts c = samaya_gb300::read_counts();
+  std::printf("%d %lld %lld %.6f %.6f\n", same_model(fast, own) ? 1 : 0, c.fast, c.samaya,
+              std::chrono::duration<double>(t1 - t0).count(),
+              std::chrono::duration<double>(t2 - t1).count());
+  return 0;
+}
+
 }  // namespace
 
 namespace samaya {
@@ -101,6 +152,14 @@ PdlpResult solve_pdlp(const LpProblem& lp, const PdlpOptions& options, const Log
 }  // namespace samaya
 
 int main(int argc, char** argv) {
+  if (argc == 3 && std::strcmp(argv[1], "--read") == 0) {
+    try {
+      return read_mode(argv[2]);
+    } catch (const std::exception& e) {
+      std::fprintf(stderr, "%s\n", e.what());
+      return 3;
+    }
+  }
   if ((argc == 3 || argc == 4) && std::strcmp(argv[1], "--crossover") == 0) {
     if (library_solve_pdlp() == nullptr) return 2;
     try {

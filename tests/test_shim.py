@@ -68,6 +68,7 @@ def shim(tmp_path_factory):
            os.path.join(ROOT, "tests", "shim", "shim_main.cpp"),
            os.path.join(ROOT, "samaya_gb300", "shim", "solve_pdlp_gpu.cpp"),
            os.path.join(ROOT, "samaya_gb300", "shim", "samaya_c_pdlp.cpp"),
+           os.path.join(ROOT, "samaya_gb300", "shim", "read_mps_fast.cpp"),
            "-L", os.path.dirname(lib_ref), "-lsamaya_ref", "-L", os.path.dirname(lib_sg),
            "-lsamaya_gb300", f"-Wl,-rpath,{os.path.dirname(lib_ref)}",
            f"-Wl,-rpath,{os.path.dirname(lib_sg)}", "-ldl", "-lpthread", "-o", str(out)]
@@ -164,3 +165,49 @@ def test_crossover_from_the_engine_point(shim, tmp_path):
         seeded_total += seeded["simplex"]
         fresh_total += fresh["simplex"]
     assert seeded_total <= 0.05 * fresh_total, (seeded_total, fresh_total)
+
+
+def _read(exe, path):
+    p = subprocess.run([str(exe), "--read", str(path)], capture_output=True, text=True,
+                       timeout=600)
+    assert p.returncode == 0, p.stderr
+    same, fast, own, t_fast, t_own = p.stdout.split()
+    return dict(same=int(same), fast=int(fast), samaya=int(own), t_fast=float(t_fast),
+                t_own=float(t_own))
+
+
+def test_read_mps_binding_gives_samayas_model(shim, tmp_path):
+    """samaya_gb300::read_mps (the fast reader's binding) returns the Model samaya::read_mps
+    returns, every field bit for bit, on the accepted MPS cases; what the fast reader declines
+    (fixed MPS, quadratic sections) goes to samaya's reader with the same result; on a file that
+    neither reads, the binding throws samaya's error (exit status 3)."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from mps_cases import accepted_cases, rejected_cases
+    for name, text in accepted_cases():
+        path = tmp_path / f"{name}.mps"
+        path.write_bytes(text.encode())
+        r = _read(shim, path)
+        assert r["same"] == 1 and r["fast"] == 1 and r["samaya"] == 0, (name, r)
+    for name, text, status, samaya in rejected_cases():
+        path = tmp_path / f"{name}.mps"
+        path.write_bytes(text.encode())
+        if samaya == "reads":
+            r = _read(shim, path)
+            assert r["same"] == 1 and r["fast"] == 0 and r["samaya"] == 1, (name, r)
+        else:
+            p = subprocess.run([str(shim), "--read", str(path)], capture_output=True,
+                               text=True, timeout=600)
+            assert p.returncode == 3, (name, p.stdout, p.stderr)
+
+
+def test_read_mps_binding_on_the_transportation_lp(shim, tmp_path):
+    """The 93 MB transportation LP (1000 x 2000): the same Model as samaya's reader; the binding
+    (fast reader plus samaya's from_triplets) takes a fraction of samaya's time."""
+    from samaya_gb300 import generators as g
+    from samaya_gb300.mps import write_mps
+    path = tmp_path / "transport.mps"
+    write_mps(g.transportation_lp(1000, 2000, seed=0), path)
+    r = _read(shim, path)
+    assert r["same"] == 1 and r["fast"] == 1, r
+    assert r["t_fast"] < 0.5 * r["t_own"], r
