@@ -77,6 +77,9 @@ def parse():
                          "1e-8; batchA / batchB: LPs/s of the batched engine against sequential "
                          "solves; diff: the differentiable layer's forward and backward; mps: "
                          "the fast MPS reader on the transportation LP's file")
+    ap.add_argument("--mps-lp", default="transport", choices=["transport", "powerlaw"],
+                    help="--workload mps: the LP written to the file (transport: 93 MB; "
+                         "powerlaw: the 1M x 2M power-law LP, 515 MB)")
     ap.add_argument("--precision", default="auto",
                     choices=["auto", "mixed", "refined", "fp64"],
                     help="mixed: FP32 PDLP then FP64 PDLP from its answer; refined: FP32 "
@@ -418,19 +421,24 @@ def run_diff(args):
     return _device_clock_line(line, clk)
 
 
-MPS_WORKLOAD = ("transportation LP 1000 supplies x 2000 demands as a free-MPS file (3,000 rows, "
-                "2,000,000 columns, 4,000,000 entries, two entries to a line)")
+MPS_WORKLOADS = {
+    "transport": "transportation LP 1000 supplies x 2000 demands as a free-MPS file (3,000 rows, "
+                 "2,000,000 columns, 4,000,000 entries, two entries to a line)",
+    "powerlaw": "power-law LP 1,000,000 x 2,000,000 as a free-MPS file (12,000,000 entries, "
+                "two to a line; 1,000,000 RHS and 2,000,000 bound lines)"}
 
 
-def mps_file():
-    """The transportation LP written as free MPS into a temporary directory (and read once, so
-    that the timed reads come from the page cache). Returns (path, bytes, directory)."""
+def mps_file(which="transport"):
+    """An LP written as free MPS into a temporary directory (and read once, so that the timed
+    reads come from the page cache). Returns (path, bytes, directory)."""
     import tempfile
     from samaya_gb300 import generators as g
     from samaya_gb300.mps import write_mps
     tmp = tempfile.mkdtemp(prefix="sg_mps_")
-    path = os.path.join(tmp, "transport.mps")
-    write_mps(g.transportation_lp(1000, 2000, seed=0), path)
+    path = os.path.join(tmp, f"{which}.mps")
+    model = g.transportation_lp(1000, 2000, seed=0) if which == "transport" else \
+        g.power_law_lp(seed=0)
+    write_mps(model, path)
     with open(path, "rb") as f:
         while f.read(1 << 24):
             pass
@@ -447,7 +455,7 @@ def run_mps(args):
     import shutil
     from samaya_gb300 import _native
     from samaya_gb300 import mps
-    path, size, tmp = mps_file()
+    path, size, tmp = mps_file(args.mps_lp)
     lib = _native.load()
     mps._declare(lib)
     try:
@@ -475,7 +483,7 @@ def run_mps(args):
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": MPS_WORKLOAD, "file_bytes": size,
+                "config": {"workload": MPS_WORKLOADS[args.mps_lp], "file_bytes": size,
                            "threads": "automatic (one per MiB of a section, at most "
                                       "the hardware's)"},
                 "mb_per_s": size / value / 1e6, "host_cores": os.cpu_count(),
@@ -496,7 +504,7 @@ def run_mps(args):
                                                   "oracle/Makefile.ref)"}
         except Exception as e:  # the reference build is optional test infrastructure
             line["cpu_baseline"] = {"unavailable": str(e)}
-        if _native_gpu():
+        if _native_gpu() and args.mps_lp == "transport":
             line["from_file"] = mps_to_answer(path, args)
         print(json.dumps(line), flush=True)
     finally:
@@ -578,7 +586,7 @@ def run_reference_mps(args):
     except Exception as e:
         print(json.dumps({"impl": "reference", "unavailable": str(e)}))
         return 0
-    path, size, tmp = mps_file()
+    path, size, tmp = mps_file(args.mps_lp)
     try:
         times = []
         for i in range(args.warmup + args.steps):
@@ -593,7 +601,7 @@ def run_reference_mps(args):
                       "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                       "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
                       "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                      "config": {"workload": MPS_WORKLOAD, "file_bytes": size},
+                      "config": {"workload": MPS_WORKLOADS[args.mps_lp], "file_bytes": size},
                       "impl": "reference",
                       "cpu_baseline": {"value": value, "unit": "s", "cores": 1,
                                        "kind": "reference", "sample": sample},
