@@ -205,7 +205,9 @@ inline bool parse_short_decimal(const char* p, const char* e, double* v) {
 inline bool parse_number(string_view s, double* v) {
   if (!s.empty() && s.front() == '+') s.remove_prefix(1);
   double x = 0.0;
-  if (!parse_short_decimal(s.data(), s.data() + s.size(), &x)) {
+  // A token of 18 or more characters rarely fits the fast path's 2^53 mantissa (17-digit
+  // values are written that long): it goes straight to from_chars, scanned once.
+  if (s.size() >= 18 || !parse_short_decimal(s.data(), s.data() + s.size(), &x)) {
     const auto r = std::from_chars(s.data(), s.data() + s.size(), x);
     if (r.ec != std::errc() || r.ptr != s.data() + s.size()) return false;
   }
@@ -584,6 +586,32 @@ class Reader {
     return id < 0 ? -1 : cand_col_[id];
   }
 
+  static bool named(const Key& k, string_view name) {
+    return k.len == name.size() && std::memcmp(k.p, name.data(), k.len) == 0;
+  }
+
+  // find_col, trying the column after `*last` (and `*last` itself) first: bound lines mostly
+  // follow the column order, and comparing that column's name reads the text in order.
+  int32_t find_col_after(string_view name, int32_t* last) const {
+    for (int32_t c : {*last + 1, *last}) {
+      if (c >= 0 && c < n_ && named(col_keys_[col_cand_[c]], name)) return *last = c;
+    }
+    const int32_t c = find_col(name);
+    if (c >= 0) *last = c;
+    return c;
+  }
+
+  // find_row with the same guess for right-hand sides and ranges listed in row order.
+  int32_t find_row_after(string_view name, int32_t* last) const {
+    if (name.size() == objective_.size() && name == objective_) return kObjectiveRow;
+    for (int32_t r : {*last + 1, *last}) {
+      if (r >= 0 && r < m_ && named(row_keys_[row_name_id_[r]], name)) return *last = r;
+    }
+    const int32_t r = find_row(name);
+    if (r >= 0) *last = r;
+    return r;
+  }
+
   // ---- ROWS (mps_reader.cpp:225-244) ----
   void rows(const char* b, const char* e) {
     struct Chunk {
@@ -819,6 +847,7 @@ class Reader {
     run_threads(parts, [&](int t) {
       Chunk& c = ch[t];
       Tokens tk;
+      int32_t last = -2;
       for_lines(cut[t], cut[t + 1], [&](const char* p, const char* q) {
         if (p == q || *p == '*') return true;
         tokenize(p, q, tk);
@@ -829,7 +858,7 @@ class Reader {
                                           : "RHS entry has the wrong number of fields");
         }
         for (int j = first; j + 1 < tk.n; j += 2) {
-          const int32_t row = find_row(tk.t[j]);
+          const int32_t row = find_row_after(tk.t[j], &last);
           if (row == kUnknownRow) return c.error.fail(p, "unknown row '" + std::string(tk.t[j]) + "'");
           double v;
           if (!parse_number(tk.t[j + 1], &v)) {
@@ -882,6 +911,7 @@ class Reader {
     run_threads(parts, [&](int t) {
       Chunk& c = ch[t];
       Tokens tk;
+      int32_t last = -2;
       for_lines(cut[t], cut[t + 1], [&](const char* p, const char* q) {
         if (p == q || *p == '*') return true;
         tokenize(p, q, tk);
@@ -904,7 +934,7 @@ class Reader {
         } else if (tk.n > 4) {
           return c.error.fail(p, "BOUNDS entry has the wrong number of fields");
         }
-        const int32_t col = find_col(tk.t[pos]);
+        const int32_t col = find_col_after(tk.t[pos], &last);
         if (col < 0) return c.error.fail(p, "unknown column '" + std::string(tk.t[pos]) + "'");
         double v = 0.0;
         if (!no_value && !parse_number(tk.t[pos + 1], &v)) {

@@ -103,6 +103,28 @@ BOUNDS
 ENDATA
 """
 
+OBJNAME_IS_A_CONSTRAINT = """NAME objrow
+OBJNAME r2
+ROWS
+ N n0
+ E r1
+ E r2
+ L r3
+COLUMNS
+ a n0 1 r1 1
+ a r2 2 r3 1
+ b r1 1 r2 -1
+ b r3 2
+RHS
+ rhs r1 1 r2 5
+ rhs r3 4
+BOUNDS
+ UP bnd b 3
+ UP bnd a 2
+ LO bnd b 1
+ENDATA
+"""
+
 COMMENTS_CRLF_TABS = ("NAME\tcrlf\r\n*comment\r\nROWS\r\n N\tobj\r\n\r\n E\tr1\r\n   \r\n"
                       " L r2\r\nCOLUMNS\r\n\tx\tobj\t1\tr1\t1\r\n* inside\r\n x\tr2\t2\r\n\r\n"
                       "\ty\tr1\t-1\r\nRHS\r\n rhs\tr1\t3\r\n rhs r2 4\r\nBOUNDS\r\n UP\tbnd\tx\t"
@@ -351,7 +373,9 @@ def fixed_format_case() -> str:
 
 def accepted_cases():
     cases = [("all_features", ALL_FEATURES), ("objsense_section", OBJSENSE_SECTION),
-             ("objname_header", OBJNAME_HEADER), ("comments_crlf_tabs", COMMENTS_CRLF_TABS),
+             ("objname_header", OBJNAME_HEADER),
+             ("objname_is_a_constraint", OBJNAME_IS_A_CONSTRAINT),
+             ("comments_crlf_tabs", COMMENTS_CRLF_TABS),
              ("repeated_columns", REPEATED_COLUMNS), ("infinities", INFINITIES),
              ("empty_model", EMPTY_MODEL), ("no_name_no_end", NO_NAME_NO_END),
              ("long_names", LONG_NAMES), ("rhs_last_wins", RHS_LAST_WINS),
