@@ -111,7 +111,8 @@ def parse():
     args = ap.parse_args()
     if args.algorithm == "auto":
         args.algorithm = {"transport": "halpern", "random": "reference", "powerlaw": "halpern",
-                          "batchA": "reference"}.get(args.workload, "enhanced")
+                          "batchA": "reference", "mps": "halpern"}.get(args.workload,
+                                                                     "enhanced")
     if args.precision == "auto":
         args.precision = "fp64" if args.workload == "powerlaw" else "mixed"
     global TOL
