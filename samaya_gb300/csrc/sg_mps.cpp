@@ -34,6 +34,9 @@
 #include <atomic>
 #include <cerrno>
 #include <charconv>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <exception>
@@ -377,6 +380,28 @@ constexpr int32_t kObjectiveRow = -1;
 constexpr int32_t kFreeRow = -2;
 constexpr int32_t kUnknownRow = -3;
 
+// With SG_MPS_PHASES set (to anything but "0"), the reader prints the wall time of each phase to
+// stderr: a diagnostic for profiling the reader.
+class PhaseClock {
+ public:
+  PhaseClock() {
+    const char* e = std::getenv("SG_MPS_PHASES");
+    on_ = e != nullptr && *e != '\0' && std::strcmp(e, "0") != 0;
+    last_ = std::chrono::steady_clock::now();
+  }
+  void mark(const char* phase) {
+    if (!on_) return;
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "sg_mps %-10s %9.2f ms\n", phase,
+                 std::chrono::duration<double, std::milli>(now - last_).count());
+    last_ = now;
+  }
+
+ private:
+  bool on_ = false;
+  std::chrono::steady_clock::time_point last_;
+};
+
 class Reader {
  public:
   Reader(const char* text, size_t len, int threads) : text_(text), len_(len) {
@@ -388,6 +413,7 @@ class Reader {
   void read(MpsModel* out) {
     const char* end = text_ + len_;
     const std::vector<const char*> headers = find_headers();
+    clock_.mark("headers");
     no_data(text_, headers.empty() ? end : headers[0]);
     for (size_t k = 0; k < headers.size(); ++k) {
       const char* h = headers[k];
@@ -412,11 +438,11 @@ class Reader {
           each_data_line(body, body_end,
                          [&](const Tokens& t, const char* p) { set_objective_name(t.t[0], p); });
           break;
-        case Section::kRows: rows(body, body_end); break;
+        case Section::kRows: rows(body, body_end); clock_.mark("rows"); break;
         case Section::kColumns: columns(body, body_end); break;
-        case Section::kRhs: rhs(body, body_end, false); break;
-        case Section::kRanges: rhs(body, body_end, true); break;
-        case Section::kBounds: bounds(body, body_end); break;
+        case Section::kRhs: rhs(body, body_end, false); clock_.mark("rhs"); break;
+        case Section::kRanges: rhs(body, body_end, true); clock_.mark("ranges"); break;
+        case Section::kBounds: bounds(body, body_end); clock_.mark("bounds"); break;
         case Section::kEnd: break;
       }
     }
@@ -750,6 +776,7 @@ class Reader {
     std::vector<ColChunk>& ch = *sec;
     run_threads(parts, [&](int t) { parse_columns(cut[t], cut[t + 1], ch[t]); });
     rethrow_first(ch);
+    clock_.mark("col parse");
 
     // Candidates (runs) numbered in file order after those of earlier COLUMNS sections.
     const size_t base = col_keys_.size();
@@ -829,6 +856,7 @@ class Reader {
     n_ = static_cast<int32_t>(n_new);
     for (ColChunk& c : ch) chunks_.push_back(&c);
     sections_.push_back(std::move(sec));
+    clock_.mark("col table");
   }
 
   // ---- RHS and RANGES (mps_reader.cpp:304-344) ----
@@ -1331,6 +1359,7 @@ class Reader {
     int64_t bad_obj = -1;
     bool bad_entry = false;
     build_matrix(out, &bad_obj, &bad_entry);
+    clock_.mark("matrix");
 
     if (!std::isfinite(obj_offset_)) fail(nullptr, "objective offset is not finite");
     if (bad_obj >= 0) fail(nullptr, "objective coefficient " + std::to_string(bad_obj) + " is not finite");
@@ -1351,6 +1380,7 @@ class Reader {
     out->col_integer = std::move(col_integer_);
     copy_names(row_keys_, row_name_id_, out->row_names, out->row_name_start, nt);
     copy_names(col_keys_, col_cand_, out->col_names, out->col_name_start, nt);
+    clock_.mark("names");
   }
 
   struct Extra {
@@ -1361,6 +1391,7 @@ class Reader {
   const char* text_;
   size_t len_;
   const char* last_line_ = nullptr;  // the ENDATA line, once read
+  PhaseClock clock_;
   int hw_threads_ = 1;
   int forced_ = 0;
 
