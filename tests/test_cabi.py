@@ -186,3 +186,43 @@ def test_csc_to_csr_matches_the_sequential_transpose():
     rc, _, _, _ = run(2, 2, colptr, np.array([0, 1, 1], dtype=np.int32),
                       np.array([1.0, np.inf, 2.0]))
     assert rc == -1
+
+
+def test_plain_c_caller_reads_mps(tmp_path):
+    """include/sg_mps.h and include/sg_pdlp.h compile as C99; a C program linked with the
+    library reads an MPS file through sg_mps_* (the same sizes, sense, offset and entries as the
+    Python binding), reports a refused file with its status and message, and gets
+    SG_ERR_NO_DEVICE on a machine without a GPU."""
+    import shutil
+    import subprocess
+    from samaya_gb300 import build, mps
+    from samaya_gb300 import generators as g
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    lib = build.build()
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = tmp_path / "mps_reader_c"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-pedantic", "-I",
+                    os.path.join(root, "include"), os.path.join(root, "tests", "c",
+                                                                "mps_reader_c.c"),
+                    "-L", os.path.dirname(lib), "-lsamaya_gb300",
+                    f"-Wl,-rpath,{os.path.dirname(lib)}", "-o", str(exe)], check=True)
+    model = g.random_sparse_lp(50, 120, seed=4)
+    path = tmp_path / "lp.mps"
+    mps.write_mps(model, path)
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    out = subprocess.run([str(exe), str(path)], capture_output=True, text=True, env=env,
+                         check=True).stdout.split("\n")
+    f = mps.read_mps(path)
+    got = out[0].split()
+    assert got[0] == "read", out
+    assert [int(v) for v in got[1:6]] == [f.model.m, f.model.n, f.model.nnz, 0, 0]
+    assert float(got[6]) == f.model.obj_offset
+    assert float(got[7]) == pytest.approx(float(np.sum(f.model.vals)), rel=1e-12)
+    assert got[8:] == ["R0", "C0"]
+    assert out[1] == "available -2"
+    bad = tmp_path / "bad.mps"
+    bad.write_text("NAME x\nROWS\n N obj\nCOLUMNS\n x r 1\nENDATA\n")
+    out = subprocess.run([str(exe), str(bad)], capture_output=True, text=True, env=env,
+                         check=True).stdout
+    assert out.startswith("error -8 not valid free MPS: line 5: unknown row 'r'"), out
