@@ -736,13 +736,15 @@ class Reader {
         return true;
       }
       if (tk.n != 3 && tk.n != 5) return c.error.fail(p, "COLUMNS entry needs 3 or 5 fields");
-      const Key k = make_key(tk.t[0]);
-      if (c.runs.empty() || !same(c.keys.back(), k)) {
+      // A line that goes on with the last run's column is told by its bytes, without a hash.
+      const string_view name = tk.t[0];
+      if (c.runs.empty() || c.keys.back().len != name.size() ||
+          std::memcmp(c.keys.back().p, name.data(), name.size()) != 0) {
         if (c.rows.size() > std::numeric_limits<uint32_t>::max() - 2 ||
             c.objv.size() > std::numeric_limits<uint32_t>::max() - 2) {
           return c.error.fail(p, "too many entries in one range");
         }
-        c.keys.push_back(k);
+        c.keys.push_back(make_key(name));
         c.runs.push_back(Run{static_cast<uint32_t>(c.rows.size()), 0,
                              static_cast<uint32_t>(c.objv.size()), 0, state});
       }
