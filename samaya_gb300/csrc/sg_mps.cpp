@@ -674,9 +674,16 @@ class Reader {
         return true;
       });
     });
-    rethrow_first(ch);
+    // A malformed line fails the read, but a duplicate name on an earlier line fails it first
+    // (samaya stops at the first of the two): the records of the ranges up to the failing one,
+    // which all precede the failing line, still go through the duplicate check below.
+    size_t failed = ch.size();
+    for (size_t t = 0; t < ch.size() && failed == ch.size(); ++t) {
+      if (ch[t].error.at != nullptr) failed = t;
+    }
     const size_t base = row_keys_.size();
-    for (const Chunk& c : ch) {
+    for (size_t t = 0; t < ch.size() && t <= failed; ++t) {
+      const Chunk& c = ch[t];
       for (size_t i = 0; i < c.keys.size(); ++i) {
         const Key& k = c.keys[i];
         int32_t v;
@@ -704,6 +711,7 @@ class Reader {
         fail(row_keys_[id].p, "duplicate row '" + std::string(row_keys_[id].view()) + "'");
       }
     }
+    if (failed < ch.size()) fail(ch[failed].error.at, ch[failed].error.message);
   }
 
   int threads_for(size_t items) const {

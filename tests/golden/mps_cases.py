@@ -419,6 +419,8 @@ def rejected_cases():
         ("four_fields", _edit(" y r1 1", " y r1 1 r2"), "parse", "raises"),
         ("duplicate_row", _edit(" L r2", " L r2\n E r1"), "parse", "raises"),
         ("unknown_row_type", _edit(" L r2", " X r2"), "parse", "raises"),
+        ("duplicate_before_bad_row", _edit(" L r2", " L r2\n E r1\n G r3\n X r4"), "parse",
+         "raises"),
         ("row_without_name", _edit(" L r2", " L"), "parse", "raises"),
         ("unknown_section", _edit("RHS\n", "FOO\nRHS\n"), "parse", "raises"),
         ("data_before_section", " x y\n" + _BASE, "parse", "raises"),

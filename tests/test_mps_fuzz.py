@@ -177,3 +177,54 @@ def test_random_texts_read_alike(block):
         else:
             read += 1
     assert read > 30 and refused > 10, (read, refused)
+
+
+def _mutated(seed: int) -> bytes:
+    """A random text with one to three byte edits: a byte replaced, a byte inserted (CR, NUL,
+    blanks, newline, sign, point, exponent, quote, high bytes), a run deleted, the text cut, or
+    a slice of it repeated elsewhere."""
+    rng = np.random.default_rng(10_000 + seed)
+    b = bytearray(_text(seed).encode())
+    junk = (b"\r", b"\x00", b" ", b"\t", b"\n", b"*", b"+", b"-", b"e", b".", b"\xff",
+            b"\xc3\xa9", b"'", b"1")
+    for _ in range(int(rng.integers(1, 4))):
+        op = int(rng.integers(0, 5))
+        i = int(rng.integers(0, max(1, len(b))))
+        if op == 0 and b:
+            b[i] = int(rng.integers(0, 256))
+        elif op == 1:
+            b[i:i] = junk[int(rng.integers(0, len(junk)))]
+        elif op == 2 and b:
+            del b[i:i + int(rng.integers(1, 8))]
+        elif op == 3:
+            b = b[:i]
+        else:
+            j = int(rng.integers(0, max(1, len(b))))
+            b[i:i] = b[j:j + int(rng.integers(1, 40))]
+    return bytes(b)
+
+
+def test_mutated_texts_read_alike():
+    """Byte-level mutations of the random texts: the same Model or the same refusal (line) as
+    samaya's reader, at 1 and 4 threads."""
+    from oracle import ref
+    if not ref.available():
+        pytest.skip("the samaya checkout is not present")
+    ref.build()
+    for seed in range(400):
+        text = _mutated(seed)
+        try:
+            want = ref.mps_read_text(text)
+        except ref.RefMpsError as e:
+            want, why = None, str(e)
+        for threads in (1, 4):
+            try:
+                got = _fast_dict(mps.read_mps_text(text, threads=threads))
+            except mps.MpsReadError as e:
+                assert want is None or e.code == mps.SG_ERR_UNSUPPORTED, (seed, str(e))
+                if want is None and e.code == mps.SG_ERR_PARSE:
+                    assert _line(str(e)) == _line(why), (seed, str(e), why)
+                continue
+            assert want is not None, (seed, why)
+            _assert_same(got, want, f"mutated seed {seed} threads {threads}")
+
