@@ -168,3 +168,38 @@ def test_full_size_transportation_lp(tmp_path):
     except pytest.skip.Exception:
         return
     _assert_same(_fast_dict(f), ref.mps_read_file(path), "transport 1000 x 2000")
+
+
+def test_samayas_own_test_inputs():
+    """The MPS inputs of samaya's own reader tests: the complete texts in
+    tests/test_mps_reader.cpp and the files of tests/instances (a MIPLIB instance with integer
+    markers, a crude-blending LP, pooling problems with QCMATRIX rows), read from the samaya
+    checkout at test time. The linear ones read to samaya's Model bit for bit; the quadratic
+    ones are declined for samaya's reader to take."""
+    import glob
+    from oracle import ref
+    root = ref.REFERENCE_ROOT
+    src = os.path.join(root, "tests", "test_mps_reader.cpp")
+    if not os.path.exists(src):
+        pytest.skip("the samaya checkout is not present")
+    ref.build()
+    with open(src) as f:
+        texts = [t for t in re.findall(r'R"\((.*?)\)"', f.read(), re.S)
+                 if t.lstrip().startswith("NAME")]
+    inputs = [(f"test_mps_reader.cpp #{i}", t.encode()) for i, t in enumerate(texts)]
+    for p in sorted(glob.glob(os.path.join(root, "tests", "instances", "*.mps"))):
+        with open(p, "rb") as f:
+            inputs.append((os.path.basename(p), f.read()))
+    linear = quadratic = 0
+    for name, text in inputs:
+        want = ref.mps_read_text(text)
+        if want["q_nnz"] or want["quadratic_rows"]:
+            with pytest.raises(mps.MpsReadError) as e:
+                mps.read_mps_text(text, threads=3)
+            assert e.value.code == mps.SG_ERR_UNSUPPORTED, name
+            quadratic += 1
+            continue
+        for threads in (0, 3):
+            _assert_same(_fast_dict(mps.read_mps_text(text, threads=threads)), want, name)
+        linear += 1
+    assert linear >= 7 and quadratic >= 3, (linear, quadratic)
