@@ -275,7 +275,9 @@ int sg_csc_to_csr(int m, int n, const int64_t* a_colptr, const int32_t* a_rowidx
  * src/lp/lp_solver.cpp:28-51). The model is min/max obj'x s.t. row_lower <= A x <= row_upper,
  * col_lower <= x <= col_upper with A in CSC form. Writes the scaled A (lp_colptr n + 1,
  * lp_rowidx/lp_val sized by the model's nonzeros; *lp_nnz set), cost/lower/upper (n + m) and
- * the scale factors (col n, row m). Host only; no GPU needed. */
+ * the scale factors (col n, row m). Host only; no GPU needed. SG_ERR_INVALID_ARGUMENT for
+ * column starts that do not begin at 0 or decrease, a row index out of range, a matrix value or
+ * cost that is not finite, or a NaN bound (the checks of sg_scale_model_device). */
 int sg_scale_model(int m, int n, const int64_t* a_colptr, const int32_t* a_rowidx,
                    const double* a_val, const double* obj, const double* col_lower,
                    const double* col_upper, const double* row_lower, const double* row_upper,

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/sg_pdlp.h"
+#include "sg_transpose.h"
 
 namespace {
 
@@ -58,6 +59,34 @@ void row_extremes(const Csc& a, const std::vector<double>& c, std::vector<double
 
 }  // namespace
 
+namespace {
+
+// The model checks of sg_scale_model_device (sg_setup_device.cu, check_host): column starts
+// from 0 and never decreasing, the matrix arrays present, every row index in range and every
+// value finite (host threads), every cost finite and no bound NaN.
+bool valid_model(int m, int n, const int64_t* colptr, const int32_t* rowidx, const double* val,
+                 const double* obj, const double* col_lower, const double* col_upper,
+                 const double* row_lower, const double* row_upper) {
+  if (colptr[0] != 0) return false;
+  for (int j = 0; j < n; ++j) {
+    if (colptr[j + 1] < colptr[j]) return false;
+  }
+  const int64_t nnz = colptr[n];
+  if (nnz > 0 && (rowidx == nullptr || val == nullptr)) return false;
+  for (int j = 0; j < n; ++j) {
+    if (!std::isfinite(obj[j]) || std::isnan(col_lower[j]) || std::isnan(col_upper[j])) {
+      return false;
+    }
+  }
+  for (int i = 0; i < m; ++i) {
+    if (std::isnan(row_lower[i]) || std::isnan(row_upper[i])) return false;
+  }
+  const char* why = nullptr;
+  return nnz == 0 || sg::check_nonzeros(m, nnz, rowidx, val, 16, &why) == 0;
+}
+
+}  // namespace
+
 extern "C" {
 
 /* See include/sg_pdlp.h. */
@@ -75,10 +104,11 @@ int sg_scale_model(int m, int n, const int64_t* a_colptr, const int32_t* a_rowid
   if (m > 0 && (row_lower == nullptr || row_upper == nullptr || row_scale == nullptr)) {
     return SG_ERR_INVALID_ARGUMENT;
   }
-  const int64_t nnz = a_colptr[n];
-  for (int64_t p = 0; p < nnz; ++p) {
-    if (a_rowidx[p] < 0 || a_rowidx[p] >= m) return SG_ERR_INVALID_ARGUMENT;
+  if (!valid_model(m, n, a_colptr, a_rowidx, a_val, obj, col_lower, col_upper, row_lower,
+                   row_upper)) {
+    return SG_ERR_INVALID_ARGUMENT;
   }
+  const int64_t nnz = a_colptr[n];
   const Csc a{m, n, a_colptr, a_rowidx, a_val};
   std::vector<double> r(static_cast<size_t>(m), 1.0), c(static_cast<size_t>(n), 1.0);
   if (nnz > 0) {

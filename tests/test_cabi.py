@@ -226,3 +226,51 @@ def test_plain_c_caller_reads_mps(tmp_path):
     out = subprocess.run([str(exe), str(bad)], capture_output=True, text=True, env=env,
                          check=True).stdout
     assert out.startswith("error -8 not valid free MPS: line 5: unknown row 'r'"), out
+
+
+def test_scale_model_refuses_malformed_models():
+    """sg_scale_model answers SG_ERR_INVALID_ARGUMENT, writing nothing past its outputs, for
+    column starts that do not begin at 0 or decrease, a row index out of range, a value or cost
+    that is not finite, or a NaN bound; a valid model gives SG_OK."""
+    from samaya_gb300 import generators as g
+    lib = _lib()
+    base = g.random_sparse_lp(30, 70, seed=2)
+
+    def run(**kw):
+        md = {k: np.array(getattr(base, k), copy=True) for k in (
+            "colptr", "rowidx", "vals", "obj", "col_lower", "col_upper", "row_lower",
+            "row_upper")}
+        for k, f in kw.items():
+            f(md[k])
+        m, n, nnz = base.m, base.n, int(base.colptr[-1])
+        cp = np.ascontiguousarray(md["colptr"], dtype=np.int64)
+        ri = np.ascontiguousarray(md["rowidx"], dtype=np.int32)
+        d = [np.ascontiguousarray(md[k], dtype=np.float64) for k in (
+            "vals", "obj", "col_lower", "col_upper", "row_lower", "row_upper")]
+        oc = np.zeros(n + 1, dtype=np.int64)
+        orow = np.zeros(nnz, dtype=np.int32)
+        ov = np.zeros(nnz)
+        outs = [np.zeros(n + m) for _ in range(3)] + [np.zeros(n), np.zeros(m)]
+        k = ctypes.c_int64(0)
+        D = ctypes.POINTER(ctypes.c_double)
+        return lib.sg_scale_model(m, n, _p(cp, ctypes.c_int64), _p(ri, ctypes.c_int32),
+                                  *[a.ctypes.data_as(D) for a in d], 0,
+                                  _p(oc, ctypes.c_int64), _p(orow, ctypes.c_int32),
+                                  ov.ctypes.data_as(D), *[a.ctypes.data_as(D) for a in outs],
+                                  ctypes.byref(k))
+
+    def at(i, v):
+        def f(a):
+            a[i] = v
+        return f
+    assert run() == 0
+    assert run(colptr=at(0, 1)) == -1
+    assert run(colptr=at(5, int(base.colptr[6]) + 1)) == -1
+    assert run(rowidx=at(3, base.m)) == -1
+    assert run(rowidx=at(3, -1)) == -1
+    assert run(vals=at(7, np.nan)) == -1
+    assert run(vals=at(7, np.inf)) == -1
+    assert run(obj=at(2, np.inf)) == -1
+    assert run(col_upper=at(4, np.nan)) == -1
+    assert run(row_lower=at(1, np.nan)) == -1
+    assert run(col_upper=at(4, np.inf), row_lower=at(1, -np.inf)) == 0
