@@ -73,10 +73,17 @@ int Batch::create(Batch** out, int nmat, const int* mat_m, const int* mat_n,
       return SG_ERR_INVALID_ARGUMENT;
     }
     cp_off[g + 1] = cp_off[g] + mat_n[g] + 1;
-    const long long nnz = mat_colptr[cp_off[g] + mat_n[g]];
-    if (mat_colptr[cp_off[g]] != 0 || nnz < 0 || nnz >= std::numeric_limits<int>::max()) {
+    const int64_t* cp = mat_colptr + cp_off[g];
+    const long long nnz = cp[mat_n[g]];
+    if (cp[0] != 0 || nnz < 0 || nnz >= std::numeric_limits<int>::max()) {
       if (err) *err = "bad column starts";
       return SG_ERR_INVALID_ARGUMENT;
+    }
+    for (int j = 0; j < mat_n[g]; ++j) {
+      if (cp[j + 1] < cp[j]) {
+        if (err) *err = "column starts decrease";
+        return SG_ERR_INVALID_ARGUMENT;
+      }
     }
     nnz_off[g + 1] = nnz_off[g] + nnz;
     kptr_off[g + 1] = kptr_off[g] + mat_m[g] + 1;
@@ -85,6 +92,10 @@ int Batch::create(Batch** out, int nmat, const int* mat_m, const int* mat_n,
     row_off[g + 1] = row_off[g] + mat_m[g];
   }
   const long long total_nnz = nnz_off[nmat];
+  if (total_nnz > 0 && (mat_rowidx == nullptr || mat_val == nullptr)) {
+    if (err) *err = "null matrix arrays";
+    return SG_ERR_INVALID_ARGUMENT;
+  }
   std::vector<int> kptr(kptr_off[nmat]), tptr(tptr_off[nmat]), kidx(std::max(total_nnz, 1LL)),
       tidx(std::max(total_nnz, 1LL));
   std::vector<double> kval(std::max(total_nnz, 1LL)), tval(std::max(total_nnz, 1LL));

@@ -191,7 +191,10 @@ int sg_scale_model(int m, int n, const int64_t* a_colptr, const int32_t* a_rowid
 int sg_unscale_solution(int m, int n, const double* col_scale, const double* row_scale,
                         int maximize, const double* x_lp, const double* y_lp, double* x,
                         double* row_activity, double* row_dual) {
-  if (m < 0 || n < 0 || col_scale == nullptr || x_lp == nullptr) return SG_ERR_INVALID_ARGUMENT;
+  if (m < 0 || n < 0 || col_scale == nullptr || x_lp == nullptr ||
+      (m > 0 && (row_activity != nullptr || row_dual != nullptr) && row_scale == nullptr)) {
+    return SG_ERR_INVALID_ARGUMENT;
+  }
   const double sense = maximize ? -1.0 : 1.0;
   for (int j = 0; j < n; ++j) {
     if (x) x[j] = x_lp[j] * col_scale[j];

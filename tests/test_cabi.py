@@ -274,3 +274,39 @@ def test_scale_model_refuses_malformed_models():
     assert run(col_upper=at(4, np.nan)) == -1
     assert run(row_lower=at(1, np.nan)) == -1
     assert run(col_upper=at(4, np.inf), row_lower=at(1, -np.inf)) == 0
+
+
+def test_batch_create_checks_every_matrix_before_the_device():
+    """sg_batch_create checks each matrix's column starts (from 0, never decreasing) and entries
+    before it looks for a GPU: a malformed matrix is SG_ERR_INVALID_ARGUMENT with its reason,
+    and on a machine without a GPU a valid batch is SG_ERR_NO_DEVICE."""
+    from samaya_gb300 import _native
+    from samaya_gb300.batch import BatchSolver
+    from samaya_gb300 import generators as g
+    from samaya_gb300.problem import make_problem
+    lp = make_problem(g.random_sparse_lp(20, 50, seed=1))[0]
+    good = (lp.m, lp.n, lp.colptr, lp.rowidx, lp.vals)
+    cp = lp.colptr.copy()
+    cp[3] = cp[4] + 1
+    bad = (lp.m, lp.n, cp, lp.rowidx, lp.vals)
+    inst = [(1, lp.cost, lp.lower, lp.upper)]
+    with pytest.raises(_native.EngineError) as e:
+        BatchSolver([good, bad], inst)
+    assert e.value.code == -1 and "column starts decrease" in str(e.value)
+    if not _has_gpu():
+        with pytest.raises(_native.EngineError) as e:
+            BatchSolver([good], [(0, lp.cost, lp.lower, lp.upper)])
+        assert e.value.code == -2
+
+
+def test_unscale_needs_row_scales_for_row_outputs():
+    lib = _lib()
+    x_lp = np.zeros(5)
+    x = np.zeros(3)
+    act = np.zeros(2)
+    cs = np.ones(3)
+    D = ctypes.POINTER(ctypes.c_double)
+    assert lib.sg_unscale_solution(2, 3, cs.ctypes.data_as(D), None, 0, x_lp.ctypes.data_as(D),
+                                   None, x.ctypes.data_as(D), act.ctypes.data_as(D), None) == -1
+    assert lib.sg_unscale_solution(2, 3, cs.ctypes.data_as(D), None, 0, x_lp.ctypes.data_as(D),
+                                   None, x.ctypes.data_as(D), None, None) == 0
