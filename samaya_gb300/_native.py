@@ -10,7 +10,8 @@ import os
 import re
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "_lib", "libsamaya_gb300.so")
+# SAMAYA_GB300_LIB names another build of the library to load (a sanitizer build in tests).
+LIB_PATH = os.environ.get("SAMAYA_GB300_LIB") or os.path.join(_HERE, "_lib", "libsamaya_gb300.so")
 HEADER = os.path.join(_HERE, "..", "include", "sg_pdlp.h")
 
 c_double_p = ctypes.POINTER(ctypes.c_double)

@@ -46,11 +46,10 @@ def _digest(paths) -> str:
     return h.hexdigest()
 
 
-def _compile(src: str, flags) -> str:
-    obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
-    cmd = [nvcc_path(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-           "-Xcompiler", "-O2", "-I", os.path.join(HERE, "..", "include"), *flags, "-c", src,
-           "-o", obj]
+def _compile(src: str, flags, obj_dir: str = OBJ_DIR, opt=("-O3", "-Xcompiler", "-O2")) -> str:
+    obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
+    cmd = [nvcc_path(), *ARCH, opt[0], "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+           *opt[1:], "-I", os.path.join(HERE, "..", "include"), *flags, "-c", src, "-o", obj]
     if src.endswith(".cpp"):
         cmd = [nvcc_path(), "-x", "cu", *cmd[1:]]
     subprocess.run(cmd, check=True)
@@ -78,6 +77,22 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     if verbose:
         print("built", LIB_PATH)
     return LIB_PATH
+
+
+def build_sanitized(out_dir: str) -> str:
+    """The same library with AddressSanitizer in its host code (-O1, -g), linked into out_dir,
+    never in-tree: for tests that run the host-only entry points under the sanitizer (load it
+    with SAMAYA_GB300_LIB and the ASan runtime preloaded). Returns its path."""
+    obj_dir = os.path.join(out_dir, "obj")
+    os.makedirs(obj_dir, exist_ok=True)
+    san = ["-g", "-Xcompiler", "-fsanitize=address,-fno-omit-frame-pointer"]
+    srcs = _sources()
+    with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        objs = list(ex.map(lambda s: _compile(s, san, obj_dir, ("-O1",)), srcs))
+    path = os.path.join(out_dir, "libsamaya_gb300.so")
+    subprocess.run([nvcc_path(), *ARCH, "-shared", "-o", path, *objs, "-cudart", "static",
+                    "-lpthread", "-Xcompiler", "-fsanitize=address"], check=True)
+    return path
 
 
 if __name__ == "__main__":
