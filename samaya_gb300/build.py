@@ -80,18 +80,21 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
 
 
 def build_sanitized(out_dir: str) -> str:
-    """The same library with AddressSanitizer in its host code (-O1, -g), linked into out_dir,
-    never in-tree: for tests that run the host-only entry points under the sanitizer (load it
-    with SAMAYA_GB300_LIB and the ASan runtime preloaded). Returns its path."""
+    """The same library with AddressSanitizer and UBSan in its host code (-O1, -g), linked into
+    out_dir, never in-tree: for tests that run the host-only entry points under the sanitizers
+    (load it with SAMAYA_GB300_LIB and the sanitizer runtimes preloaded). Returns its path."""
     obj_dir = os.path.join(out_dir, "obj")
     os.makedirs(obj_dir, exist_ok=True)
-    san = ["-g", "-Xcompiler", "-fsanitize=address,-fno-omit-frame-pointer"]
+    san = ["-g", "-Xcompiler",
+           "-fsanitize=address,-fsanitize=undefined,-fno-sanitize-recover=all,"
+           "-fno-omit-frame-pointer"]
     srcs = _sources()
     with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, san, obj_dir, ("-O1",)), srcs))
     path = os.path.join(out_dir, "libsamaya_gb300.so")
     subprocess.run([nvcc_path(), *ARCH, "-shared", "-o", path, *objs, "-cudart", "static",
-                    "-lpthread", "-Xcompiler", "-fsanitize=address"], check=True)
+                    "-lpthread", "-Xcompiler", "-fsanitize=address,-fsanitize=undefined"],
+                   check=True)
     return path
 
 
