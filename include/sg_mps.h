@@ -1,12 +1,13 @@
 /* C ABI of the fast MPS reader (samaya_gb300).
  *
- * Reads a free-format MPS file into the arrays of samaya::Model (reference
+ * Reads an MPS file (free format, and fixed format where free MPS fails, as samaya's reader
+ * does) into the arrays of samaya::Model (reference
  * include/samaya/model.hpp:44-60) on several host threads: the drop-in for samaya::read_mps
  * (reference src/io/mps_reader.cpp:530-541, declared in include/samaya/io.hpp:27-28) and its C
  * form samaya_read_mps (src/core/c_api.cpp:37-45) on linear models, which the CLI's
  * `--lp-method pdlp --gpu model.mps` path reads first (apps/cli/main.cpp:335).
  *
- * The model is the one read_mps builds from free MPS, value for value: same number conversion
+ * The model is the one read_mps builds, value for value: same number conversion
  * (std::from_chars, one leading '+' allowed, |v| >= 1e30 infinite), same defaults and bound
  * rules, A summed as SparseMatrix::from_triplets sums it (rows sorted within a column, duplicate
  * entries added, exact zeros dropped) and checked as Model::validate checks it. Where three or
@@ -15,8 +16,8 @@
  *
  * What the reader does not read it declines, and the caller then calls samaya::read_mps:
  * SG_ERR_UNSUPPORTED for the quadratic sections (QUADOBJ, QMATRIX, QSECTION, QCMATRIX),
- * SG_ERR_PARSE for input that free MPS rejects (read_mps then tries fixed MPS, or reports its own
- * error), SG_ERR_IO when the file cannot be read. The message and line are in
+ * SG_ERR_PARSE for input that neither free nor fixed MPS reads (with the free reading's
+ * message and line, as read_mps reports it), SG_ERR_IO when the file cannot be read. The message and line are in
  * sg_pdlp_last_error(). Host only: no GPU is used or needed.
  */
 #ifndef SG_MPS_H
@@ -46,7 +47,7 @@ typedef struct sg_mps_info {
   int64_t col_name_bytes;   /* total length of the column names */
 } sg_mps_info;
 
-/* Reads the MPS file at path. threads: 0 picks the number of host threads from the file's size
+/* Reads the MPS file at path (free MPS; where that fails, fixed MPS). threads: 0 picks the number of host threads from the file's size
  * (at most the hardware's and 64); N > 0 cuts every section into N line-aligned ranges. */
 int sg_mps_read(const char* path, int threads, sg_mps** out);
 

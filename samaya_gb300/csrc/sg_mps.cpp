@@ -1,5 +1,6 @@
-// Fast reader of free-format MPS files: the Model that samaya::read_mps (reference
-// src/io/mps_reader.cpp) builds from free MPS, for linear models, read by several host threads.
+// Fast reader of MPS files: the Model that samaya::read_mps (reference src/io/mps_reader.cpp)
+// builds, for linear models, read by several host threads. Like samaya's reader it reads free MPS
+// first and, where that fails, fixed MPS (data fields in fixed columns, names with spaces).
 //
 // The text is cut at its section headers (lines that start with neither a blank nor '*'; found by
 // one parallel scan). Each section's data lines are cut into line-aligned byte ranges, one thread
@@ -22,8 +23,8 @@
 // unstable sort leaves them (two entries give the same sum either way).
 //
 // The quadratic sections (QUADOBJ, QMATRIX, QSECTION, QCMATRIX) are declined (kUnsupported), and
-// input that free MPS rejects is a kParseError, where read_mps would go on to try fixed MPS: in
-// both cases the caller hands the file to samaya's own reader.
+// input that neither free nor fixed MPS reads is a kParseError with the free reading's message
+// and line: in both cases the caller hands the file to samaya's own reader.
 #include "sg_mps.h"
 
 #include <fcntl.h>
@@ -120,6 +121,26 @@ inline void tokenize(const char* p, const char* e, Tokens& tk) {
     while (p < e && !blank(*p)) ++p;
     if (p > s) {
       if (tk.n < Tokens::kKept) tk.t[tk.n] = string_view(s, static_cast<size_t>(p - s));
+      ++tk.n;
+    }
+  }
+}
+
+// Fixed MPS (mps_reader.cpp:100-115): the data fields sit in columns 2-3, 5-12, 15-22, 25-36,
+// 40-47 and 50-61; each is trimmed of blanks and an empty one is skipped, which leaves the token
+// layout of free MPS. Names may then contain spaces.
+inline void tokenize_fixed(const char* p, const char* e, Tokens& tk) {
+  static constexpr size_t kStart[] = {1, 4, 14, 24, 39, 49};
+  static constexpr size_t kEnd[] = {3, 12, 22, 36, 47, 61};
+  const size_t len = static_cast<size_t>(e - p);
+  tk.n = 0;
+  for (size_t f = 0; f < 6 && kStart[f] < len; ++f) {
+    const char* a = p + kStart[f];
+    const char* b = p + std::min(kEnd[f], len);
+    while (a < b && blank(*a)) ++a;
+    while (b > a && blank(b[-1])) --b;
+    if (b > a) {
+      if (tk.n < Tokens::kKept) tk.t[tk.n] = string_view(a, static_cast<size_t>(b - a));
       ++tk.n;
     }
   }
@@ -404,7 +425,8 @@ class PhaseClock {
 
 class Reader {
  public:
-  Reader(const char* text, size_t len, int threads) : text_(text), len_(len) {
+  Reader(const char* text, size_t len, int threads, bool fixed)
+      : text_(text), len_(len), fixed_(fixed) {
     const unsigned hw = std::thread::hardware_concurrency();
     hw_threads_ = std::max(1, std::min(kMaxThreads, static_cast<int>(hw == 0 ? 1 : hw)));
     forced_ = threads > 0 ? std::min(threads, kMaxThreads) : 0;
@@ -473,13 +495,22 @@ class Reader {
     return cut;
   }
 
+  // The tokens of a data line, free or fixed.
+  void tokens(const char* p, const char* q, Tokens& tk) const {
+    if (fixed_) {
+      tokenize_fixed(p, q, tk);
+    } else {
+      tokenize(p, q, tk);
+    }
+  }
+
   // The column named by a COLUMNS line, or an empty view for a line that names none (empty,
   // comment, blanks only, a marker line).
-  static string_view column_of(const char* p, const char* q) {
+  string_view column_of(const char* p, const char* q) const {
     if (q > p && q[-1] == '\r') --q;
     if (p == q || *p == '*') return {};
     Tokens tk;
-    tokenize(p, q, tk);
+    tokens(p, q, tk);
     if (tk.n == 0 || (tk.n >= 3 && tk.t[1] == "'MARKER'")) return {};
     return tk.t[0];
   }
@@ -487,7 +518,7 @@ class Reader {
   // split_lines for a COLUMNS body, each cut moved on past the lines of the column it would split
   // (markers, comments and blank lines in between included), so that every run of consecutive
   // lines of one column lies in one range.
-  static std::vector<const char*> split_columns(const char* b, const char* e, int parts) {
+  std::vector<const char*> split_columns(const char* b, const char* e, int parts) const {
     std::vector<const char*> cut = split_lines(b, e, parts);
     for (int t = 1; t < parts; ++t) {
       const char* p = std::max(cut[t], cut[t - 1]);
@@ -544,7 +575,7 @@ class Reader {
     Tokens tk;
     for_lines(b, e, [&](const char* p, const char* q) {
       if (p == q || *p == '*') return true;
-      tokenize(p, q, tk);
+      tokens(p, q, tk);
       if (tk.n > 0) f(tk, p);
       return true;
     });
@@ -653,7 +684,7 @@ class Reader {
       Tokens tk;
       for_lines(cut[t], cut[t + 1], [&](const char* p, const char* q) {
         if (p == q || *p == '*') return true;
-        tokenize(p, q, tk);
+        tokens(p, q, tk);
         if (tk.n == 0) return true;
         if (tk.n < 2) return c.error.fail(p, "ROWS entry needs a type and a name");
         const string_view type = tk.t[0];
@@ -731,7 +762,7 @@ class Reader {
     c.objv.reserve(bytes / 40);
     for_lines(b, e, [&](const char* p, const char* q) {
       if (p == q || *p == '*') return true;
-      tokenize(p, q, tk);
+      tokens(p, q, tk);
       if (tk.n == 0) return true;
       if (tk.n >= 3 && tk.t[1] == "'MARKER'") {
         if (tk.t[2] == "'INTORG'") {
@@ -888,7 +919,7 @@ class Reader {
       int32_t last = -2;
       for_lines(cut[t], cut[t + 1], [&](const char* p, const char* q) {
         if (p == q || *p == '*') return true;
-        tokenize(p, q, tk);
+        tokens(p, q, tk);
         if (tk.n == 0) return true;
         const int first = tk.n % 2 == 1 ? 1 : 0;
         if (tk.n - first != 2 && tk.n - first != 4) {
@@ -952,7 +983,7 @@ class Reader {
       int32_t last = -2;
       for_lines(cut[t], cut[t + 1], [&](const char* p, const char* q) {
         if (p == q || *p == '*') return true;
-        tokenize(p, q, tk);
+        tokens(p, q, tk);
         if (tk.n == 0) return true;
         if (tk.n < 2) return c.error.fail(p, "BOUNDS entry is too short");
         const string_view type = tk.t[0];
@@ -1400,6 +1431,7 @@ class Reader {
 
   const char* text_;
   size_t len_;
+  bool fixed_;                        // data lines in fixed MPS (header lines are always free)
   const char* last_line_ = nullptr;  // the ENDATA line, once read
   PhaseClock clock_;
   int hw_threads_ = 1;
@@ -1448,8 +1480,21 @@ MpsStatus read_mps_text(const char* text, size_t len, int threads, MpsModel* out
     len = 0;
   }
   try {
+    // Free MPS first; where it fails, fixed MPS, and where that fails too, the free error
+    // (read_mps_from_string, mps_reader.cpp:515-527).
     MpsModel model;
-    Reader(text, len, threads).read(&model);
+    try {
+      Reader(text, len, threads, false).read(&model);
+    } catch (const Failure& free_error) {
+      if (free_error.status != MpsStatus::kParseError) throw;
+      try {
+        model = MpsModel();
+        Reader(text, len, threads, true).read(&model);
+      } catch (const Failure& fixed_error) {
+        if (fixed_error.status == MpsStatus::kParseError) throw free_error;
+        throw;
+      }
+    }
     *out = std::move(model);
     return MpsStatus::kOk;
   } catch (const Failure& f) {

@@ -1,11 +1,12 @@
 """MPS files for the PDLP path: the engine library's fast reader (include/sg_mps.h) and a
 free-MPS writer.
 
-``read_mps`` reads a free-format MPS file on several host threads into the arrays of
-samaya::Model, the model samaya::read_mps (reference src/io/mps_reader.cpp:530-541) builds from
-it. What the fast reader declines — the quadratic sections, input that free MPS rejects (fixed
-MPS among it), unreadable files — raises ``MpsReadError`` carrying the C status, and the caller
-falls back to samaya's own reader (the C++ binding does that, samaya_gb300/shim/read_mps_fast.cpp).
+``read_mps`` reads an MPS file (free MPS, and fixed MPS where free fails) on several host
+threads into the arrays of samaya::Model, the model samaya::read_mps (reference
+src/io/mps_reader.cpp:530-541) builds from it. What the fast reader declines — the quadratic
+sections, input that neither format reads, unreadable files — raises ``MpsReadError`` carrying
+the C status, and the caller falls back to samaya's own reader (the C++ binding does that,
+samaya_gb300/shim/read_mps_fast.cpp).
 
 ``write_mps`` writes a ``Model`` as free MPS (samaya has no writer): rows R<i>, columns C<j>,
 values by ``repr`` so that reading them back gives the same doubles.
@@ -141,8 +142,7 @@ def _finish(lib, rc, handle) -> MpsFile:
 
 
 def read_mps(path, threads: int = 0) -> MpsFile:
-    """Reads a free-format MPS file (threads: 0 = by the file's size; N = N ranges per
-    section)."""
+    """Reads an MPS file (threads: 0 = by the file's size; N = N ranges per section)."""
     lib = _lib()
     handle = ctypes.c_void_p()
     rc = lib.sg_mps_read(os.fsencode(path), int(threads), ctypes.byref(handle))

@@ -11,8 +11,8 @@
 
 namespace samaya_gb300 {
 
-// Reads an MPS file into the Model samaya::read_mps returns for it. Free MPS of linear models
-// goes through the fast reader; everything it declines (fixed MPS, the quadratic sections, an
+// Reads an MPS file into the Model samaya::read_mps returns for it. Linear models in free or
+// fixed MPS go through the fast reader; everything it declines (the quadratic sections, an
 // unreadable or invalid file) goes to samaya::read_mps, which then reads the file or throws its
 // own error. Threads: 0 picks them from the file's size.
 samaya::Model read_mps(const std::string& path, int threads = 0);

@@ -357,17 +357,48 @@ def _generated(kind: str, seed: int):
     return "\n".join(mps_lines(model, name=f"{kind}{seed}", col_integer=integer)) + "\n"
 
 
+def _fixed(t, a, b="", v="", c="", w=""):
+    """One fixed-MPS data line: type in columns 2-3, names in 5-12, 15-22 and 40-47, values in
+    25-36 and 50-61."""
+    s = " " + t.ljust(2) + " " + a.ljust(8) + "  " + b.ljust(8) + "  " + v.rjust(12)
+    if c:
+        s += "   " + c.ljust(8) + "  " + w.rjust(12)
+    return s.rstrip()
+
+
 def fixed_format_case() -> str:
     """Fixed MPS with a column name that contains a space (Netlib style): free MPS rejects it,
-    samaya's reader then reads it as fixed MPS."""
-    def f(t, a, b="", v="", c="", w=""):
-        s = " " + t.ljust(2) + " " + a.ljust(8) + "  " + b.ljust(8) + "  " + v.rjust(12)
-        if c:
-            s += "   " + c.ljust(8) + "  " + w.rjust(12)
-        return s.rstrip()
+    and it is read as fixed MPS."""
+    f = _fixed
     lines = ["NAME          FIXED", "ROWS", f("N", "COST"), f("L", "LIM1"), "COLUMNS",
              f("", "MY VAR", "COST", "1.", "LIM1", "1."), f("", "X2", "COST", "2.", "LIM1", "1."),
              "RHS", f("", "RHS", "LIM1", "4."), "ENDATA"]
+    return "\n".join(lines) + "\n"
+
+
+def fixed_format_full_case() -> str:
+    """Fixed MPS with every section: row and column names with spaces, two entries to a line,
+    set names, ranges, bound types, integer markers, OBJSENSE as a section."""
+    f = _fixed
+    lines = ["NAME          FULL FIXED", "OBJSENSE", "    MAX", "ROWS", f("N", "PROFIT"),
+             f("E", "BAL 1"), f("L", "CAP A"), f("G", "DEM B"), f("L", "R4"), "COLUMNS",
+             f("", "PROD 1", "PROFIT", "3.5", "BAL 1", "1."),
+             f("", "PROD 1", "CAP A", "2."),
+             f("", "PROD 2", "PROFIT", "-1.25", "DEM B", "1."),
+             f("", "PROD 2", "BAL 1", "-1.", "R4", "0.5"),
+             f("", "MARKER", "'MARKER'", "", "'INTORG'"),
+             f("", "INT X", "PROFIT", "2.", "CAP A", "1."),
+             f("", "INT X", "R4", "1."),
+             f("", "MARKER", "'MARKER'", "", "'INTEND'"),
+             f("", "SLACK", "DEM B", "1.", "R4", "-1."),
+             "RHS", f("", "RHS SET", "BAL 1", "0.", "CAP A", "10."),
+             f("", "RHS SET", "DEM B", "2.", "R4", "7.5"),
+             f("", "RHS SET", "PROFIT", "-4."),
+             "RANGES", f("", "RNG", "BAL 1", "3."), f("", "RNG", "R4", "-2."),
+             "BOUNDS", f("UP", "BND", "PROD 1", "4."), f("LO", "BND", "PROD 2", "-1."),
+             f("UP", "BND", "INT X", "6."), f("MI", "BND", "SLACK"),
+             f("UP", "BND", "SLACK", "-0.5"),
+             "ENDATA"]
     return "\n".join(lines) + "\n"
 
 
@@ -380,7 +411,8 @@ def accepted_cases():
              ("empty_model", EMPTY_MODEL), ("no_name_no_end", NO_NAME_NO_END),
              ("long_names", LONG_NAMES), ("rhs_last_wins", RHS_LAST_WINS),
              ("bound_forms", BOUND_FORMS), ("negative_upper", NEGATIVE_UPPER),
-             ("numbers", _numbers_case()), ("markers", _marker_case())]
+             ("numbers", _numbers_case()), ("markers", _marker_case()),
+             ("fixed_format", fixed_format_case()), ("fixed_format_full", fixed_format_full_case())]
     for kind, seeds in (("random", (1, 2)), ("transport", (3,)), ("powerlaw", (4,))):
         for seed in seeds:
             cases.append((f"{kind}_{seed}", _generated(kind, seed)))
@@ -447,7 +479,6 @@ def rejected_cases():
         ("unknown_sense", _edit("ROWS\n", "OBJSENSE\n    UP\nROWS\n"), "parse", "raises"),
         ("columns_before_rows", "NAME x\nCOLUMNS\n x r 1\nROWS\n N obj\n E r\nENDATA\n",
          "parse", "raises"),
-        ("fixed_format", fixed_format_case(), "parse", "reads"),
         ("quadobj", _edit("ENDATA", "QUADOBJ\n x x 2\n x y 1\nENDATA"), "unsupported",
          "reads"),
         ("qmatrix", _edit("ENDATA", "QMATRIX\n x x 2\nENDATA"), "unsupported", "reads"),

@@ -228,3 +228,81 @@ def test_mutated_texts_read_alike():
             assert want is not None, (seed, why)
             _assert_same(got, want, f"mutated seed {seed} threads {threads}")
 
+
+
+def _fixed_text(seed: int) -> str:
+    """A random fixed-MPS text: row and column names with spaces, one or two entries to a
+    line, set names, ranges, bound types, markers, values of up to 12 characters; now and then
+    a field out of place or an unknown name."""
+    from mps_cases import _fixed as f
+    rng = np.random.default_rng(20_000 + seed)
+    m, n = int(rng.integers(1, 8)), int(rng.integers(1, 12))
+    rows = [f"R {i}" for i in range(m)]
+    cols = [f"X {j}" if j % 2 else f"COL{j}" for j in range(n)]
+    kinds = ["E", "L", "G", "N"]
+
+    def val():
+        return f"{float(rng.standard_normal() * 10.0 ** int(rng.integers(-2, 3))):.6g}"[:12]
+    out = ["NAME          FIX" + str(seed)]
+    if rng.random() < 0.3:
+        out += ["OBJSENSE", "    MAX"]
+    out += ["ROWS", f("N", "OBJ")]
+    rk = {}
+    for r in rows:
+        rk[r] = kinds[int(rng.integers(0, 4))]
+        out.append(f(rk[r], r))
+    out.append("COLUMNS")
+    in_int = False
+    for c in cols:
+        if rng.random() < 0.2:
+            in_int = not in_int
+            out.append(f("", "MARKER", "'MARKER'", "", "'INTORG'" if in_int else "'INTEND'"))
+        targets = list(rng.permutation(rows + ["OBJ"]))[:int(rng.integers(1, 4))]
+        for k in range(0, len(targets), 2):
+            pair = targets[k:k + 2]
+            out.append(f("", c, pair[0], val(), *((pair[1], val()) if len(pair) > 1 else ())))
+    if in_int:
+        out.append(f("", "MARKER", "'MARKER'", "", "'INTEND'"))
+    out.append("RHS")
+    for r in rows + ["OBJ"]:
+        if rng.random() < 0.6:
+            out.append(f("", "RHS", r, val()))
+    if rng.random() < 0.5:
+        out.append("RANGES")
+        out += [f("", "RNG", r, val()) for r in rows if rk[r] != "N" and rng.random() < 0.4]
+    out.append("BOUNDS")
+    for c in cols:
+        t = ("UP", "LO", "FX", "MI", "PL", "BV", "FR")[int(rng.integers(0, 7))]
+        out.append(f(t, "BND", c, "" if t in ("MI", "PL", "BV", "FR") else val()))
+    out.append("ENDATA")
+    if rng.random() < 0.2:
+        i = int(rng.integers(1, len(out) - 1))
+        out[i] = out[i].replace("R 0", "R 9").replace("COL0", "COLX")
+    return "\n".join(out) + "\n"
+
+
+def test_fixed_format_texts_read_alike():
+    """Random fixed-MPS texts: the fast reader reads them as samaya's reader does (free MPS
+    first, then fixed), the same Model or the same refusal, at 1 and 4 threads."""
+    from oracle import ref
+    if not ref.available():
+        pytest.skip("the samaya checkout is not present")
+    ref.build()
+    read = 0
+    for seed in range(200):
+        text = _fixed_text(seed)
+        try:
+            want = ref.mps_read_text(text)
+        except ref.RefMpsError as e:
+            want, why = None, str(e)
+        for threads in (1, 4):
+            try:
+                got = _fast_dict(mps.read_mps_text(text, threads=threads))
+            except mps.MpsReadError as e:
+                assert want is None, (seed, str(e))
+                assert _line(str(e)) == _line(why), (seed, str(e), why)
+                continue
+            assert want is not None, (seed, why)
+            _assert_same(got, want, f"fixed seed {seed} threads {threads}")
+        read += want is not None
+    assert read > 100, read

@@ -179,7 +179,7 @@ def _read(exe, path):
 def test_read_mps_binding_gives_samayas_model(shim, tmp_path):
     """samaya_gb300::read_mps (the fast reader's binding) returns the Model samaya::read_mps
     returns, every field bit for bit, on the accepted MPS cases; what the fast reader declines
-    (fixed MPS, quadratic sections) goes to samaya's reader with the same result; on a file that
+    (the quadratic sections) goes to samaya's reader with the same result; on a file that
     neither reads, the binding throws samaya's error (exit status 3)."""
     import sys
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
