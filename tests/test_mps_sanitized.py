@@ -1,6 +1,6 @@
 """The fast MPS reader's host code under AddressSanitizer and UBSan (CPU test): sg_mps.cpp built
 with -fsanitize=address,undefined together with tests/c/mps_sanitize_driver.cpp and run on every
-case of tests/golden/mps_cases.py, the seeded random and byte-mutated texts of
+case of tests/golden/mps_cases.py, the seeded random, fixed-format and byte-mutated texts of
 test_mps_fuzz.py, and a generated power-law LP of 1.2M entries, each at 1, 3 and 7 threads. No
 sanitizer report, and the same status, sizes and checksum at every thread count."""
 from __future__ import annotations
@@ -23,7 +23,7 @@ def test_reader_is_clean_under_sanitizers(tmp_path):
     if shutil.which("g++") is None:
         pytest.skip("no C++ compiler")
     from mps_cases import accepted_cases, rejected_cases
-    from test_mps_fuzz import _mutated, _text
+    from test_mps_fuzz import _fixed_text, _mutated, _text
     from samaya_gb300 import generators as g
     from samaya_gb300.mps import write_mps
     exe = tmp_path / "mps_sanitize"
@@ -39,6 +39,7 @@ def test_reader_is_clean_under_sanitizers(tmp_path):
     texts = [t.encode() for _, t in accepted_cases()]
     texts += [case[1].encode() for case in rejected_cases()]
     texts += [_text(s).encode() for s in range(100)] + [_mutated(s) for s in range(300)]
+    texts += [_fixed_text(s).encode() for s in range(100)]
     paths = []
     for k, t in enumerate(texts):
         p = tmp_path / f"t{k}.mps"
