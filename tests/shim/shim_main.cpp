@@ -27,6 +27,12 @@
 // reads the file with the fast reader's binding (samaya_gb300/shim/read_mps_fast.cpp) and with
 // samaya::read_mps, compares every field of the two Models bit for bit and prints: same
 // fast_reads samaya_reads binding_seconds samaya_seconds.
+//
+//   shim_main --cli <model.mps> <tol>
+// the CLI's `--lp-method pdlp --gpu` chain with the fast reader: the model read by the binding,
+// then samaya's Solver with lp_method PDLP and use_gpu (solve_pdlp routed through the engine's
+// binding, as above); and the same with samaya::read_mps. Prints: same_bits status objective
+// verified fast_reads engine_solves cpu_solves.
 #include <dlfcn.h>
 
 #include <chrono>
@@ -136,6 +142,25 @@ int read_mode(const char* path) {
   return 0;
 }
 
+int cli_mode(const char* path, double tol) {
+  samaya::Params params;
+  params.log_level = 0;
+  params.lp_method = samaya::LpMethod::kPdlp;
+  params.use_gpu = true;
+  params.primal_feasibility_tol = tol;
+  params.dual_feasibility_tol = tol;
+  const samaya::Result a = samaya::Solver(params).solve(samaya_gb300::read_mps(path));
+  const samaya::Result b = samaya::Solver(params).solve(samaya::read_mps(path));
+  const bool same = a.status == b.status && same_bits(a.col_value, b.col_value) &&
+                    same_bits(a.row_dual, b.row_dual) &&
+                    std::memcmp(&a.objective, &b.objective, sizeof(double)) == 0;
+  const samaya_gb300::ShimCounts c = samaya_gb300::shim_counts();
+  std::printf("%d %d %.17g %d %lld %lld %lld\n", same ? 1 : 0, static_cast<int>(a.status),
+              a.objective, a.verified ? 1 : 0, samaya_gb300::read_counts().fast, c.engine,
+              c.cpu);
+  return 0;
+}
+
 }  // namespace
 
 namespace samaya {
@@ -152,6 +177,15 @@ PdlpResult solve_pdlp(const LpProblem& lp, const PdlpOptions& options, const Log
 }  // namespace samaya
 
 int main(int argc, char** argv) {
+  if (argc == 4 && std::strcmp(argv[1], "--cli") == 0) {
+    if (library_solve_pdlp() == nullptr) return 2;
+    try {
+      return cli_mode(argv[2], std::atof(argv[3]));
+    } catch (const std::exception& e) {
+      std::fprintf(stderr, "%s\n", e.what());
+      return 3;
+    }
+  }
   if (argc == 3 && std::strcmp(argv[1], "--read") == 0) {
     try {
       return read_mode(argv[2]);

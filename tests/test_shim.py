@@ -211,3 +211,23 @@ def test_read_mps_binding_on_the_transportation_lp(shim, tmp_path):
     r = _read(shim, path)
     assert r["same"] == 1 and r["fast"] == 1, r
     assert r["t_fast"] < 0.5 * r["t_own"], r
+
+
+def test_cli_chain_with_the_fast_reader(shim, tmp_path):
+    """The CLI's `--lp-method pdlp --gpu model.mps` chain with the fast reader's binding in
+    place of samaya::read_mps: samaya's Solver, with solve_pdlp routed through the engine's
+    binding (no GPU here: samaya's CPU PDLP), answers bit for bit as it does from samaya's own
+    reader, optimal and verified."""
+    from samaya_gb300 import generators as g
+    from samaya_gb300.mps import write_mps
+    for k, model in enumerate((g.random_sparse_lp(60, 150, seed=3),
+                               g.transportation_lp(8, 12, seed=4))):
+        path = tmp_path / f"lp{k}.mps"
+        write_mps(model, path)
+        env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+        p = subprocess.run([str(shim), "--cli", str(path), "1e-7"], capture_output=True,
+                           text=True, env=env, timeout=600)
+        assert p.returncode == 0, p.stderr
+        same, status, objective, verified, fast, engine, cpu = p.stdout.split()
+        assert same == "1" and status == str(SAMAYA_OPTIMAL) and verified == "1", p.stdout
+        assert fast == "1" and engine == "0" and int(cpu) >= 2, p.stdout
